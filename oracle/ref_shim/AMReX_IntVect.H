@@ -1,0 +1,2 @@
+// Forwarding header of the project-written AMReX stand-in.
+#include "mph_amrex_standin.H"
