@@ -1,0 +1,275 @@
+"""Benchmark of the lattice-Boltzmann step on one GB300 (N GPUs: replicas).
+
+Workload (default): the D3Q19 channel -- periodic in x and z, bounce-back
+(NoSlip) walls at y = 0 and y = Ny, Guo body force 1e-6 along x, tau = 0.6,
+rho = 1 + seeded uniform noise of amplitude 1e-4, u = 0 -- on a 512^3 grid
+(2 x 20.4 GB of FP64 populations, far larger than the 129 MB L2, so no L2
+flush is needed between steps).  One step = one advance() of the whole grid.
+
+Prints one JSON line (rank 0):
+  value     MLUPS with the populations resident in HBM (device-timed, CUDA
+            events on the step kernel's stream)
+  e2e       MLUPS through the C ABI with host buffers: every step uploads the
+            populations from pinned host memory, advances, downloads them
+  roofline  achieved HBM bandwidth of the step kernel (algorithmic bytes
+            2*Q*8 per cell update) against the measured copy peak
+  cpu_baseline  the CPU oracle (restated reference CPU path) on the host
+            cores, bounded sample of the same workload
+
+--impl reference: the reference's CPU implementation of the step (the CPU
+oracle, restated from the reference sources) on the host cores with all
+threads, on the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+LATTICE_Q = {"D2Q9": 9, "D3Q15": 15, "D3Q19": 19, "D3Q27": 27}
+ELEM = {"f64": 8, "f64_fast": 8, "f32": 4, "f16s": 2, "bf16s": 2}
+DTYPE = {"f64": "f64", "f64_fast": "f64", "f32": "f32", "f16s": "f16 storage / f32 arithmetic",
+         "bf16s": "bf16 storage / f32 arithmetic"}
+METRIC = "MLUPS"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(workload: str):
+    """Per-launch DRAM bytes of the step kernel from a committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as fh:
+            return json.load(fh).get(workload)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def channel_desc(m, n, precision, tau=0.6, F=1e-6):
+    faces = ["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic", "Periodic"]
+    return m.make_desc("D3Q19", n, 1.0 / tau, faces=faces, force=(F, 0.0, 0.0), precision=precision)
+
+
+def channel_fields(n, seed=20261203):
+    N = n[0] * n[1] * n[2]
+    rng = np.random.default_rng(seed)
+    return 1.0 + rng.uniform(-1e-4, 1e-4, N), np.zeros(3 * N)
+
+
+def cpu_reference(n, steps, warmup, threads):
+    """The restated reference CPU path on `threads` host threads: MLUPS."""
+    from oracle import oracle as O
+    O.build()
+    cfg = O.Config("D3Q19", n, omega=1.0 / 0.6, faces=["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic",
+                                                       "Periodic"], force=(1e-6, 0.0, 0.0))
+    sim = O.OracleSim(cfg, "port")
+    rho, u = channel_fields(n)
+    sim.init_fields(rho, u)
+    if warmup:
+        sim.step(warmup, threads)
+    t0 = time.perf_counter()
+    sim.step(steps, threads)
+    dt = time.perf_counter() - t0
+    cells = n[0] * n[1] * n[2]
+    return cells * steps / dt / 1e6, dt
+
+
+def run_reference(args):
+    from muphfasa_gb300 import replicas
+    rank, world, _ = replicas.rank_info()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    n = (256, 256, 256)
+    value, dt = cpu_reference(n, args.steps, args.warmup, threads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "MLUPS", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * dt / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"channel_d3q19_{args.n}^3", "lattice": "D3Q19", "grid": [args.n] * 3, "tau": 0.6,
+                   "force": 1e-6, "sample_grid": list(n), "parallelism": "replicas"},
+        "cpu_baseline": {"value": round(value, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
+                         "sample": f"{n[0]}^3 domain of the workload, {args.steps} steps after {args.warmup} warm-up, "
+                                   f"OpenMP over cells, {threads} threads"},
+        "e2e": {"value": round(value, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=512, help="cells per side of the channel")
+    ap.add_argument("--precision", default="f64_fast", choices=list(ELEM))
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import muphfasa_gb300 as m
+    from muphfasa_gb300 import replicas
+    rank, world, local = replicas.rank_info()
+    dist = replicas.init("nccl" if world > 1 else None)
+    import torch
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    m.set_device(local)
+
+    n = (args.n, args.n, args.n)
+    q = 19
+    cells = n[0] * n[1] * n[2]
+    workload = f"channel_d3q19_{args.n}^3_{args.precision}"
+    sim = m.Simulation(channel_desc(m, n, args.precision))
+    rho, u = channel_fields(n, seed=20261203 + rank)
+    sim.initialize(rho, u)
+    del rho, u
+    sim.advance(args.warmup)
+
+    dev = torch.device("cuda", local) if torch.cuda.is_available() else "cpu"
+    replicas.barrier(dist, dev)
+    with ClockSampler(local) as clk:
+        ms = sim.advance_timed(args.steps)  # CUDA events on the step kernels' stream
+    ms_max = replicas.max_over_ranks(dist, ms, dev)
+    total_cells = replicas.sum_over_ranks(dist, cells, dev)
+    value = total_cells * args.steps / (ms_max / 1e3) / 1e6
+    kernel_ms = ms / args.steps  # one step kernel per step
+    alg_bytes = 2 * q * ELEM[args.precision] * cells  # per launch
+    achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = ncu_traffic(workload)
+
+    # End to end through the C ABI with host buffers (pinned), every step:
+    # upload f, one advance, download f.
+    e2e = None
+    try:
+        f_host = torch.empty(q * cells, dtype=torch.float64, pin_memory=True).numpy()
+        sim.f(out=f_host)
+        sim.step_host(f_host, f_host, 1)  # warm-up of the path
+        replicas.barrier(dist, dev)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            sim.step_host(f_host, f_host, 1)
+        dt = time.perf_counter() - t0
+        dt = replicas.max_over_ranks(dist, dt, dev)
+        e2e = {"value": round(total_cells * args.e2e_steps / dt / 1e6, 3), "unit": "MLUPS",
+               "h2d_bytes_per_step": q * cells * 8, "d2h_bytes_per_step": q * cells * 8,
+               "steps": args.e2e_steps, "host_buffers": "pinned", "api": "mph_step_host"}
+        del f_host
+    except Exception as ex:  # report, do not hide
+        e2e = {"value": None, "unit": "MLUPS", "error": str(ex)[:200]}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        sn = (256, 256, 256)
+        v, dt = cpu_reference(sn, 20, 1, threads)
+        cpu = {"value": round(v, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
+               "sample": f"{sn[0]}^3 domain of the workload, 20 steps after 1 warm-up, FP64, OpenMP {threads} threads "
+                         f"({dt:.2f} s)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.precision], "data": "synthetic",
+            "config": {"workload": workload, "lattice": "D3Q19", "grid": list(n), "tau": 0.6, "force": 1e-6,
+                       "walls": "NoSlip at y=0 and y=Ny; periodic x, z", "precision": args.precision,
+                       "init": "rho = 1 + U(-1e-4, 1e-4) seeded, u = 0",
+                       "l2": "inputs larger than L2 (no flush needed)", "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "peak_kind": peak_kind, "bytes_per_cell_update": 2 * q * ELEM[args.precision]},
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": args.steps * sim.launches_per_step(),
+        }
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

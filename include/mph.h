@@ -1,0 +1,192 @@
+/* mph.h -- C ABI of the GB300-native lattice-Boltzmann time step.
+ *
+ * A drop-in for the stream-collide step of the reference solver (MuPhFASa):
+ * the same inputs file, lattices (D2Q9, D3Q15, D3Q19, D3Q27), BGK relaxation,
+ * Guo forcing and boundary types (NoSlip, MovingWall, Inflow, Outflow,
+ * PressureOutlet, Periodic), computed by hand-written sm_103a CUDA kernels on
+ * structure-of-arrays populations.
+ *
+ * Conventions
+ *   - Every entry point returns an int status (MPH_OK on success) and never
+ *     aborts the process; mph_last_error() gives the message of the calling
+ *     thread's last failure.  Where the reference calls amrex::Abort the
+ *     corresponding entry point returns MPH_ERR_CONFIG or MPH_ERR_PARSE.
+ *   - Host population arrays are "valid-cell SoA": f[n][k][j][i], i fastest,
+ *     population n slowest, exactly the component-last order of the
+ *     reference's FABs without their ghost layer (Collision.cpp:18-92 reads
+ *     fin(i,j,k,n)).  rho[k][j][i]; u[d][k][j][i].
+ *   - Faces are ordered xlo, xhi, ylo, yhi, zlo, zhi (faceIndex,
+ *     BoundaryConditions.H:37-39); a direction is periodic when its lo face is
+ *     Periodic (GeometryHandler.cpp:39-48).
+ *   - A simulation handle owns its device memory and one CUDA stream; calls
+ *     on one handle are synchronous and not thread-safe; separate handles are
+ *     independent.
+ */
+#ifndef MPH_H
+#define MPH_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPH_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define MPH_OK 0
+#define MPH_ERR_ARG 1          /* null pointer, bad size, bad enum value          */
+#define MPH_ERR_CONFIG 2       /* configuration the reference rejects (aborts)    */
+#define MPH_ERR_CUDA 3         /* CUDA runtime failure (message has the details)  */
+#define MPH_ERR_UNSUPPORTED 4  /* recognised but not implemented (TRT/MRT, EB)    */
+#define MPH_ERR_PARSE 5        /* inputs-file syntax, missing required key        */
+#define MPH_ERR_NONFINITE 6    /* a checked step found NaN/Inf populations        */
+#define MPH_ERR_STATE 7        /* call out of order (e.g. advance before init)    */
+
+/* ---- boundary types: the order of enum class lbmBCtype
+ *      (BoundaryConditions.H:41) ------------------------------------------- */
+#define MPH_BC_MOVING_WALL 0
+#define MPH_BC_NO_SLIP 1
+#define MPH_BC_INFLOW 2
+#define MPH_BC_OUTFLOW 3
+#define MPH_BC_PRESSURE_OUTLET 4
+#define MPH_BC_PERIODIC 5
+
+/* ---- storage / arithmetic of the populations ---------------------------- */
+/* FP64 storage, FP64 arithmetic in the reference's operation order: results
+ * are bit-identical to the reference CPU path. */
+#define MPH_PREC_F64 0
+/* FP64 storage and arithmetic, FMA-contracted and refactored: agrees with the
+ * reference to ~1e-15 per step (tested at 1e-12 after N steps). */
+#define MPH_PREC_F64_FAST 1
+/* FP32 storage and arithmetic. */
+#define MPH_PREC_F32 2
+/* f_i - w_i stored as FP16 / BF16, FP32 collide arithmetic. */
+#define MPH_PREC_F16S 3
+#define MPH_PREC_BF16S 4
+
+/* ---- lattice-unit description of one domain ---------------------------- */
+typedef struct {
+    int dim;               /* 2 or 3                                          */
+    int q;                 /* 9 (dim 2); 15, 19 or 27 (dim 3)                  */
+    int n[3];              /* valid cells per direction; n[2] = 1 for dim 2    */
+    double omega;          /* BGK relaxation frequency 1/tau                   */
+    int forced;            /* 1 selects the Guo-forced kernels                 */
+    double force[3];       /* body force, lattice units                        */
+    int face_type[6];      /* MPH_BC_* per face                                */
+    double face_rho[6];    /* face density (lattice units)                     */
+    double face_U[6][3];   /* face velocity (lattice units)                    */
+    int precision;         /* MPH_PREC_*                                       */
+} mph_desc;
+
+typedef struct {
+    int type;              /* MPH_BC_* after edge/corner priority resolution   */
+    double rho;
+    double U[3];
+} mph_resolved_bc;
+
+/* Scales derived by the unit converter (Units.cpp:20-183) and the run
+ * parameters of the driver loop (main.cpp:14-38, InputParser.cpp:92-323). */
+typedef struct {
+    double dx, dt, u_lat, nu_lat, tau, omega, Re, nu_phys;
+    double ref_length, ref_velocity, ref_density;
+    int max_step;
+    double stop_time;      /* physical; <= 0 means run to max_step            */
+    int plot_int, chk_int;
+} mph_run_info;
+
+const char* mph_last_error(void);
+int mph_abi_version(void);
+/* Selects the CUDA device used by handles created afterwards on the calling
+ * thread (the reference binds one device per MPI rank when AMReX initialises
+ * its GPU backend; here one process drives one device). */
+int mph_set_device(int device);
+
+/* ---- inputs file: InputParser / UnitConverter / buildBCManager ----------- */
+typedef struct mph_inputs mph_inputs;
+
+/* Parses a ParmParse-style inputs file followed by "key=value" overrides
+ * (amrex::Initialize(argc, argv); the last definition of a key wins).
+ * path may be NULL to start from the overrides alone. */
+int mph_inputs_load(const char* path, int noverrides, const char* const* overrides,
+                    mph_inputs** out);
+/* Same from an in-memory text. */
+int mph_inputs_parse_string(const char* text, int noverrides, const char* const* overrides,
+                            mph_inputs** out);
+void mph_inputs_free(mph_inputs* in);
+/* Raw value string of the last definition of `key` ("prefix.name");
+ * MPH_ERR_ARG when absent. */
+int mph_inputs_get(const mph_inputs* in, const char* key, char* buf, size_t buflen);
+/* The lattice-unit domain description and scales that SimulationImpl's
+ * constructor derives (SimulationSetup.cpp:32-89, 237-299). */
+int mph_inputs_derive(const mph_inputs* in, int precision, mph_desc* desc, mph_run_info* info);
+
+/* BCManager::finalize (BoundaryConditions.cpp:99-155): the 3^dim ghost-class
+ * table indexed by sum_d (code_d + 1) 3^d.  table must hold 27 entries. */
+int mph_resolve_bc(const mph_desc* desc, mph_resolved_bc* table);
+
+/* ---- simulation handle: the ISimulation surface (ISimulation.H:16-44) ---- */
+typedef struct mph_sim mph_sim;
+
+int mph_create(const mph_desc* desc, mph_sim** out);
+int mph_destroy(mph_sim* sim);
+/* Upload / download populations (host valid-cell SoA, FP64). */
+int mph_set_f(mph_sim* sim, const double* f);
+int mph_get_f(mph_sim* sim, double* f);
+/* setInitialConditions (SimulationSetup.cpp:201-219) from the given
+ * macroscopic fields (what initData produces) plus the ghost fill of
+ * initialize(); on the forced path rho/u are overwritten with the stored
+ * macroscopic fields, as the reference overwrites m_rho/m_vel. */
+int mph_init_fields(mph_sim* sim, double* rho, double* u);
+/* nsteps x SimulationImpl::advance() (SimulationSetup.cpp:120-139). */
+int mph_advance(mph_sim* sim, int nsteps);
+/* updateMacroscopic (SimulationSetup.cpp:142-166): (rho, u) of the streamed,
+ * pre-collision populations; u includes F/2 on the forced path. */
+int mph_update_macroscopic(mph_sim* sim, double* rho, double* u);
+/* FP64 sums of the stored populations: out[0] = sum f (mass),
+ * out[1..3] = sum c f (momentum). */
+int mph_reduce(mph_sim* sim, double* out);
+/* Lattice time (number of completed advance() calls since init). */
+int mph_time(const mph_sim* sim, double* t);
+/* Number of step-kernel launches one advance() issues. */
+int mph_launches_per_step(const mph_sim* sim, int* n);
+/* nsteps advances timed with CUDA events on the handle's own stream;
+ * *ms is the elapsed device time of the whole sequence. */
+int mph_advance_timed(mph_sim* sim, int nsteps, float* ms);
+/* Drop-in with host buffers: uploads f_in, advances nsteps, downloads the
+ * result into f_out (both host valid-cell SoA FP64; may alias). */
+int mph_step_host(mph_sim* sim, const double* f_in, double* f_out, int nsteps);
+
+/* ---- plugin level: caller-owned device memory in AMReX Array4 layout ----- */
+/* An Array4 view: element (i,j,k,n) lives at
+ *   p[(i-begin[0]) + (j-begin[1])*jstride + (k-begin[2])*kstride + n*nstride]. */
+typedef struct {
+    double* p;
+    long long jstride, kstride, nstride;
+    int begin[3];
+    int end[3];            /* exclusive */
+    int ncomp;
+} mph_array4;
+
+/* pullCollideFusedArr<L,BGK> (Collision.cpp:18-92) over the cells
+ * lo..hi (inclusive) of a ghost-grown fin; force NULL selects the unforced
+ * variant.  Reference arithmetic order (bit-exact).  stream may be NULL. */
+int mph_pull_collide_fused_arr(int dim, int q, const int lo[3], const int hi[3],
+                               const mph_array4* fin, const mph_array4* fout, double omega,
+                               const double* force, void* stream);
+/* MultiFab::FillBoundary(periodicity) for one box covering the whole domain
+ * dom_lo..dom_hi: ghost cells whose periodic image is valid receive all
+ * components of that image (SimulationSetup.cpp:227). */
+int mph_periodic_fill_arr(int dim, int q, const int dom_lo[3], const int dom_hi[3],
+                          const int periodic[3], const mph_array4* f, void* stream);
+/* BCManager<L>::operator() (BoundaryConditions.H:124-189) applied to every
+ * ghost cell of f outside the domain, with the resolved table of
+ * mph_resolve_bc. */
+int mph_bc_fill_arr(int dim, int q, const int dom_lo[3], const int dom_hi[3],
+                    const int periodic[3], const mph_resolved_bc* table, const mph_array4* f,
+                    void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPH_H */

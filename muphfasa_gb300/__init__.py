@@ -1,0 +1,291 @@
+"""muphfasa_gb300 -- GB300-native lattice-Boltzmann time step.
+
+Python binding of the C ABI in ``include/mph.h`` (the library itself is C++
+and sm_103a CUDA, built in-tree into ``muphfasa_gb300/_build/libmph.so``).
+The classes mirror the reference solver's host interface:
+
+* :class:`InputParser` -- the inputs file (ParmParse format, ``key=value``
+  overrides; reference src/IO/InputParser.cpp).
+* :func:`make_simulation` -- ``makeSimulation`` (SimulationFactory.cpp:36-60).
+* :class:`Simulation` -- ``ISimulation`` (ISimulation.H:16-44): ``initialize``,
+  ``advance``, ``update_macroscopic``, ``f``, ``rho``, ``vel``, ``time``,
+  ``omega``.
+
+There is no CPU fallback: if the compiled library is missing or no CUDA
+device is present the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libmph.so")
+
+MPH_OK = 0
+ERRORS = {1: "MPH_ERR_ARG", 2: "MPH_ERR_CONFIG", 3: "MPH_ERR_CUDA", 4: "MPH_ERR_UNSUPPORTED",
+          5: "MPH_ERR_PARSE", 6: "MPH_ERR_NONFINITE", 7: "MPH_ERR_STATE"}
+BC = {"MovingWall": 0, "NoSlip": 1, "Inflow": 2, "Outflow": 3, "PressureOutlet": 4, "Periodic": 5}
+PRECISION = {"f64": 0, "f64_fast": 1, "f32": 2, "f16s": 3, "bf16s": 4}
+LATTICE_DQ = {"D2Q9": (2, 9), "D3Q15": (3, 15), "D3Q19": (3, 19), "D3Q27": (3, 27)}
+
+# Exported entry points (the declarations of include/mph.h).
+EXPORTS = [
+    "mph_last_error", "mph_abi_version", "mph_set_device", "mph_inputs_load", "mph_inputs_parse_string", "mph_inputs_free",
+    "mph_inputs_get", "mph_inputs_derive", "mph_resolve_bc", "mph_create", "mph_destroy", "mph_set_f",
+    "mph_get_f", "mph_init_fields", "mph_advance", "mph_update_macroscopic", "mph_reduce", "mph_time",
+    "mph_launches_per_step", "mph_advance_timed", "mph_step_host", "mph_pull_collide_fused_arr",
+    "mph_periodic_fill_arr", "mph_bc_fill_arr",
+]
+
+
+class MphError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Desc(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int), ("q", C.c_int), ("n", C.c_int * 3), ("omega", C.c_double), ("forced", C.c_int),
+        ("force", C.c_double * 3), ("face_type", C.c_int * 6), ("face_rho", C.c_double * 6),
+        ("face_U", (C.c_double * 3) * 6), ("precision", C.c_int),
+    ]
+
+
+class ResolvedBC(C.Structure):
+    _fields_ = [("type", C.c_int), ("rho", C.c_double), ("U", C.c_double * 3)]
+
+
+class RunInfo(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("dx", "dt", "u_lat", "nu_lat", "tau", "omega", "Re", "nu_phys",
+                                           "ref_length", "ref_velocity", "ref_density")] + [
+        ("max_step", C.c_int), ("stop_time", C.c_double), ("plot_int", C.c_int), ("chk_int", C.c_int)]
+
+
+class Array4(C.Structure):
+    _fields_ = [("p", C.c_void_p), ("jstride", C.c_longlong), ("kstride", C.c_longlong),
+                ("nstride", C.c_longlong), ("begin", C.c_int * 3), ("end", C.c_int * 3), ("ncomp", C.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libmph.so (building it first if only the sources are present)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        from . import build as _build
+        _build.build()
+    L = C.CDLL(LIB_PATH)
+    P, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)
+    L.mph_last_error.restype = C.c_char_p
+    L.mph_abi_version.restype = C.c_int
+    L.mph_set_device.argtypes = [C.c_int]
+    L.mph_inputs_load.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(P)]
+    L.mph_inputs_parse_string.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(P)]
+    L.mph_inputs_free.argtypes = [P]
+    L.mph_inputs_free.restype = None
+    L.mph_inputs_get.argtypes = [P, C.c_char_p, C.c_char_p, C.c_size_t]
+    L.mph_inputs_derive.argtypes = [P, C.c_int, C.POINTER(Desc), C.POINTER(RunInfo)]
+    L.mph_resolve_bc.argtypes = [C.POINTER(Desc), C.POINTER(ResolvedBC)]
+    L.mph_create.argtypes = [C.POINTER(Desc), C.POINTER(P)]
+    L.mph_destroy.argtypes = [P]
+    L.mph_set_f.argtypes = [P, dp]
+    L.mph_get_f.argtypes = [P, dp]
+    L.mph_init_fields.argtypes = [P, dp, dp]
+    L.mph_advance.argtypes = [P, C.c_int]
+    L.mph_update_macroscopic.argtypes = [P, dp, dp]
+    L.mph_reduce.argtypes = [P, dp]
+    L.mph_time.argtypes = [P, dp]
+    L.mph_launches_per_step.argtypes = [P, ip]
+    L.mph_advance_timed.argtypes = [P, C.c_int, C.POINTER(C.c_float)]
+    L.mph_step_host.argtypes = [P, dp, dp, C.c_int]
+    L.mph_pull_collide_fused_arr.argtypes = [C.c_int, C.c_int, ip, ip, C.POINTER(Array4), C.POINTER(Array4),
+                                             C.c_double, dp, P]
+    L.mph_periodic_fill_arr.argtypes = [C.c_int, C.c_int, ip, ip, ip, C.POINTER(Array4), P]
+    L.mph_bc_fill_arr.argtypes = [C.c_int, C.c_int, ip, ip, ip, C.POINTER(ResolvedBC), C.POINTER(Array4), P]
+    _lib = L
+    return L
+
+
+def check(rc: int):
+    if rc != MPH_OK:
+        raise MphError(rc, lib().mph_last_error().decode(errors="replace"))
+
+
+def _dp(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def make_desc(lattice: str, n, omega: float, faces=None, face_rho=None, face_U=None, force=None,
+              precision: str = "f64") -> Desc:
+    """A lattice-unit domain description (what SimulationImpl's constructor derives)."""
+    dim, q = LATTICE_DQ[lattice]
+    d = Desc()
+    d.dim, d.q = dim, q
+    nn = list(n) + [1] * (3 - len(n))
+    for i in range(3):
+        d.n[i] = int(nn[i])
+    d.omega = float(omega)
+    d.forced = 1 if force is not None else 0
+    F = list(force or (0.0, 0.0, 0.0)) + [0.0] * 3
+    for i in range(3):
+        d.force[i] = float(F[i])
+    faces = faces or ["Periodic"] * 6
+    face_rho = face_rho or [1.0] * 6
+    face_U = face_U or [[0.0, 0.0, 0.0]] * 6
+    for i in range(6):
+        d.face_type[i] = BC[faces[i]] if isinstance(faces[i], str) else int(faces[i])
+        d.face_rho[i] = float(face_rho[i])
+        for c in range(3):
+            d.face_U[i][c] = float(face_U[i][c])
+    d.precision = PRECISION[precision] if isinstance(precision, str) else int(precision)
+    return d
+
+
+def set_device(device: int):
+    """Device for handles created afterwards on this thread (one per rank)."""
+    check(lib().mph_set_device(int(device)))
+
+
+def resolve_bc(desc: Desc):
+    tab = (ResolvedBC * 27)()
+    check(lib().mph_resolve_bc(C.byref(desc), tab))
+    return [(t.type, t.rho, tuple(t.U)) for t in tab]
+
+
+class InputParser:
+    """An inputs file plus ``key=value`` overrides (amrex::Initialize(argc, argv))."""
+
+    def __init__(self, path: str | None = None, overrides=(), text: str | None = None):
+        L = lib()
+        arr = (C.c_char_p * max(1, len(overrides)))(*[o.encode() for o in overrides])
+        h = C.c_void_p()
+        if text is not None:
+            check(L.mph_inputs_parse_string(text.encode(), len(overrides), arr, C.byref(h)))
+        else:
+            check(L.mph_inputs_load(path.encode() if path else None, len(overrides), arr, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib().mph_inputs_free(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def get(self, key: str) -> str | None:
+        buf = C.create_string_buffer(4096)
+        rc = lib().mph_inputs_get(self._h, key.encode(), buf, 4096)
+        return buf.value.decode() if rc == MPH_OK else None
+
+    def derive(self, precision: str = "f64"):
+        d, info = Desc(), RunInfo()
+        p = PRECISION[precision] if isinstance(precision, str) else int(precision)
+        check(lib().mph_inputs_derive(self._h, p, C.byref(d), C.byref(info)))
+        return d, info
+
+
+class Simulation:
+    """Device-resident domain advanced by the sm_103a kernels (the ISimulation surface)."""
+
+    def __init__(self, desc: Desc, info: RunInfo | None = None):
+        self.desc = desc
+        self.info = info
+        self.dim, self.q = desc.dim, desc.q
+        self.shape = (desc.n[2], desc.n[1], desc.n[0]) if desc.dim == 3 else (desc.n[1], desc.n[0])
+        self.ncell = int(np.prod(self.shape))
+        h = C.c_void_p()
+        check(lib().mph_create(C.byref(desc), C.byref(h)))
+        self._h = h
+        self._rho = np.ones(self.ncell)
+        self._vel = np.zeros(self.dim * self.ncell)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- lifecycle ---------------------------------------------------------
+    def initialize(self, rho=None, u=None):
+        """setInitialConditions from (rho, u) (quiescent by default, InitData.cpp:8-15)."""
+        rho = np.ones(self.ncell) if rho is None else np.ascontiguousarray(rho, dtype=np.float64).reshape(-1).copy()
+        u = np.zeros(self.dim * self.ncell) if u is None else np.ascontiguousarray(u, dtype=np.float64).reshape(-1).copy()
+        assert rho.size == self.ncell and u.size == self.dim * self.ncell
+        check(lib().mph_init_fields(self._h, _dp(rho), _dp(u)))
+        self._rho, self._vel = rho, u
+        return rho, u
+
+    def advance(self, nsteps: int = 1):
+        check(lib().mph_advance(self._h, int(nsteps)))
+
+    def advance_timed(self, nsteps: int) -> float:
+        ms = C.c_float()
+        check(lib().mph_advance_timed(self._h, int(nsteps), C.byref(ms)))
+        return float(ms.value)
+
+    def step_host(self, f_in: np.ndarray, f_out: np.ndarray, nsteps: int = 1):
+        check(lib().mph_step_host(self._h, _dp(f_in), _dp(f_out), int(nsteps)))
+
+    def update_macroscopic(self):
+        rho = np.empty(self.ncell)
+        u = np.empty(self.dim * self.ncell)
+        check(lib().mph_update_macroscopic(self._h, _dp(rho), _dp(u)))
+        self._rho, self._vel = rho, u
+        return rho, u
+
+    # -- state -------------------------------------------------------------
+    def set_f(self, f: np.ndarray):
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        assert f.size == self.q * self.ncell
+        check(lib().mph_set_f(self._h, _dp(f)))
+
+    def f(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.q * self.ncell)
+        assert out.size == self.q * self.ncell
+        check(lib().mph_get_f(self._h, _dp(out)))
+        return out
+
+    def rho(self):
+        return self._rho
+
+    def vel(self):
+        return self._vel
+
+    def reduce(self):
+        out = np.zeros(4)
+        check(lib().mph_reduce(self._h, _dp(out)))
+        return out
+
+    def time(self) -> float:
+        t = C.c_double()
+        check(lib().mph_time(self._h, C.byref(t)))
+        return t.value
+
+    def omega(self) -> float:
+        return self.desc.omega
+
+    def launches_per_step(self) -> int:
+        n = C.c_int()
+        check(lib().mph_launches_per_step(self._h, C.byref(n)))
+        return n.value
+
+
+def make_simulation(inputs: InputParser, precision: str = "f64") -> Simulation:
+    """makeSimulation (SimulationFactory.cpp:36-60): lattice/collision dispatch from the inputs."""
+    d, info = inputs.derive(precision)
+    return Simulation(d, info)

@@ -1,0 +1,31 @@
+// k_fast_common.cuh -- launcher template of the refactored (FMA) step
+// kernels, instantiated per storage precision by k_fast_*.cu.
+#pragma once
+
+#include "lbm_launch.h"
+
+namespace mph {
+
+template <class St>
+cudaError_t launch_step_fast(int q, bool forced, const void* fin, void* fout, const KParams& p, const KParams* pg,
+                             cudaStream_t s) {
+    dim3 g, b;
+    step_shape(p, g, b);
+    auto in = static_cast<const typename St::T*>(fin);
+    auto out = static_cast<typename St::T*>(fout);
+#define MPH_FAST_CASE(QQ)                                                              \
+    case QQ:                                                                           \
+        if (forced) k_step<QQ, St, kFast, true><<<g, b, 0, s>>>(in, out, p, pg);      \
+        else k_step<QQ, St, kFast, false><<<g, b, 0, s>>>(in, out, p, pg);            \
+        return cudaGetLastError();
+    switch (q) {
+        MPH_FAST_CASE(9)
+        MPH_FAST_CASE(15)
+        MPH_FAST_CASE(19)
+        MPH_FAST_CASE(27)
+    }
+#undef MPH_FAST_CASE
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace mph

@@ -1,0 +1,481 @@
+// lbm_kernels.cuh -- device code of the fused lattice-Boltzmann step.
+//
+// One thread owns one cell.  A step pulls the Q populations that stream into
+// the cell (f_in(x - c_n, n), Streaming.H:20-35), takes the moments, relaxes
+// towards equilibrium (BGK, with the Guo force term when forced) and writes Q
+// populations: 2*Q*sizeof(T) bytes of HBM traffic per cell update, no ghost
+// layer.  Boundaries are applied link-wise inside the pull: a population
+// whose upstream cell g = x - c_n lies outside the domain in a non-periodic
+// direction takes the value that the reference's ghost fill would have
+// written at g (BCManager<L>::operator(), BoundaryConditions.H:124-189), and
+// that value depends only on the post-collision populations of x itself
+// because the ghost-fill source cell is g + c_n = x.  Periodic directions
+// wrap the index, which equals the reference's FillBoundary copy.
+//
+// Two arithmetic modes share the pull:
+//   kExact -- the reference's floating-point operation order (Collision.cpp
+//             :18-92, Macroscopic.H, Equilibrium.H:28-57, Collision.H:21-76);
+//             compiled in a translation unit with --fmad=false it reproduces
+//             the reference's FP64 results bit for bit.
+//   kFast  -- algebraically refactored, FMA-contracted arithmetic (pair
+//             sums for the moments, one reciprocal, shared quadratic terms)
+//             in the compute type R of the storage policy.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "lattice.cuh"
+
+namespace mph {
+
+enum { kBcMoving = 0, kBcNoSlip = 1, kBcInflow = 2, kBcOutflow = 3, kBcPressure = 4, kBcPeriodic = 5 };
+enum { kExact = 0, kFast = 1 };
+
+// Per-domain constants passed by value to every kernel.
+struct KParams {
+    int nx, ny, nz;
+    int periodic[3];
+    long long ncell;      // nx*ny*nz: stride between populations
+    double omega, omc;    // omega and 1 - omega (BGK::collide, Collision.H:68-76)
+    double F[3], hF[3];   // body force and 0.5*F (Macroscopic.H:241-278)
+    double gpref[27];     // ((1 - 0.5 omega) w_n) cs2inv  (guoForceTerm prefactor)
+    double gcF[27];       // c_n . F                         (guoForceTerm)
+    int bc_type[27];      // resolved ghost-class table (BCManager::finalize)
+    double bc_rho[27];
+    double bc_U[27][3];
+};
+
+// ---------------------------------------------------------------------------
+// Storage policies: how a population is kept in HBM and the compute type R.
+// ---------------------------------------------------------------------------
+struct StF64 {
+    using T = double;
+    using R = double;
+    template <int Q> static __device__ __forceinline__ R ld(const T* __restrict__ f, int n, long long i, long long N) {
+        return __ldg(f + n * N + i);
+    }
+    template <int Q> static __device__ __forceinline__ void st(T* __restrict__ f, int n, long long i, long long N, R v) {
+        f[n * N + i] = v;
+    }
+};
+struct StF32 {
+    using T = float;
+    using R = float;
+    template <int Q> static __device__ __forceinline__ R ld(const T* __restrict__ f, int n, long long i, long long N) {
+        return __ldg(f + n * N + i);
+    }
+    template <int Q> static __device__ __forceinline__ void st(T* __restrict__ f, int n, long long i, long long N, R v) {
+        f[n * N + i] = v;
+    }
+};
+// Shifted 16-bit storage: the deviation f_n - w_n is stored, so that the
+// 11 (FP16) or 8 (BF16) significant bits resolve the small departure from the
+// rest state instead of the O(w) value itself.
+struct StF16S {
+    using T = __half;
+    using R = float;
+    template <int Q> static __device__ __forceinline__ R ld(const T* __restrict__ f, int n, long long i, long long N) {
+        return __half2float(f[n * N + i]) + (float)Lat<Q>::w(n);
+    }
+    template <int Q> static __device__ __forceinline__ void st(T* __restrict__ f, int n, long long i, long long N, R v) {
+        f[n * N + i] = __float2half_rn(v - (float)Lat<Q>::w(n));
+    }
+};
+struct StBF16S {
+    using T = __nv_bfloat16;
+    using R = float;
+    template <int Q> static __device__ __forceinline__ R ld(const T* __restrict__ f, int n, long long i, long long N) {
+        return __bfloat162float(f[n * N + i]) + (float)Lat<Q>::w(n);
+    }
+    template <int Q> static __device__ __forceinline__ void st(T* __restrict__ f, int n, long long i, long long N, R v) {
+        f[n * N + i] = __float2bfloat16_rn(v - (float)Lat<Q>::w(n));
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Pull with link-wise boundary conditions.
+// ---------------------------------------------------------------------------
+
+// Value the reference's ghost fill stores at ghost g = x - c_n for population
+// n, evaluated from the populations of x itself (the ghost-fill source cell
+// g + c_n is x):
+//   BounceBack family (BCTypes/BounceBack.H:36-63; NoSlip with rho=1, U=0,
+//   NoSlipKernel.H:20-28; MovingWall, Inflow with the resolved rho, U):
+//       f(x, opp n) + (((-2 rho) w_opp) (c_opp . U)) cs2inv
+//   Outflow (OutflowKernel.H:26-38):           f(x, n)
+//   PressureOutlet (PressureOutletKernel.H:29-64):
+//       -f(x, opp n) + 2 w_n rho_out (1 + 0.5 cu^2 cs2inv^2 - 0.5 uu cs2inv)
+// Rare path: reads its constants from the global copy pg of the parameters.
+template <int Q, class St>
+__device__ __noinline__ typename St::R boundary_value(const KParams* __restrict__ pg, int n, int cls,
+                                                      const typename St::T* __restrict__ fin, long long c) {
+    using L = Lat<Q>;
+    using R = typename St::R;
+    const long long N = pg->ncell;
+    const int t = pg->bc_type[cls];
+    const int o = L::opp(n);
+    if (t == kBcOutflow) return St::template ld<Q>(fin, n, c, N);
+    if (t == kBcPressure) {
+        R rho = R(0.0), j0 = R(0.0), j1 = R(0.0), j2 = R(0.0);
+#pragma unroll
+        for (int m = 0; m < Q; ++m) {
+            const R fm = St::template ld<Q>(fin, m, c, N);
+            rho += fm;
+            j0 += (R)L::cx(m) * fm;
+            j1 += (R)L::cy(m) * fm;
+            if (L::D == 3) j2 += (R)L::cz(m) * fm;
+        }
+        const R inv_rho = R(1.0) / rho;
+        R cu, uu;
+        if (L::D == 2) {
+            cu = ((R)L::cx(n) * j0 + (R)L::cy(n) * j1) * inv_rho;
+            uu = (j0 * j0 + j1 * j1) * inv_rho * inv_rho;
+        } else {
+            cu = ((R)L::cx(n) * j0 + (R)L::cy(n) * j1 + (R)L::cz(n) * j2) * inv_rho;
+            uu = (j0 * j0 + j1 * j1 + j2 * j2) * inv_rho * inv_rho;
+        }
+        const R rho_out = (R)pg->bc_rho[cls];
+        const R feq_even = (R)L::w(n) * rho_out *
+                           (R(1.0) + R(0.5) * cu * cu * R(3.0) * R(3.0) - R(0.5) * uu * R(3.0));
+        return -St::template ld<Q>(fin, o, c, N) + R(2.0) * feq_even;
+    }
+    if (t == kBcPeriodic) return R(__longlong_as_double(0x7ff8000000000000ULL));  // unreachable
+    R rho = R(1), U0 = R(0.), U1 = R(0.), U2 = R(0.);
+    if (t != kBcNoSlip) {
+        rho = (R)pg->bc_rho[cls];
+        U0 = (R)pg->bc_U[cls][0];
+        U1 = (R)pg->bc_U[cls][1];
+        U2 = (R)pg->bc_U[cls][2];
+    }
+    R cdotu;
+    if (L::D == 2) cdotu = (R)L::cx(o) * U0 + (R)L::cy(o) * U1;
+    else cdotu = (R)L::cx(o) * U0 + (R)L::cy(o) * U1 + (R)L::cz(o) * U2;
+    const R contrib = R(-2.) * rho * (R)L::w(o) * cdotu * R(3.0);
+    return St::template ld<Q>(fin, o, c, N) + contrib;
+}
+
+// Pull of a cell next to the domain boundary: periodic wrap, or the link-wise
+// boundary value for ghosts outside a non-periodic face.
+template <int Q, class St>
+__device__ __forceinline__ void pull_edge(const KParams& p, const KParams* __restrict__ pg,
+                                          const typename St::T* __restrict__ fin, int x, int y, int z, long long c,
+                                          typename St::R* f) {
+    using L = Lat<Q>;
+#pragma unroll
+    for (int n = 0; n < Q; ++n) {
+        int gx = x - L::cx(n), gy = y - L::cy(n), gz = z - L::cz(n);
+        int k0 = 0, k1 = 0, k2 = 0;
+        if (gx < 0) { if (p.periodic[0]) gx += p.nx; else k0 = -1; }
+        else if (gx >= p.nx) { if (p.periodic[0]) gx -= p.nx; else k0 = 1; }
+        if (gy < 0) { if (p.periodic[1]) gy += p.ny; else k1 = -1; }
+        else if (gy >= p.ny) { if (p.periodic[1]) gy -= p.ny; else k1 = 1; }
+        if (L::D == 3) {
+            if (gz < 0) { if (p.periodic[2]) gz += p.nz; else k2 = -1; }
+            else if (gz >= p.nz) { if (p.periodic[2]) gz -= p.nz; else k2 = 1; }
+        }
+        if ((k0 | k1 | k2) == 0) {
+            f[n] = St::template ld<Q>(fin, n, ((long long)gz * p.ny + gy) * p.nx + gx, p.ncell);
+        } else {
+            const int cls = (k0 + 1) + 3 * (k1 + 1) + (L::D == 3 ? 9 * (k2 + 1) : 0);
+            f[n] = boundary_value<Q, St>(pg, n, cls, fin, c);
+        }
+    }
+}
+
+template <int Q, class St>
+__device__ __forceinline__ void pull(const KParams& p, const KParams* __restrict__ pg,
+                                     const typename St::T* __restrict__ fin, int x, int y, int z, long long c,
+                                     typename St::R* f) {
+    using L = Lat<Q>;
+    const bool interior = x > 0 && x < p.nx - 1 && y > 0 && y < p.ny - 1 && (L::D == 2 || (z > 0 && z < p.nz - 1));
+    if (interior) {
+        const long long plane = (long long)p.nx * p.ny;
+#pragma unroll
+        for (int n = 0; n < Q; ++n)
+            f[n] = St::template ld<Q>(fin, n, c - (L::cx(n) + (long long)L::cy(n) * p.nx + L::cz(n) * plane), p.ncell);
+    } else {
+        pull_edge<Q, St>(p, pg, fin, x, y, z, c, f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Moments and collision.
+// ---------------------------------------------------------------------------
+
+// rho = sum f and u = (sum c f [+ F/2]) / rho in the reference's order
+// (Macroscopic.H:36-45, 158-204, 226-278).  Terms with c = 0 are skipped and
+// c = -1 terms are subtracted: the running sums start at +0 and never become
+// -0, so this is bit-identical to adding c*f.
+template <int Q, bool FORCED>
+__device__ __forceinline__ void moments_exact(const KParams& p, const double* f, double& rho, double* u) {
+    using L = Lat<Q>;
+    rho = 0.;
+#pragma unroll
+    for (int n = 0; n < Q; ++n) rho += f[n];
+    double ux = 0., uy = 0., uz = 0.;
+#pragma unroll
+    for (int n = 0; n < Q; ++n) {
+        if (L::cx(n) == 1) ux += f[n];
+        else if (L::cx(n) == -1) ux -= f[n];
+        if (L::cy(n) == 1) uy += f[n];
+        else if (L::cy(n) == -1) uy -= f[n];
+        if (L::D == 3) {
+            if (L::cz(n) == 1) uz += f[n];
+            else if (L::cz(n) == -1) uz -= f[n];
+        }
+    }
+    if (!FORCED) {
+        u[0] = ux / rho;
+        u[1] = uy / rho;
+        u[2] = (L::D == 3) ? uz / rho : 0.0;
+    } else {
+        u[0] = (ux + p.hF[0]) / rho;
+        u[1] = (uy + p.hF[1]) / rho;
+        u[2] = (L::D == 3) ? (uz + p.hF[2]) / rho : 0.0;
+    }
+}
+
+// c_n . u with the reference's left-to-right sum; zero components dropped
+// (bit-identical: cu only enters through 1 + 3 cu, cu^2 and 3 cu * cF).
+template <int Q, class R>
+__device__ __forceinline__ R cdot(int n, const R* u) {
+    using L = Lat<Q>;
+    R s = R(0);
+    bool first = true;
+    const int c[3] = {L::cx(n), L::cy(n), L::cz(n)};
+#pragma unroll
+    for (int d = 0; d < L::D; ++d) {
+        if (c[d] == 0) continue;
+        if (first) { s = (c[d] > 0) ? u[d] : -u[d]; first = false; }
+        else s = (c[d] > 0) ? s + u[d] : s - u[d];
+    }
+    return s;
+}
+
+// Equilibrium (Equilibrium.H:28-57) + BGK (Collision.H:68-76) + Guo
+// (Collision.H:21-65), reference operation order, in place on f.
+template <int Q, bool FORCED>
+__device__ __forceinline__ void collide_exact(const KParams& p, double* f) {
+    using L = Lat<Q>;
+    double rho, u[3];
+    moments_exact<Q, FORCED>(p, f, rho, u);
+    const double usq = (L::D == 2) ? u[0] * u[0] + u[1] * u[1] : u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+    const double s = 1.5 * usq;  // 0.5 * cs2inv * u_sq
+    double udotF = 0.0;
+    if (FORCED) udotF = (L::D == 2) ? u[0] * p.F[0] + u[1] * p.F[1] : u[0] * p.F[0] + u[1] * p.F[1] + u[2] * p.F[2];
+    const double omega = p.omega, omc = p.omc;
+    {   // rest population: c = 0, so 1 + 3 cu + 4.5 cu^2 = 1 exactly
+        const double feq = L::w(0) * rho * (1.0 - s);
+        double o = omc * f[0] + omega * feq;
+        if (FORCED) o = o + p.gpref[0] * ((p.gcF[0] + 0.0 * p.gcF[0]) - udotF);
+        f[0] = o;
+    }
+#pragma unroll
+    for (int n = 1; n < Q; ++n) {
+        const int m = L::opp(n);
+        if (m < n) continue;
+        const double cu = cdot<Q, double>(n, u);
+        const double t3 = 3.0 * cu;
+        const double sq = 4.5 * cu * cu;
+        const double wr = L::w(n) * rho;
+        const double feq_n = wr * (((1.0 + t3) + sq) - s);
+        const double feq_m = wr * (((1.0 - t3) + sq) - s);
+        double on = omc * f[n] + omega * feq_n;
+        double om = omc * f[m] + omega * feq_m;
+        if (FORCED) {
+            on = on + p.gpref[n] * ((p.gcF[n] + t3 * p.gcF[n]) - udotF);
+            om = om + p.gpref[m] * ((p.gcF[m] + (-t3) * p.gcF[m]) - udotF);
+        }
+        f[n] = on;
+        f[m] = om;
+    }
+}
+
+template <class R> __device__ __forceinline__ R recip(R x);
+template <> __device__ __forceinline__ double recip<double>(double x) {
+    // float reciprocal seed refined by two Newton steps: ~1 ulp.
+    double r = (double)__frcp_rn((float)x);
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    return fma(r, e, r);
+}
+template <> __device__ __forceinline__ float recip<float>(float x) { return __frcp_rn(x); }
+
+// Refactored BGK (+Guo) in compute type R, FMA-friendly:
+//   out_n = f_n + omega (feq_n - f_n) [+ guo_n],
+//   feq_{n, opp} = w rho (B + 4.5 cu^2 +- 3 cu),  B = 1 - 1.5 u^2.
+template <int Q, class R, bool FORCED>
+__device__ __forceinline__ void collide_fast(const KParams& p, R* f) {
+    using L = Lat<Q>;
+    R rho = f[0], jx = R(0), jy = R(0), jz = R(0);
+#pragma unroll
+    for (int n = 1; n < Q; ++n) {
+        const int m = L::opp(n);
+        if (m < n) continue;
+        const R sm = f[n] + f[m];
+        const R df = f[n] - f[m];
+        rho += sm;
+        if (L::cx(n) == 1) jx += df; else if (L::cx(n) == -1) jx -= df;
+        if (L::cy(n) == 1) jy += df; else if (L::cy(n) == -1) jy -= df;
+        if (L::D == 3) { if (L::cz(n) == 1) jz += df; else if (L::cz(n) == -1) jz -= df; }
+    }
+    const R inv = recip<R>(rho);
+    R u[3];
+    if (FORCED) {
+        u[0] = (jx + (R)p.hF[0]) * inv;
+        u[1] = (jy + (R)p.hF[1]) * inv;
+        u[2] = (L::D == 3) ? (jz + (R)p.hF[2]) * inv : R(0);
+    } else {
+        u[0] = jx * inv;
+        u[1] = jy * inv;
+        u[2] = (L::D == 3) ? jz * inv : R(0);
+    }
+    const R usq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+    const R B = R(1) - R(1.5) * usq;
+    const R omega = (R)p.omega;
+    R udotF = R(0);
+    if (FORCED) udotF = u[0] * (R)p.F[0] + u[1] * (R)p.F[1] + u[2] * (R)p.F[2];
+    {
+        const R feq = (R)L::w(0) * rho * B;
+        R o = f[0] + omega * (feq - f[0]);
+        if (FORCED) o -= (R)p.gpref[0] * udotF;
+        f[0] = o;
+    }
+#pragma unroll
+    for (int n = 1; n < Q; ++n) {
+        const int m = L::opp(n);
+        if (m < n) continue;
+        const R cu = cdot<Q, R>(n, u);
+        const R a = (R(4.5) * cu) * cu + B;
+        const R b = R(3) * cu;
+        const R wr = (R)L::w(n) * rho;
+        const R feq_n = wr * (a + b);
+        const R feq_m = wr * (a - b);
+        R on = f[n] + omega * (feq_n - f[n]);
+        R om = f[m] + omega * (feq_m - f[m]);
+        if (FORCED) {
+            const R cF = (R)p.gcF[n];
+            on += (R)p.gpref[n] * ((cF + b * cF) - udotF);
+            om += (R)p.gpref[m] * ((b * cF - cF) - udotF);
+        }
+        f[n] = on;
+        f[m] = om;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Kernels on the handle's SoA state (no ghost layer).
+// Block (BX, BY): lanes run along x so every warp shares (y, z).
+// ---------------------------------------------------------------------------
+template <int Q, class St, int ARITH, bool FORCED>
+__global__ void __launch_bounds__(256) k_step(const typename St::T* __restrict__ fin, typename St::T* __restrict__ fout,
+                                              const KParams p, const KParams* __restrict__ pg) {
+    using R = typename St::R;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x >= p.nx || y >= p.ny) return;
+    const long long c = ((long long)z * p.ny + y) * p.nx + x;
+    R f[Q];
+    pull<Q, St>(p, pg, fin, x, y, z, c, f);
+    if constexpr (ARITH == kExact) collide_exact<Q, FORCED>(p, f);
+    else collide_fast<Q, R, FORCED>(p, f);
+#pragma unroll
+    for (int n = 0; n < Q; ++n) St::template st<Q>(fout, n, c, p.ncell, f[n]);
+}
+
+// updateMacroscopic (SimulationSetup.cpp:142-166): moments of the streamed
+// populations, written as FP64 rho[c], u[d*N + c].
+template <int Q, class St, bool FORCED>
+__global__ void __launch_bounds__(256) k_moments(const typename St::T* __restrict__ fin, double* __restrict__ rho_out,
+                                                 double* __restrict__ u_out, const KParams p,
+                                                 const KParams* __restrict__ pg) {
+    using R = typename St::R;
+    using L = Lat<Q>;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x >= p.nx || y >= p.ny) return;
+    const long long c = ((long long)z * p.ny + y) * p.nx + x;
+    R fr[Q];
+    pull<Q, St>(p, pg, fin, x, y, z, c, fr);
+    double f[Q];
+#pragma unroll
+    for (int n = 0; n < Q; ++n) f[n] = (double)fr[n];
+    double rho, u[3];
+    moments_exact<Q, FORCED>(p, f, rho, u);
+    rho_out[c] = rho;
+#pragma unroll
+    for (int d = 0; d < L::D; ++d) u_out[d * p.ncell + c] = u[d];
+}
+
+// setInitialConditions (SimulationSetup.cpp:201-219): forced runs shift u by
+// -F/(2 rho) (initVelCorrection, Macroscopic.cpp:164-181), f = feq(rho, u)
+// (computeEquilibrium, Equilibrium.cpp:32-43), and the macroscopic fields are
+// recomputed from the stored f (computeMacroscopic, Macroscopic.cpp:139-162).
+template <int Q, class St, bool FORCED>
+__global__ void __launch_bounds__(256) k_init(typename St::T* __restrict__ fout, double* __restrict__ rho_io,
+                                              double* __restrict__ u_io, const KParams p) {
+    using L = Lat<Q>;
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= p.ncell) return;
+    const double rho = rho_io[c];
+    double u[3] = {u_io[c], u_io[p.ncell + c], L::D == 3 ? u_io[2 * p.ncell + c] : 0.0};
+    if (FORCED)
+        for (int d = 0; d < L::D; ++d) u[d] = u[d] - 0.5 * p.F[d] / rho;
+    const double usq = (L::D == 2) ? u[0] * u[0] + u[1] * u[1] : u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+    double f[Q];
+#pragma unroll
+    for (int n = 0; n < Q; ++n) {
+        const double cu = (n == 0) ? 0.0 : cdot<Q, double>(n, u);
+        f[n] = L::w(n) * rho * (1 + 3.0 * cu + 4.5 * cu * cu - 1.5 * usq);
+        St::template st<Q>(fout, n, c, p.ncell, (typename St::R)f[n]);
+    }
+    if (FORCED) {
+        double fs[Q];
+#pragma unroll
+        for (int n = 0; n < Q; ++n) fs[n] = (double)St::template ld<Q>(fout, n, c, p.ncell);
+        double r, uu[3];
+        moments_exact<Q, true>(p, fs, r, uu);
+        rho_io[c] = r;
+        for (int d = 0; d < L::D; ++d) u_io[d * p.ncell + c] = uu[d];
+    }
+}
+
+// FP64 sums of the stored populations: block partials (mass, jx, jy, jz)
+// into part[4*block]; k_reduce_final adds them in block order.
+template <int Q, class St>
+__global__ void __launch_bounds__(256) k_reduce_partial(const typename St::T* __restrict__ fin, double* __restrict__ part,
+                                                        long long ncell) {
+    using L = Lat<Q>;
+    double a[4] = {0.0, 0.0, 0.0, 0.0};
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int n = 0; n < Q; ++n) {
+            const double v = (double)St::template ld<Q>(fin, n, c, ncell);
+            a[0] += v;
+            if (L::cx(n)) a[1] += L::cx(n) * v;
+            if (L::cy(n)) a[2] += L::cy(n) * v;
+            if (L::cz(n)) a[3] += L::cz(n) * v;
+        }
+    }
+    __shared__ double sh[4][8];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        double v = a[k];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) sh[k][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += sh[threadIdx.x][w];
+        part[4 * blockIdx.x + threadIdx.x] = v;
+    }
+}
+
+}  // namespace mph

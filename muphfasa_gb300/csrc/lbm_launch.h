@@ -1,0 +1,64 @@
+// lbm_launch.h -- host-side launchers of the step kernels.  Each kernel
+// translation unit defines the launchers of the precisions it compiles;
+// sim.cu dispatches on the handle's precision.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "lbm_kernels.cuh"
+
+namespace mph {
+
+// Block of 256 threads with lanes along x (rows of one (y, z)), grid over
+// (x-blocks, y-blocks, z).
+inline void step_shape(const KParams& p, dim3& grid, dim3& block) {
+    int bx = ((p.nx + 31) / 32) * 32;
+    if (bx > 256) bx = 256;
+    const int by = 256 / bx;
+    block = dim3(bx, by, 1);
+    grid = dim3((p.nx + bx - 1) / bx, (p.ny + by - 1) / by, p.nz);
+}
+
+// Plain 1-D shape over the cells.
+inline void flat_shape(long long ncell, dim3& grid, dim3& block) {
+    block = dim3(256, 1, 1);
+    grid = dim3((unsigned)((ncell + 255) / 256), 1, 1);
+}
+
+// ---- k_f64_exact.cu (reference operation order, --fmad=false) ----------
+cudaError_t launch_step_exact(int q, bool forced, const double* fin, double* fout, const KParams& p,
+                              const KParams* pg, cudaStream_t s);
+// prec selects the storage policy of fin (MPH_PREC_*); moments/init/reduce
+// use the reference operation order in FP64 for every precision.
+cudaError_t launch_moments(int prec, int q, bool forced, const void* fin, double* rho, double* u, const KParams& p,
+                           const KParams* pg, cudaStream_t s);
+cudaError_t launch_init(int prec, int q, bool forced, void* f, double* rho, double* u, const KParams& p,
+                        cudaStream_t s);
+cudaError_t launch_reduce(int prec, int q, const void* f, long long ncell, double* part, int nblocks, double* out4,
+                          cudaStream_t s);
+cudaError_t launch_convert(int prec, int q, bool to_store, void* store, double* f64, int n, long long ncell,
+                           cudaStream_t s);
+
+struct A4 {
+    double* p;
+    long long js, ks, ns;
+    int b[3], e[3];
+};
+cudaError_t launch_pull_collide_arr(int dim, int q, bool forced, const int lo[3], const int hi[3], const A4& fin,
+                                    const A4& fout, const KParams& p, cudaStream_t s);
+cudaError_t launch_periodic_fill_arr(int dim, int q, const int dlo[3], const int dhi[3], const int per[3],
+                                     const A4& f, cudaStream_t s);
+cudaError_t launch_bc_fill_arr(int dim, int q, const int dlo[3], const int dhi[3], const int per[3],
+                               const KParams* pg, const A4& f, cudaStream_t s);
+
+// ---- k_fast_*.cu (refactored FMA arithmetic) ----------------------------
+cudaError_t launch_step_fast_f64(int q, bool forced, const double* fin, double* fout, const KParams& p,
+                                 const KParams* pg, cudaStream_t s);
+cudaError_t launch_step_fast_f32(int q, bool forced, const float* fin, float* fout, const KParams& p,
+                                 const KParams* pg, cudaStream_t s);
+cudaError_t launch_step_fast_f16s(int q, bool forced, const void* fin, void* fout, const KParams& p,
+                                  const KParams* pg, cudaStream_t s);
+cudaError_t launch_step_fast_bf16s(int q, bool forced, const void* fin, void* fout, const KParams& p,
+                                   const KParams* pg, cudaStream_t s);
+
+}  // namespace mph

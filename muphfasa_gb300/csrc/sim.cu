@@ -1,0 +1,438 @@
+// sim.cu -- the simulation handle behind the C ABI: device-resident
+// populations (two SoA buffers swapped every step, the A/B pattern of
+// SimulationImpl's m_fin/m_fout), one CUDA stream, and the ISimulation
+// operations (ISimulation.H:16-44) mapped onto the kernels.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <utility>
+
+#include "lbm_launch.h"
+#include "mph_internal.h"
+
+using namespace mph;
+
+struct mph_sim {
+    mph_desc d;
+    mph_resolved_bc table[27];
+    KParams kp;
+    KParams* d_kp = nullptr;  // global copy for the boundary path
+    size_t elem = 8;          // bytes per stored population value
+    void* fa = nullptr;       // current populations (m_fin)
+    void* fb = nullptr;       // next populations (m_fout)
+    double* d_rho = nullptr;  // macroscopic scratch (init / moments)
+    double* d_u = nullptr;
+    double* d_stage = nullptr;  // FP64 staging of one population (conversions)
+    double* d_part = nullptr;   // reduction partials
+    double* d_red = nullptr;    // reduction result
+    int red_blocks = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double time = 0.0;
+    bool has_state = false;
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(MPH_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define MPH_CK(call, what)                                   \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_fail(e_, (what)); \
+    } while (0)
+
+size_t elem_size(int prec) {
+    switch (prec) {
+        case MPH_PREC_F64:
+        case MPH_PREC_F64_FAST: return 8;
+        case MPH_PREC_F32: return 4;
+        case MPH_PREC_F16S:
+        case MPH_PREC_BF16S: return 2;
+    }
+    return 0;
+}
+
+template <int Q>
+void guo_tables(const mph_desc& d, KParams& kp) {
+    using L = Lat<Q>;
+    for (int n = 0; n < 27; ++n) { kp.gpref[n] = 0.0; kp.gcF[n] = 0.0; }
+    for (int n = 0; n < Q; ++n) {
+        // guoForceTerm prefactor and c.F (Collision.H:21-65), same order.
+        kp.gpref[n] = (1.0 - 0.5 * d.omega) * L::w(n) * 3.0;
+        if (L::D == 2) kp.gcF[n] = L::cx(n) * kp.F[0] + L::cy(n) * kp.F[1];
+        else kp.gcF[n] = L::cx(n) * kp.F[0] + L::cy(n) * kp.F[1] + L::cz(n) * kp.F[2];
+    }
+}
+
+void build_params(const mph_desc& d, const mph_resolved_bc* tab, KParams& kp) {
+    std::memset(&kp, 0, sizeof(kp));
+    kp.nx = d.n[0];
+    kp.ny = d.n[1];
+    kp.nz = d.dim == 3 ? d.n[2] : 1;
+    for (int a = 0; a < 3; ++a) kp.periodic[a] = (a < d.dim) && d.face_type[2 * a] == MPH_BC_PERIODIC;
+    kp.ncell = (long long)kp.nx * kp.ny * kp.nz;
+    kp.omega = d.omega;
+    kp.omc = 1.0 - d.omega;
+    for (int a = 0; a < 3; ++a) {
+        kp.F[a] = (d.forced && a < d.dim) ? d.force[a] : 0.0;
+        kp.hF[a] = 0.5 * kp.F[a];
+    }
+    switch (d.q) {
+        case 9: guo_tables<9>(d, kp); break;
+        case 15: guo_tables<15>(d, kp); break;
+        case 19: guo_tables<19>(d, kp); break;
+        case 27: guo_tables<27>(d, kp); break;
+    }
+    for (int c = 0; c < 27; ++c) {
+        kp.bc_type[c] = tab[c].type;
+        kp.bc_rho[c] = tab[c].rho;
+        for (int a = 0; a < 3; ++a) kp.bc_U[c][a] = tab[c].U[a];
+    }
+}
+
+void free_all(mph_sim* s) {
+    if (!s) return;
+    cudaFree(s->fa);
+    cudaFree(s->fb);
+    cudaFree(s->d_kp);
+    cudaFree(s->d_rho);
+    cudaFree(s->d_u);
+    cudaFree(s->d_stage);
+    cudaFree(s->d_part);
+    cudaFree(s->d_red);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->stream) cudaStreamDestroy(s->stream);
+}
+
+int ensure_macro(mph_sim* s) {
+    if (!s->d_rho) MPH_CK(cudaMalloc(&s->d_rho, sizeof(double) * s->kp.ncell), "cudaMalloc(rho)");
+    if (!s->d_u) MPH_CK(cudaMalloc(&s->d_u, sizeof(double) * 3 * s->kp.ncell), "cudaMalloc(u)");
+    return MPH_OK;
+}
+
+int ensure_stage(mph_sim* s) {
+    if (!s->d_stage) MPH_CK(cudaMalloc(&s->d_stage, sizeof(double) * s->kp.ncell), "cudaMalloc(stage)");
+    return MPH_OK;
+}
+
+bool is_f64(const mph_sim* s) { return s->d.precision == MPH_PREC_F64 || s->d.precision == MPH_PREC_F64_FAST; }
+
+cudaError_t launch_one_step(mph_sim* s) {
+    const int q = s->d.q;
+    const bool forced = s->d.forced != 0;
+    switch (s->d.precision) {
+        case MPH_PREC_F64:
+            return launch_step_exact(q, forced, (const double*)s->fa, (double*)s->fb, s->kp, s->d_kp, s->stream);
+        case MPH_PREC_F64_FAST:
+            return launch_step_fast_f64(q, forced, (const double*)s->fa, (double*)s->fb, s->kp, s->d_kp, s->stream);
+        case MPH_PREC_F32:
+            return launch_step_fast_f32(q, forced, (const float*)s->fa, (float*)s->fb, s->kp, s->d_kp, s->stream);
+        case MPH_PREC_F16S:
+            return launch_step_fast_f16s(q, forced, s->fa, s->fb, s->kp, s->d_kp, s->stream);
+        case MPH_PREC_BF16S:
+            return launch_step_fast_bf16s(q, forced, s->fa, s->fb, s->kp, s->d_kp, s->stream);
+    }
+    return cudaErrorInvalidValue;
+}
+
+int advance_async(mph_sim* s, int nsteps) {
+    for (int t = 0; t < nsteps; ++t) {
+        cudaError_t e = launch_one_step(s);
+        if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
+        std::swap(s->fa, s->fb);  // SimulationSetup.cpp:132
+    }
+    s->time += nsteps;  // SimulationSetup.cpp:138
+    return MPH_OK;
+}
+
+int upload(mph_sim* s, const double* f) {
+    const size_t n = (size_t)s->d.q * s->kp.ncell;
+    if (is_f64(s)) {
+        MPH_CK(cudaMemcpyAsync(s->fa, f, n * sizeof(double), cudaMemcpyHostToDevice, s->stream), "upload f");
+        return MPH_OK;
+    }
+    int rc = ensure_stage(s);
+    if (rc) return rc;
+    for (int q = 0; q < s->d.q; ++q) {
+        MPH_CK(cudaMemcpyAsync(s->d_stage, f + (size_t)q * s->kp.ncell, sizeof(double) * s->kp.ncell,
+                               cudaMemcpyHostToDevice, s->stream), "upload f");
+        MPH_CK(launch_convert(s->d.precision, s->d.q, true, s->fa, s->d_stage, q, s->kp.ncell, s->stream), "convert f");
+    }
+    return MPH_OK;
+}
+
+int download(mph_sim* s, double* f) {
+    const size_t n = (size_t)s->d.q * s->kp.ncell;
+    if (is_f64(s)) {
+        MPH_CK(cudaMemcpyAsync(f, s->fa, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream), "download f");
+        return MPH_OK;
+    }
+    int rc = ensure_stage(s);
+    if (rc) return rc;
+    for (int q = 0; q < s->d.q; ++q) {
+        MPH_CK(launch_convert(s->d.precision, s->d.q, false, s->fa, s->d_stage, q, s->kp.ncell, s->stream), "convert f");
+        MPH_CK(cudaMemcpyAsync(f + (size_t)q * s->kp.ncell, s->d_stage, sizeof(double) * s->kp.ncell,
+                               cudaMemcpyDeviceToHost, s->stream), "download f");
+    }
+    return MPH_OK;
+}
+
+int sync(mph_sim* s, const char* what) {
+    MPH_CK(cudaStreamSynchronize(s->stream), what);
+    return MPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mph_set_device(int device) {
+    int n = 0;
+    MPH_CK(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+    if (device < 0 || device >= n) return fail(MPH_ERR_ARG, "mph_set_device: no such device");
+    MPH_CK(cudaSetDevice(device), "cudaSetDevice");
+    return MPH_OK;
+}
+
+int mph_create(const mph_desc* desc, mph_sim** out) {
+    if (!desc || !out) return fail(MPH_ERR_ARG, "mph_create: NULL argument");
+    *out = nullptr;
+    const mph_desc& d = *desc;
+    if (!lattice_ok(d.dim, d.q)) return fail(MPH_ERR_ARG, "mph_create: unsupported lattice (dim, q)");
+    if (elem_size(d.precision) == 0) return fail(MPH_ERR_ARG, "mph_create: unknown precision");
+    for (int a = 0; a < d.dim; ++a)
+        if (d.n[a] < 1) return fail(MPH_ERR_ARG, "mph_create: cell counts must be positive");
+    if (d.dim == 2 && d.n[2] != 1) return fail(MPH_ERR_ARG, "mph_create: n[2] must be 1 for a 2-D lattice");
+    const long long ncell = (long long)d.n[0] * d.n[1] * (d.dim == 3 ? d.n[2] : 1);
+    if (ncell >= (1LL << 31)) return fail(MPH_ERR_ARG, "mph_create: more than 2^31-1 cells");
+    if ((d.dim == 3 ? d.n[2] : 1) > 65535 || (d.n[1] + 7) / 8 > 65535)
+        return fail(MPH_ERR_ARG, "mph_create: ny or nz exceeds the launch grid limit (65535)");
+    if (!(d.omega > 0.0 && d.omega < 2.0)) return fail(MPH_ERR_CONFIG, "mph_create: omega must lie in (0, 2)");
+    auto* s = new mph_sim();
+    s->d = d;
+    if (d.dim == 2) s->d.n[2] = 1;
+    int rc = resolve_table(s->d, s->table);
+    if (rc) { delete s; return rc; }
+    build_params(s->d, s->table, s->kp);
+    s->elem = elem_size(d.precision);
+    const size_t bytes = s->elem * (size_t)d.q * (size_t)ncell;
+    cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
+    if (e == cudaSuccess) e = cudaMalloc(&s->fa, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&s->fb, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_kp, sizeof(KParams));
+    if (e == cudaSuccess) e = cudaMemcpy(s->d_kp, &s->kp, sizeof(KParams), cudaMemcpyHostToDevice);
+    s->red_blocks = 152 * 4;
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_part, sizeof(double) * 4 * s->red_blocks);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_red, sizeof(double) * 4);
+    if (e != cudaSuccess) {
+        rc = cuda_fail(e, "mph_create");
+        free_all(s);
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return MPH_OK;
+}
+
+int mph_destroy(mph_sim* s) {
+    if (!s) return MPH_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    free_all(s);
+    delete s;
+    return MPH_OK;
+}
+
+int mph_set_f(mph_sim* s, const double* f) {
+    if (!s || !f) return fail(MPH_ERR_ARG, "mph_set_f: NULL argument");
+    int rc = upload(s, f);
+    if (rc) return rc;
+    s->has_state = true;
+    return sync(s, "mph_set_f");
+}
+
+int mph_get_f(mph_sim* s, double* f) {
+    if (!s || !f) return fail(MPH_ERR_ARG, "mph_get_f: NULL argument");
+    if (!s->has_state) return fail(MPH_ERR_STATE, "mph_get_f: no populations yet (call mph_set_f or mph_init_fields)");
+    int rc = download(s, f);
+    if (rc) return rc;
+    return sync(s, "mph_get_f");
+}
+
+int mph_init_fields(mph_sim* s, double* rho, double* u) {
+    if (!s || !rho || !u) return fail(MPH_ERR_ARG, "mph_init_fields: NULL argument");
+    int rc = ensure_macro(s);
+    if (rc) return rc;
+    const long long N = s->kp.ncell;
+    MPH_CK(cudaMemcpyAsync(s->d_rho, rho, sizeof(double) * N, cudaMemcpyHostToDevice, s->stream), "init upload rho");
+    MPH_CK(cudaMemcpyAsync(s->d_u, u, sizeof(double) * s->d.dim * N, cudaMemcpyHostToDevice, s->stream), "init upload u");
+    MPH_CK(launch_init(s->d.precision, s->d.q, s->d.forced != 0, s->fa, s->d_rho, s->d_u, s->kp, s->stream), "init kernel");
+    if (s->d.forced) {
+        MPH_CK(cudaMemcpyAsync(rho, s->d_rho, sizeof(double) * N, cudaMemcpyDeviceToHost, s->stream), "init download rho");
+        MPH_CK(cudaMemcpyAsync(u, s->d_u, sizeof(double) * s->d.dim * N, cudaMemcpyDeviceToHost, s->stream), "init download u");
+    }
+    s->has_state = true;
+    s->time = 0.0;
+    return sync(s, "mph_init_fields");
+}
+
+int mph_advance(mph_sim* s, int nsteps) {
+    if (!s || nsteps < 0) return fail(MPH_ERR_ARG, "mph_advance: bad argument");
+    if (!s->has_state) return fail(MPH_ERR_STATE, "mph_advance: no populations yet");
+    int rc = advance_async(s, nsteps);
+    if (rc) return rc;
+    return sync(s, "mph_advance");
+}
+
+int mph_advance_timed(mph_sim* s, int nsteps, float* ms) {
+    if (!s || nsteps < 0 || !ms) return fail(MPH_ERR_ARG, "mph_advance_timed: bad argument");
+    if (!s->has_state) return fail(MPH_ERR_STATE, "mph_advance_timed: no populations yet");
+    MPH_CK(cudaEventRecord(s->ev0, s->stream), "event record");
+    int rc = advance_async(s, nsteps);
+    if (rc) return rc;
+    MPH_CK(cudaEventRecord(s->ev1, s->stream), "event record");
+    MPH_CK(cudaEventSynchronize(s->ev1), "event sync");
+    MPH_CK(cudaEventElapsedTime(ms, s->ev0, s->ev1), "event elapsed");
+    return MPH_OK;
+}
+
+int mph_update_macroscopic(mph_sim* s, double* rho, double* u) {
+    if (!s || !rho || !u) return fail(MPH_ERR_ARG, "mph_update_macroscopic: NULL argument");
+    if (!s->has_state) return fail(MPH_ERR_STATE, "mph_update_macroscopic: no populations yet");
+    int rc = ensure_macro(s);
+    if (rc) return rc;
+    const long long N = s->kp.ncell;
+    MPH_CK(launch_moments(s->d.precision, s->d.q, s->d.forced != 0, s->fa, s->d_rho, s->d_u, s->kp, s->d_kp, s->stream),
+           "moments kernel");
+    MPH_CK(cudaMemcpyAsync(rho, s->d_rho, sizeof(double) * N, cudaMemcpyDeviceToHost, s->stream), "download rho");
+    MPH_CK(cudaMemcpyAsync(u, s->d_u, sizeof(double) * s->d.dim * N, cudaMemcpyDeviceToHost, s->stream), "download u");
+    return sync(s, "mph_update_macroscopic");
+}
+
+int mph_reduce(mph_sim* s, double* out) {
+    if (!s || !out) return fail(MPH_ERR_ARG, "mph_reduce: NULL argument");
+    if (!s->has_state) return fail(MPH_ERR_STATE, "mph_reduce: no populations yet");
+    MPH_CK(launch_reduce(s->d.precision, s->d.q, s->fa, s->kp.ncell, s->d_part, s->red_blocks, s->d_red, s->stream),
+           "reduce kernel");
+    MPH_CK(cudaMemcpyAsync(out, s->d_red, sizeof(double) * 4, cudaMemcpyDeviceToHost, s->stream), "download sums");
+    return sync(s, "mph_reduce");
+}
+
+int mph_time(const mph_sim* s, double* t) {
+    if (!s || !t) return fail(MPH_ERR_ARG, "mph_time: NULL argument");
+    *t = s->time;
+    return MPH_OK;
+}
+
+int mph_launches_per_step(const mph_sim* s, int* n) {
+    if (!s || !n) return fail(MPH_ERR_ARG, "mph_launches_per_step: NULL argument");
+    *n = 1;
+    return MPH_OK;
+}
+
+int mph_step_host(mph_sim* s, const double* f_in, double* f_out, int nsteps) {
+    if (!s || !f_in || !f_out || nsteps < 0) return fail(MPH_ERR_ARG, "mph_step_host: bad argument");
+    int rc = upload(s, f_in);
+    if (rc) return rc;
+    s->has_state = true;
+    rc = advance_async(s, nsteps);
+    if (rc) return rc;
+    rc = download(s, f_out);
+    if (rc) return rc;
+    return sync(s, "mph_step_host");
+}
+
+// ---- plugin level ------------------------------------------------------
+static int to_a4(const mph_array4* a, A4& o, int q, const char* what) {
+    if (!a || !a->p) return fail(MPH_ERR_ARG, std::string(what) + ": NULL Array4");
+    if (a->ncomp < q) return fail(MPH_ERR_ARG, std::string(what) + ": Array4 has fewer than Q components");
+    o.p = a->p;
+    o.js = a->jstride; o.ks = a->kstride; o.ns = a->nstride;
+    for (int d = 0; d < 3; ++d) {
+        o.b[d] = a->begin[d];
+        o.e[d] = a->end[d];
+        if (o.e[d] <= o.b[d]) return fail(MPH_ERR_ARG, std::string(what) + ": empty Array4 extent");
+    }
+    return MPH_OK;
+}
+
+static bool a4_contains(const A4& a, const int lo[3], const int hi[3]) {
+    for (int d = 0; d < 3; ++d)
+        if (lo[d] < a.b[d] || hi[d] >= a.e[d]) return false;
+    return true;
+}
+
+int mph_pull_collide_fused_arr(int dim, int q, const int lo[3], const int hi[3], const mph_array4* fin,
+                               const mph_array4* fout, double omega, const double* force, void* stream) {
+    if (!lattice_ok(dim, q) || !lo || !hi) return fail(MPH_ERR_ARG, "mph_pull_collide_fused_arr: bad lattice or box");
+    A4 a, b;
+    int rc = to_a4(fin, a, q, "mph_pull_collide_fused_arr(fin)");
+    if (rc) return rc;
+    rc = to_a4(fout, b, q, "mph_pull_collide_fused_arr(fout)");
+    if (rc) return rc;
+    int l[3] = {lo[0], lo[1], dim == 3 ? lo[2] : 0}, h[3] = {hi[0], hi[1], dim == 3 ? hi[2] : 0};
+    for (int d = 0; d < dim; ++d)
+        if (h[d] < l[d]) return fail(MPH_ERR_ARG, "mph_pull_collide_fused_arr: empty box");
+    int gl[3] = {l[0] - 1, l[1] - 1, dim == 3 ? l[2] - 1 : l[2]}, gh[3] = {h[0] + 1, h[1] + 1, dim == 3 ? h[2] + 1 : h[2]};
+    if (!a4_contains(a, gl, gh)) return fail(MPH_ERR_ARG, "mph_pull_collide_fused_arr: fin does not cover box grown by 1");
+    if (!a4_contains(b, l, h)) return fail(MPH_ERR_ARG, "mph_pull_collide_fused_arr: fout does not cover the box");
+    mph_desc d;
+    std::memset(&d, 0, sizeof(d));
+    d.dim = dim; d.q = q; d.omega = omega; d.forced = force != nullptr;
+    d.n[0] = h[0] - l[0] + 1; d.n[1] = h[1] - l[1] + 1; d.n[2] = h[2] - l[2] + 1;
+    for (int a2 = 0; a2 < 3; ++a2) d.force[a2] = (force && a2 < dim) ? force[a2] : 0.0;
+    for (int f = 0; f < 6; ++f) d.face_type[f] = MPH_BC_PERIODIC;
+    mph_resolved_bc tab[27];
+    for (int c = 0; c < 27; ++c) { tab[c].type = MPH_BC_PERIODIC; tab[c].rho = 1.0; tab[c].U[0] = tab[c].U[1] = tab[c].U[2] = 0.0; }
+    KParams kp;
+    build_params(d, tab, kp);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    MPH_CK(launch_pull_collide_arr(dim, q, force != nullptr, l, h, a, b, kp, st), "pull_collide_arr");
+    MPH_CK(cudaStreamSynchronize(st), "pull_collide_arr sync");
+    return MPH_OK;
+}
+
+int mph_periodic_fill_arr(int dim, int q, const int dom_lo[3], const int dom_hi[3], const int periodic[3],
+                          const mph_array4* f, void* stream) {
+    if (!lattice_ok(dim, q) || !dom_lo || !dom_hi || !periodic) return fail(MPH_ERR_ARG, "mph_periodic_fill_arr: bad argument");
+    A4 a;
+    int rc = to_a4(f, a, q, "mph_periodic_fill_arr");
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    MPH_CK(launch_periodic_fill_arr(dim, q, dom_lo, dom_hi, periodic, a, st), "periodic_fill_arr");
+    MPH_CK(cudaStreamSynchronize(st), "periodic_fill_arr sync");
+    return MPH_OK;
+}
+
+int mph_bc_fill_arr(int dim, int q, const int dom_lo[3], const int dom_hi[3], const int periodic[3],
+                    const mph_resolved_bc* table, const mph_array4* f, void* stream) {
+    if (!lattice_ok(dim, q) || !dom_lo || !dom_hi || !periodic || !table)
+        return fail(MPH_ERR_ARG, "mph_bc_fill_arr: bad argument");
+    A4 a;
+    int rc = to_a4(f, a, q, "mph_bc_fill_arr");
+    if (rc) return rc;
+    KParams kp;
+    std::memset(&kp, 0, sizeof(kp));
+    for (int c = 0; c < 27; ++c) {
+        if (table[c].type < 0 || table[c].type > MPH_BC_PERIODIC) return fail(MPH_ERR_ARG, "mph_bc_fill_arr: bad table type");
+        kp.bc_type[c] = table[c].type;
+        kp.bc_rho[c] = table[c].rho;
+        for (int k = 0; k < 3; ++k) kp.bc_U[c][k] = table[c].U[k];
+    }
+    KParams* dkp = nullptr;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    MPH_CK(cudaMalloc(&dkp, sizeof(KParams)), "bc_fill_arr params");
+    cudaError_t e = cudaMemcpyAsync(dkp, &kp, sizeof(KParams), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = launch_bc_fill_arr(dim, q, dom_lo, dom_hi, periodic, dkp, a, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(dkp);
+    if (e != cudaSuccess) return cuda_fail(e, "bc_fill_arr");
+    return MPH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,169 @@
+"""The configurations of the benchmark at full size: bit-exact FP64 parity on
+the 2-D Taylor-Green case (256^2, 5000 steps) and the D3Q19 channel at reduced
+size/steps; size-independent properties at full size (mass conservation,
+uniform-force momentum growth, symmetry, analytic decay and start-up
+Poiseuille profile)."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def tgv_fields(N, u0):
+    """Taylor-Green initial field of the 2-D benchmark: u = u0 (sin kx cos ky,
+    -cos kx sin ky), k = 2 pi / N, cell centres x = i + 0.5; uniform rho."""
+    k = 2.0 * math.pi / N
+    x = np.arange(N) + 0.5
+    X, Y = np.meshgrid(x, x, indexing="xy")  # [j][i]
+    ux = u0 * np.sin(k * X) * np.cos(k * Y)
+    uy = -u0 * np.cos(k * X) * np.sin(k * Y)
+    return np.ones(N * N), np.concatenate([ux.ravel(), uy.ravel()])
+
+
+def test_tgv2d_256_5000_steps_bitwise_and_decay(mph, oracle_mod):
+    N, steps, tau, u0 = 256, 5000, 0.8, 0.05
+    O = oracle_mod
+    cfg = O.Config("D2Q9", (N, N), omega=1.0 / tau)
+    o = O.OracleSim(cfg, "port")
+    s = mph.Simulation(mph.make_desc("D2Q9", (N, N), 1.0 / tau))
+    rho, u = tgv_fields(N, u0)
+    o.init_fields(rho, u)
+    s.initialize(rho, u)
+    o.step(steps, nthreads=16)
+    s.advance(steps)
+    assert np.array_equal(o.get_f(), s.f())
+    _, us = s.update_macroscopic()
+    # analytic decay of the amplitude: exp(-2 nu k^2 t), nu = (tau - 1/2)/3
+    nu = (tau - 0.5) / 3.0
+    k = 2 * math.pi / N
+    amp = np.abs(us).max() / u0
+    assert abs(amp / math.exp(-2 * nu * k * k * steps) - 1.0) < 5e-3
+
+
+def channel_init(n, rng):
+    N = n[0] * n[1] * n[2]
+    rho = 1.0 + rng.uniform(-1e-4, 1e-4, N)
+    return rho, np.zeros(3 * N)
+
+
+CH_FACES = ["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic", "Periodic"]
+
+
+def test_channel_d3q19_64cubed_2000_steps_bitwise(mph, oracle_mod):
+    n, steps = (64, 64, 64), 2000
+    O = oracle_mod
+    F = (1e-6, 0.0, 0.0)
+    cfg = O.Config("D3Q19", n, omega=1.0 / 0.6, faces=CH_FACES, force=F)
+    o = O.OracleSim(cfg, "port")
+    s = mph.Simulation(mph.make_desc("D3Q19", n, 1.0 / 0.6, faces=CH_FACES, force=F))
+    rho, u = channel_init(n, np.random.default_rng(2024))
+    o.init_fields(rho, u)
+    s.initialize(rho, u)
+    o.step(steps, nthreads=16)
+    s.advance(steps)
+    assert np.array_equal(o.get_f(), s.f())
+
+
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-12), ("f64_fast", 1e-12)])
+def test_channel_d3q19_256cubed_vs_oracle(prec, tol, mph, oracle_mod):
+    n, steps = (256, 256, 256), 100
+    O = oracle_mod
+    F = (1e-6, 0.0, 0.0)
+    o = O.OracleSim(O.Config("D3Q19", n, omega=1.0 / 0.6, faces=CH_FACES, force=F), "port")
+    s = mph.Simulation(mph.make_desc("D3Q19", n, 1.0 / 0.6, faces=CH_FACES, force=F, precision=prec))
+    rho, u = channel_init(n, np.random.default_rng(7))
+    o.init_fields(rho, u)
+    s.initialize(rho, u)
+    o.step(steps, nthreads=16)
+    s.advance(steps)
+    fo, fs = o.get_f(), s.f()
+    err = float(np.max(np.abs(fs - fo) / np.abs(fo)))
+    print(f"{prec}: 256^3 channel, {steps} steps: max rel err {err:.3e}")
+    if prec == "f64":
+        assert err == 0.0
+    assert err < tol
+
+
+def test_channel_512cubed_properties(mph):
+    """Full-size channel: mass is conserved to round-off, the flow is symmetric
+    about the mid-plane, and the centre-line velocity follows the start-up
+    Poiseuille series u(y, t) = (F/(2 nu)) y (H - y) - sum_k ... ."""
+    n, steps = (512, 512, 512), 200
+    F, tau = 1e-6, 0.6
+    s = mph.Simulation(mph.make_desc("D3Q19", n, 1.0 / tau, faces=CH_FACES, force=(F, 0, 0),
+                                     precision="f64_fast"))
+    N = n[0] * n[1] * n[2]
+    s.initialize(np.ones(N), np.zeros(3 * N))
+    m0 = s.reduce()[0]
+    s.advance(steps)
+    m1 = s.reduce()
+    assert abs(m1[0] - m0) / m0 < 1e-12
+    # momentum grows by exactly F per cell per step in a periodic box; the
+    # walls remove some of it, so it is bounded by steps*N*F from above.
+    assert 0 < m1[1] <= steps * N * F * (1 + 1e-9)
+    rho, u = s.update_macroscopic()
+    ux = u[:N].reshape(n[2], n[1], n[0])
+    prof = ux.mean(axis=(0, 2))
+    assert np.allclose(prof, prof[::-1], rtol=1e-9, atol=1e-18)
+    H, nu = float(n[1]), (tau - 0.5) / 3.0
+    y = np.arange(n[1]) + 0.5
+    t = float(steps)
+    # start-up series for a body-force-driven channel (Fourier sine modes)
+    ua = F / (2 * nu) * y * (H - y)
+    for kk in range(1, 400, 2):
+        lam = (kk * math.pi / H) ** 2 * nu
+        ua -= 4 * F * H * H / (nu * (kk * math.pi) ** 3) * np.sin(kk * math.pi * y / H) * math.exp(-lam * t)
+    rel = np.abs(prof - ua).max() / np.abs(ua).max()
+    assert rel < 2e-2
+
+
+@pytest.mark.parametrize("lat", ["D2Q9", "D3Q15", "D3Q19", "D3Q27"])
+def test_uniform_force_every_step(lat, mph):
+    # tests/regression/uniform_force/main.cpp: u_k = k F / rho to 1e-12.
+    dim = mph.LATTICE_DQ[lat][0]
+    n = (8, 8, 8) if dim == 3 else (8, 8)
+    F = (4e-4, -2e-4, 3e-4)[:dim] + (0.0,) * (3 - dim)
+    s = mph.Simulation(mph.make_desc(lat, n, 1.25, force=F))
+    N = int(np.prod(n))
+    s.initialize(np.ones(N), np.zeros(dim * N))
+    for k in range(1, 31):
+        s.advance(1)
+        rho, u = s.update_macroscopic()
+        u = u.reshape(dim, N)
+        for d in range(dim):
+            assert np.abs(u[d] - k * F[d]).max() < 1e-12
+        assert np.abs(rho - 1.0).max() < 1e-12
+
+
+def test_closed_box_mass_conservation(mph):
+    n = (48, 40, 32)
+    faces = ["NoSlip"] * 5 + ["MovingWall"]
+    U = [[0.0] * 3 for _ in range(6)]
+    U[5] = [0.05, 0.02, 0.0]
+    s = mph.Simulation(mph.make_desc("D3Q19", n, 1.5, faces=faces, face_U=U))
+    N = int(np.prod(n))
+    s.initialize(np.ones(N), np.zeros(3 * N))
+    m0 = s.reduce()[0]
+    s.advance(500)
+    assert abs(s.reduce()[0] - m0) / m0 < 1e-12
+
+
+def test_lid_cavity_re100_centerline(mph):
+    """Lid-driven cavity at Re = 100 (tests/regression/lid2d): after the flow
+    settles the centre-line velocity minimum lies near the published value
+    -0.2140 U_lid (within 2 %)."""
+    N, U, Re = 64, 0.1, 100.0
+    nu = U * N / Re
+    tau = 3 * nu + 0.5
+    faces = ["NoSlip", "NoSlip", "NoSlip", "MovingWall", "Periodic", "Periodic"]
+    Uw = [[0.0] * 3 for _ in range(6)]
+    Uw[3] = [U, 0.0, 0.0]
+    s = mph.Simulation(mph.make_desc("D2Q9", (N, N), 1.0 / tau, faces=faces, face_U=Uw))
+    s.initialize(np.ones(N * N), np.zeros(2 * N * N))
+    s.advance(20000)
+    _, u = s.update_macroscopic()
+    ux = u[: N * N].reshape(N, N)
+    col = 0.5 * (ux[:, N // 2 - 1] + ux[:, N // 2])
+    assert abs(col.min() / U - (-0.2140417)) < 0.02 * 0.2140417

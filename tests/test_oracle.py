@@ -1,0 +1,148 @@
+"""The CPU oracle against the golden fixtures produced by the reference's own
+LBM sources, and the physics pins of the reference's unit tests
+(tests/unit/test_lattice.cpp, test_equilibrium.cpp, test_forcing.cpp,
+test_bc_corners.cpp, tests/regression/uniform_force/main.cpp)."""
+import numpy as np
+import pytest
+
+import golden_cases as G
+
+
+def _run_case(case, O, kind="port"):
+    cfg = G.oracle_config(case, O)
+    sim = O.OracleSim(cfg, kind)
+    name = case["name"]
+    if case["kind"] == "fields":
+        r, u = sim.init_fields(G.arr(name, "rho0"), G.arr(name, "u0"))
+        assert np.array_equal(r, G.arr(name, "rho_init"))
+        assert np.array_equal(u, G.arr(name, "u_init"))
+    else:
+        sim.set_f(G.arr(name, "f0"))
+        sim.fill_ghosts()
+    assert np.array_equal(sim.get_f(), G.arr(name, "f_init"))
+    sim.step(case["steps"], nthreads=2)
+    return sim
+
+
+@pytest.mark.parametrize("idx", range(48))
+def test_oracle_matches_golden_bitwise(idx, oracle_mod):
+    case = G.cases()[idx]
+    sim = _run_case(case, oracle_mod)
+    name = case["name"]
+    assert np.array_equal(sim.get_f(), G.arr(name, "f_final"))
+    # ghost layer too (NaN where the reference leaves a ghost population unset)
+    assert np.array_equal(sim.get_f_ghost(), G.arr(name, "fg_final"), equal_nan=True)
+    r, u = sim.moments()
+    assert np.array_equal(r, G.arr(name, "rho_final"))
+    assert np.array_equal(u, G.arr(name, "u_final"))
+
+
+def test_oracle_matches_reference_build_directly(oracle_mod):
+    O = oracle_mod
+    if not O.ref_available():
+        pytest.skip("reference-source build (oracle/_ref) not present on this host")
+    rng = np.random.default_rng(3)
+    for lat, n in (("D2Q9", (9, 7)), ("D3Q19", (4, 5, 6)), ("D3Q27", (5, 4, 3))):
+        dim = O.LATTICE_DQ[lat][0]
+        faces = ["Inflow", "PressureOutlet", "NoSlip", "MovingWall"] + (["Periodic", "Periodic"])
+        U = [[0.0] * 3 for _ in range(6)]
+        U[0][0] = 0.03
+        U[3][0] = 0.07
+        cfg = O.Config(lat, n, omega=1.3, faces=faces, face_rho=[1, 1.01, 1, 1, 1, 1], face_U=U,
+                       force=(3e-5, -1e-5, 2e-5))
+        a, b = O.OracleSim(cfg, "port"), O.OracleSim(cfg, "ref")
+        N = a.N
+        rho, u = 1 + 0.01 * rng.standard_normal(N), 0.03 * rng.standard_normal(dim * N)
+        a.init_fields(rho, u)
+        b.init_fields(rho, u)
+        a.step(25, 3)
+        b.step(25)
+        assert np.array_equal(a.get_f(), b.get_f())
+
+
+def _lattice(O, lat):
+    """Velocity table of the oracle's lattice recovered through its moments:
+    equilibrium populations at rho = 1, u = 0 are the weights."""
+    dim, q = O.LATTICE_DQ[lat]
+    n = (1, 1, 1) if dim == 3 else (1, 1)
+    sim = O.OracleSim(O.Config(lat, n, omega=1.0), "port")
+    sim.init_fields(np.ones(1), np.zeros(dim))
+    return sim.get_f()
+
+
+@pytest.mark.parametrize("lat", ["D2Q9", "D3Q15", "D3Q19", "D3Q27"])
+def test_weights_sum_to_one(lat, oracle_mod):
+    # test_lattice.cpp: sum w = 1 (feq at rest equals w)
+    w = _lattice(oracle_mod, lat)
+    assert abs(w.sum() - 1.0) < 1e-15
+
+
+@pytest.mark.parametrize("lat", ["D2Q9", "D3Q15", "D3Q19", "D3Q27"])
+def test_equilibrium_moments(lat, oracle_mod):
+    # test_equilibrium.cpp:401-473: 20 random (rho, u); sum feq = rho and
+    # sum c feq = rho u to 1e-12.  A one-cell periodic domain streams onto
+    # itself, so its updateMacroscopic moments are those of the local feq.
+    O = oracle_mod
+    dim, q = O.LATTICE_DQ[lat]
+    rng = np.random.default_rng(12345)
+    n = (1, 1, 1) if dim == 3 else (1, 1)
+    for _ in range(20):
+        rho = np.array([1 + 0.1 * rng.uniform(-1, 1)])
+        u = rng.uniform(-0.1, 0.1, dim)
+        sim = O.OracleSim(O.Config(lat, n, omega=1.0), "port")
+        sim.init_fields(rho, u)
+        r2, u2 = sim.moments()
+        assert abs(r2[0] - rho[0]) < 1e-12
+        assert np.abs(u2 - u).max() < 1e-12
+
+
+@pytest.mark.parametrize("lat", ["D2Q9", "D3Q19", "D3Q27"])
+def test_uniform_force_regression(lat, oracle_mod):
+    # tests/regression/uniform_force/main.cpp: periodic, quiescent start,
+    # u_k = k F / rho after k steps, rho constant, to 1e-12.
+    O = oracle_mod
+    dim, q = O.LATTICE_DQ[lat]
+    n = (8, 8, 8) if dim == 3 else (8, 8)
+    F = (4e-4, -2e-4, 3e-4)[:dim] + (0.0,) * (3 - dim)
+    sim = O.OracleSim(O.Config(lat, n, omega=1.25, force=F), "port")
+    N = sim.N
+    sim.init_fields(np.ones(N), np.zeros(dim * N))
+    for k in range(1, 31):
+        sim.step(1)
+        if k % 5 == 0:
+            rho, u = sim.moments()
+            u = u.reshape(dim, N)
+            for d in range(dim):
+                assert np.abs(u[d] - k * F[d] / 1.0).max() < 1e-12
+            assert np.abs(rho - 1.0).max() < 1e-12
+
+
+def test_bc_corner_population_counts(oracle_mod):
+    # test_bc_corners.cpp:531-548, 670-685: the D2Q9 (-1,-1) corner ghost
+    # receives only the (1,1) population; the D3Q19 (-1,-1,-1) corner none.
+    O = oracle_mod
+    for lat, n, expect in (("D2Q9", (6, 6), 1), ("D3Q19", (4, 4, 4), 0)):
+        dim, q = O.LATTICE_DQ[lat]
+        cfg = O.Config(lat, n, omega=1.0, faces=["NoSlip"] * (2 * dim) + ["Periodic"] * (6 - 2 * dim))
+        sim = O.OracleSim(cfg, "port")
+        sim.set_f(np.random.default_rng(42).uniform(0.5, 1.5, q * sim.N))
+        sim.fill_ghosts()
+        g = sim.get_f_ghost().reshape(q, -1)
+        corner = 0  # first ghost cell (-1,-1[,-1])
+        assert int(np.isfinite(g[:, corner]).sum()) == expect
+
+
+def test_bc_priority_and_conflicts(oracle_mod):
+    # test_bc_corners.cpp:712-823 through the resolved table.
+    O = oracle_mod
+    cfg = O.Config("D2Q9", (4, 4), omega=1.0, faces=["NoSlip", "PressureOutlet", "NoSlip", "MovingWall", "Periodic", "Periodic"])
+    rc, t, r, U = O.resolve_bc(cfg)
+    assert rc == 0
+    # class index = (code_x + 1) + 3 (code_y + 1)
+    assert t[2 + 3 * 2] == O.BC["MovingWall"]      # MovingWall beats PressureOutlet
+    assert t[0 + 3 * 2] == O.BC["NoSlip"]          # NoSlip beats MovingWall
+    assert t[2 + 3 * 0] == O.BC["NoSlip"]          # NoSlip beats PressureOutlet
+    bad = O.Config("D2Q9", (4, 4), omega=1.0, faces=["Inflow", "Outflow", "PressureOutlet", "NoSlip", "Periodic", "Periodic"])
+    assert O.resolve_bc(bad)[0] != 0               # Outflow meets PressureOutlet at a corner
+    two_moving = O.Config("D2Q9", (4, 4), omega=1.0, faces=["MovingWall", "NoSlip", "NoSlip", "MovingWall", "Periodic", "Periodic"])
+    assert O.resolve_bc(two_moving)[0] != 0
