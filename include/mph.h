@@ -64,6 +64,12 @@ extern "C" {
 /* f_i - w_i stored as FP16 / BF16, FP32 collide arithmetic. */
 #define MPH_PREC_F16S 3
 #define MPH_PREC_BF16S 4
+/* 64-bit fixed-point storage of f_n / w_n (resolution 2^-56) with integer
+ * arithmetic on the INT32/IMAD pipes: FP64-accurate (agrees with the reference
+ * to ~1e-16 per step, tested at 1e-12 after N steps) at HBM speed on GB300,
+ * whose FP64 pipes run at 1/64 of the FP32 rate.  Conversions to FP64 happen
+ * only in mph_set_f / mph_get_f / moments / sums. */
+#define MPH_PREC_F64X 5
 
 /* ---- lattice-unit description of one domain ---------------------------- */
 typedef struct {

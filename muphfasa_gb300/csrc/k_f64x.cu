@@ -1,0 +1,279 @@
+// k_f64x.cu -- the FP64-accurate step on GB300's integer pipes.
+//
+// GB300 executes FP64 at 1/64 of its FP32 rate (2 DFMA per SM per clock), so
+// a D3Q19 cell update with ~170 FP64 operations is FP64-bound at ~15% of the
+// HBM roofline.  This kernel keeps each population as a 64-bit fixed-point
+// number h_n = f_n / w_n (resolution 2^-56 of a quantity of order one, far
+// finer than FP64's 2^-53 relative rounding) and does the BGK+Guo update with
+// integer adds and 64x64->high-64 multiplies (IMAD pipe):
+//
+//   rho = sum_k w_k S_k,  J = sum_k w_k (sum_{n in k} c_n h_n) + F/2
+//   r = 1/rho (FP32 seed + two fixed-point Newton steps), u = J r
+//   Pi = J u  (= rho u u),  A = rho - 1.5 tr(Pi)
+//   feq_n / w_n = A + 3 c_n.J + 4.5 c_n c_n : Pi              (adds only)
+//   guo_n / w_n = c_n.F' + 3 (c_n.u)(c_n.F') - u.F',  F' = 3 (1 - omega/2) F
+//   h_n' = h_n + omega (feq_n/w_n - h_n) + guo_n/w_n          (1 multiply)
+//
+// which is the reference's BGK + Guo update (Collision.cpp:55-92,
+// Collision.H:21-76, Equilibrium.H:43-57) in exact arithmetic; the rounding
+// of the reference's FP64 evaluation (~1e-16 per operation) is the only
+// difference, so results agree to ~1e-16 per step.  The HBM traffic is the
+// same 2*Q*8 bytes per cell update as FP64 storage.
+//
+// Range: |h| < 128, rho in (1/16, 64), |J|, |u| < 4; a cell outside sets
+// the handle's error flag (reported as MPH_ERR_NONFINITE by the host) instead
+// of producing silent wrap-around.
+#include "lbm_launch.h"
+
+namespace mph {
+
+namespace {
+
+using i64 = long long;
+using u64 = unsigned long long;
+
+// floor(a * b / 2^64) for signed a and unsigned b.
+__device__ __forceinline__ i64 mulhi_su(i64 a, u64 b) {
+    const u64 h = __umul64hi((u64)a, b);
+    return (i64)(h - (a < 0 ? b : 0ull));
+}
+// floor(a * b / 2^64), both signed.
+__device__ __forceinline__ i64 mulhi_ss(i64 a, i64 b) { return __mul64hi(a, b); }
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Value of the ghost population at g = x - c_n for cells next to a
+// non-periodic face, in the fixed-point representation (see
+// boundary_value in lbm_kernels.cuh for the rules and their reference).
+template <int Q>
+__device__ __noinline__ i64 boundary_value_x(const KParams* __restrict__ pg, const i64* __restrict__ kbb, int n,
+                                             int cls, const i64* __restrict__ fin, long long c) {
+    using L = Lat<Q>;
+    const long long N = pg->ncell;
+    const int t = pg->bc_type[cls];
+    const int o = L::opp(n);
+    if (t == kBcOutflow) return fin[n * N + c];
+    if (t == kBcPressure) {
+        const double v = boundary_value<Q, StF64X>(pg, n, cls, fin, c);
+        return __double2ll_rn(v * L::iw(n) * 0x1p56);
+    }
+    // bounce-back family: h(x, opp n) + contrib / w_n, the constant folded on
+    // the host from the reference's contrib (BCTypes/BounceBack.H:56-63).
+    return fin[o * N + c] + kbb[cls * 27 + n];
+}
+
+template <int Q>
+__device__ __forceinline__ void pull_x(const KParams& p, const KParams* __restrict__ pg, const i64* __restrict__ kbb,
+                                       const i64* __restrict__ fin, int x, int y, int z, long long c, i64* h) {
+    using L = Lat<Q>;
+    const bool interior = x > 0 && x < p.nx - 1 && y > 0 && y < p.ny - 1 && (L::D == 2 || (z > 0 && z < p.nz - 1));
+    if (interior) {
+        const long long plane = (long long)p.nx * p.ny;
+#pragma unroll
+        for (int n = 0; n < Q; ++n)
+            h[n] = __ldg(fin + n * p.ncell + c - (L::cx(n) + (long long)L::cy(n) * p.nx + L::cz(n) * plane));
+        return;
+    }
+#pragma unroll
+    for (int n = 0; n < Q; ++n) {
+        int gx = x - L::cx(n), gy = y - L::cy(n), gz = z - L::cz(n);
+        int k0 = 0, k1 = 0, k2 = 0;
+        if (gx < 0) { if (p.periodic[0]) gx += p.nx; else k0 = -1; }
+        else if (gx >= p.nx) { if (p.periodic[0]) gx -= p.nx; else k0 = 1; }
+        if (gy < 0) { if (p.periodic[1]) gy += p.ny; else k1 = -1; }
+        else if (gy >= p.ny) { if (p.periodic[1]) gy -= p.ny; else k1 = 1; }
+        if (L::D == 3) {
+            if (gz < 0) { if (p.periodic[2]) gz += p.nz; else k2 = -1; }
+            else if (gz >= p.nz) { if (p.periodic[2]) gz -= p.nz; else k2 = 1; }
+        }
+        if ((k0 | k1 | k2) == 0) {
+            h[n] = __ldg(fin + n * p.ncell + ((long long)gz * p.ny + gy) * p.nx + gx);
+        } else {
+            const int cls = (k0 + 1) + 3 * (k1 + 1) + (L::D == 3 ? 9 * (k2 + 1) : 0);
+            h[n] = boundary_value_x<Q>(pg, kbb, n, cls, fin, c);
+        }
+    }
+}
+
+template <int Q, bool FORCED>
+__device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) {
+    using L = Lat<Q>;
+    constexpr int D = L::D;
+    // Class sums of h and of c_a h (exact integer arithmetic).
+    i64 sr[4] = {0, 0, 0, 0};
+    i64 sj[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+    for (int n = 0; n < Q; ++n) {
+        const int k = wclass<Q>(n);
+        sr[k] += h[n];
+        const int c[3] = {L::cx(n), L::cy(n), L::cz(n)};
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            if (c[a] == 1) sj[k][a] += h[n];
+            else if (c[a] == -1) sj[k][a] -= h[n];
+        }
+    }
+    // Classes present in the lattice (compile time).
+    constexpr bool has[4] = {true, true, Q == 9 || Q == 19 || Q == 27, Q == 15 || Q == 27};
+    i64 rho = 0, J[3] = {0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (!has[k]) continue;
+        rho += mulhi_su(sr[k], px.Wc[k]);
+        if (k > 0)
+#pragma unroll
+            for (int a = 0; a < D; ++a) J[a] += mulhi_su(sj[k][a], px.Wc[k]);
+    }
+    if (FORCED)
+#pragma unroll
+        for (int a = 0; a < D; ++a) J[a] += px.hF[a];
+
+    // r = 1/rho in Q.60: FP32 seed, two Newton steps e = 1 - rho r, r += r e.
+    const float rf = (float)(int)(rho >> 32) * 0x1p-24f;
+    u64 R = (u64)(unsigned)(rcp_approx(rf) * 0x1p27f) << 33;
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const u64 P = __umul64hi((u64)rho, R);          // rho r in Q.52
+        const i64 e = (i64)((1ull << 52) - P);           // 1 - rho r in Q.52
+        R += (u64)(mulhi_su(e << 11, R) << 1);           // r e in Q.60
+    }
+    // u = J r (Q.56) and Pi = J u (Q.56).
+    i64 u[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a) u[a] = mulhi_su(J[a] << 5, R) >> 1;
+    i64 Pd[3] = {0, 0, 0}, Po[3] = {0, 0, 0};  // diagonal; off-diagonal (xy, xz, yz)
+#pragma unroll
+    for (int a = 0; a < D; ++a) Pd[a] = mulhi_ss(J[a] << 5, u[a] << 5) >> 2;
+    Po[0] = mulhi_ss(J[0] << 5, u[1] << 5) >> 2;
+    if (D == 3) {
+        Po[1] = mulhi_ss(J[0] << 5, u[2] << 5) >> 2;
+        Po[2] = mulhi_ss(J[1] << 5, u[2] << 5) >> 2;
+    }
+    {
+        // range guard for the shifts above
+        const u64 lim = 4ull << kFxShift;
+        bool ok = rho > (1ll << (kFxShift - 4)) && rho < (64ll << kFxShift);
+#pragma unroll
+        for (int a = 0; a < D; ++a) ok = ok && (u64)(J[a] + (i64)lim) < 2 * lim && (u64)(u[a] + (i64)lim) < 2 * lim;
+        bad |= !ok;
+    }
+    const i64 tr = Pd[0] + Pd[1] + Pd[2];
+    const i64 A = rho - (tr + (tr >> 1));
+    i64 J3[3], P45[3], P9[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        J3[a] = J[a] + (J[a] << 1);
+        P45[a] = (Pd[a] << 2) + (Pd[a] >> 1);
+        P9[a] = (Po[a] << 3) + Po[a];
+    }
+    // Guo terms: V_ab = u_a F'_b for the nonzero components of F'.
+    i64 uF = 0, Td[3] = {0, 0, 0}, To[3] = {0, 0, 0};
+    if (FORCED) {
+        i64 V[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+        for (int b = 0; b < D; ++b) {
+            if (!(px.fmask & (1 << b))) continue;
+#pragma unroll
+            for (int a = 0; a < D; ++a) V[a][b] = mulhi_ss(u[a] << 5, px.Fp[b] << 5) >> 2;
+        }
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            uF += V[a][a];
+            Td[a] = 3 * V[a][a];
+        }
+        To[0] = 3 * (V[0][1] + V[1][0]);
+        if (D == 3) {
+            To[1] = 3 * (V[0][2] + V[2][0]);
+            To[2] = 3 * (V[1][2] + V[2][1]);
+        }
+    }
+    const u64 W = px.W;  // omega/2 in Q0.64
+    {
+        const i64 d = A - h[0];
+        i64 o = h[0] + (mulhi_su(d, W) << 1);
+        if (FORCED) o -= uF;
+        h[0] = o;
+    }
+#pragma unroll
+    for (int n = 1; n < Q; ++n) {
+        const int m = L::opp(n);
+        if (m < n) continue;
+        const int c[3] = {L::cx(n), L::cy(n), L::cz(n)};
+        i64 E = A, O = 0, Eg = 0, Og = 0;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            if (c[a] == 0) continue;
+            E += P45[a];
+            O += (c[a] > 0) ? J3[a] : -J3[a];
+            if (FORCED) {
+                Eg += Td[a];
+                Og += (c[a] > 0) ? px.Fp[a] : -px.Fp[a];
+            }
+        }
+        // off-diagonal pairs (xy, xz, yz)
+        const int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int s = c[pa[k]] * c[pb[k]];
+            if (s == 0) continue;
+            E += (s > 0) ? P9[k] : -P9[k];
+            if (FORCED) Eg += (s > 0) ? To[k] : -To[k];
+        }
+        const i64 dn = (E + O) - h[n];
+        const i64 dm = (E - O) - h[m];
+        i64 on = h[n] + (mulhi_su(dn, W) << 1);
+        i64 om = h[m] + (mulhi_su(dm, W) << 1);
+        if (FORCED) {
+            on += (Eg - uF) + Og;
+            om += (Eg - uF) - Og;
+        }
+        h[n] = on;
+        h[m] = om;
+    }
+}
+
+template <int Q, bool FORCED>
+__global__ void __launch_bounds__(256) k_step_x(const i64* __restrict__ fin, i64* __restrict__ fout, const KParams p,
+                                                const KParamsX px, const KParams* __restrict__ pg,
+                                                const i64* __restrict__ kbb, int* __restrict__ flag) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x >= p.nx || y >= p.ny) return;
+    const long long c = ((long long)z * p.ny + y) * p.nx + x;
+    i64 h[Q];
+    pull_x<Q>(p, pg, kbb, fin, x, y, z, c, h);
+    int bad = 0;
+    collide_x<Q, FORCED>(px, h, bad);
+    if (bad) atomicOr(flag, 1);
+#pragma unroll
+    for (int n = 0; n < Q; ++n) fout[n * p.ncell + c] = h[n];
+}
+
+}  // namespace
+
+cudaError_t launch_step_f64x(int q, bool forced, const long long* fin, long long* fout, const KParams& p,
+                             const KParamsX& px, const KParams* pg, const long long* kbb, int* flag,
+                             cudaStream_t s) {
+    dim3 g, b;
+    step_shape(p, g, b);
+#define MPH_X_CASE(QQ)                                                                        \
+    case QQ:                                                                                  \
+        if (forced) k_step_x<QQ, true><<<g, b, 0, s>>>(fin, fout, p, px, pg, kbb, flag);     \
+        else k_step_x<QQ, false><<<g, b, 0, s>>>(fin, fout, p, px, pg, kbb, flag);           \
+        return cudaGetLastError();
+    switch (q) {
+        MPH_X_CASE(9)
+        MPH_X_CASE(15)
+        MPH_X_CASE(19)
+        MPH_X_CASE(27)
+    }
+#undef MPH_X_CASE
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace mph

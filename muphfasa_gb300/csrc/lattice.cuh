@@ -15,6 +15,8 @@ template <int Q> struct Lat;
 
 template <> struct Lat<9> {
     static constexpr int D = 2, Q = 9;
+    // exact inverse of the weight (w is 4/9, 1/9, 1/36, ...; 1/w is representable)
+    static MPH_HD constexpr double iw(int n) { return n == 0 ? 2.25 : (n < 5 ? 9.0 : 36.0); }
     static MPH_HD constexpr int cx(int n) { constexpr int t[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1}; return t[n]; }
     static MPH_HD constexpr int cy(int n) { constexpr int t[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1}; return t[n]; }
     static MPH_HD constexpr int cz(int) { return 0; }
@@ -28,6 +30,8 @@ template <> struct Lat<9> {
 
 template <> struct Lat<15> {
     static constexpr int D = 3, Q = 15;
+    // exact inverse of the weight (w is 4/9, 1/9, 1/36, ...; 1/w is representable)
+    static MPH_HD constexpr double iw(int n) { return n == 0 ? 4.5 : (n < 7 ? 9.0 : 72.0); }
     static MPH_HD constexpr int cx(int n) { constexpr int t[15] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, -1, 1}; return t[n]; }
     static MPH_HD constexpr int cy(int n) { constexpr int t[15] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, -1, 1, 1, -1}; return t[n]; }
     static MPH_HD constexpr int cz(int n) { constexpr int t[15] = {0, 0, 0, 0, 0, 1, -1, 1, -1, -1, 1, 1, -1, 1, -1}; return t[n]; }
@@ -42,6 +46,8 @@ template <> struct Lat<15> {
 
 template <> struct Lat<19> {
     static constexpr int D = 3, Q = 19;
+    // exact inverse of the weight (w is 4/9, 1/9, 1/36, ...; 1/w is representable)
+    static MPH_HD constexpr double iw(int n) { return n == 0 ? 3.0 : (n < 7 ? 18.0 : 36.0); }
     static MPH_HD constexpr int cx(int n) { constexpr int t[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0}; return t[n]; }
     static MPH_HD constexpr int cy(int n) { constexpr int t[19] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 1, -1}; return t[n]; }
     static MPH_HD constexpr int cz(int n) { constexpr int t[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0, -1, 1, -1, 1}; return t[n]; }
@@ -57,6 +63,8 @@ template <> struct Lat<19> {
 
 template <> struct Lat<27> {
     static constexpr int D = 3, Q = 27;
+    // exact inverse of the weight (w is 4/9, 1/9, 1/36, ...; 1/w is representable)
+    static MPH_HD constexpr double iw(int n) { return n == 0 ? 3.375 : (n < 7 ? 13.5 : (n < 19 ? 54.0 : 216.0)); }
     static MPH_HD constexpr int cx(int n) {
         constexpr int t[27] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 1, -1, -1, 1};
         return t[n];
@@ -82,5 +90,11 @@ template <> struct Lat<27> {
         return t[n];
     }
 };
+
+// Weight class of population n: |c_n|^2 (0 rest, 1 face, 2 edge, 3 corner).
+template <int Q>
+MPH_HD constexpr int wclass(int n) {
+    return Lat<Q>::cx(n) * Lat<Q>::cx(n) + Lat<Q>::cy(n) * Lat<Q>::cy(n) + Lat<Q>::cz(n) * Lat<Q>::cz(n);
+}
 
 }  // namespace mph

@@ -47,6 +47,15 @@ struct KParams {
     double bc_U[27][3];
 };
 
+// Extra constants of the fixed-point step (k_f64x.cu).
+struct KParamsX {
+    unsigned long long W;      // omega / 2 in Q0.64
+    unsigned long long Wc[4];  // weight of the class |c|^2 = 0..3 in Q0.64
+    long long hF[3];           // F / 2 in Q.56
+    long long Fp[3];           // 3 (1 - omega/2) F in Q.56 (Guo prefactor folded in)
+    int fmask;                 // bit b set when Fp[b] != 0
+};
+
 // ---------------------------------------------------------------------------
 // Storage policies: how a population is kept in HBM and the compute type R.
 // ---------------------------------------------------------------------------
@@ -59,6 +68,8 @@ struct StF64 {
     template <int Q> static __device__ __forceinline__ void st(T* __restrict__ f, int n, long long i, long long N, R v) {
         f[n * N + i] = v;
     }
+    // Value that a store followed by a load returns.
+    template <int Q> static __device__ __forceinline__ R rt(int, R v) { return v; }
 };
 struct StF32 {
     using T = float;
@@ -69,6 +80,7 @@ struct StF32 {
     template <int Q> static __device__ __forceinline__ void st(T* __restrict__ f, int n, long long i, long long N, R v) {
         f[n * N + i] = v;
     }
+    template <int Q> static __device__ __forceinline__ R rt(int, R v) { return v; }
 };
 // Shifted 16-bit storage: the deviation f_n - w_n is stored, so that the
 // 11 (FP16) or 8 (BF16) significant bits resolve the small departure from the
@@ -82,6 +94,9 @@ struct StF16S {
     template <int Q> static __device__ __forceinline__ void st(T* __restrict__ f, int n, long long i, long long N, R v) {
         f[n * N + i] = __float2half_rn(v - (float)Lat<Q>::w(n));
     }
+    template <int Q> static __device__ __forceinline__ R rt(int n, R v) {
+        return __half2float(__float2half_rn(v - (float)Lat<Q>::w(n))) + (float)Lat<Q>::w(n);
+    }
 };
 struct StBF16S {
     using T = __nv_bfloat16;
@@ -91,6 +106,28 @@ struct StBF16S {
     }
     template <int Q> static __device__ __forceinline__ void st(T* __restrict__ f, int n, long long i, long long N, R v) {
         f[n * N + i] = __float2bfloat16_rn(v - (float)Lat<Q>::w(n));
+    }
+    template <int Q> static __device__ __forceinline__ R rt(int n, R v) {
+        return __bfloat162float(__float2bfloat16_rn(v - (float)Lat<Q>::w(n))) + (float)Lat<Q>::w(n);
+    }
+};
+
+// 64-bit fixed point (MPH_PREC_F64X): the stored integer is h_n = f_n / w_n
+// in units of 2^-56.  Loads and stores convert to/from FP64 for the
+// auxiliary kernels (moments, init, sums, host transfers); the step kernel of
+// k_f64x.cu works on the integers directly.
+constexpr int kFxShift = 56;
+struct StF64X {
+    using T = long long;
+    using R = double;
+    template <int Q> static __device__ __forceinline__ R ld(const T* __restrict__ f, int n, long long i, long long N) {
+        return ((double)__ldg(f + n * N + i) * 0x1p-56) / Lat<Q>::iw(n);
+    }
+    template <int Q> static __device__ __forceinline__ void st(T* __restrict__ f, int n, long long i, long long N, R v) {
+        f[n * N + i] = __double2ll_rn(v * Lat<Q>::iw(n) * 0x1p56);
+    }
+    template <int Q> static __device__ __forceinline__ R rt(int n, R v) {
+        return ((double)__double2ll_rn(v * Lat<Q>::iw(n) * 0x1p56) * 0x1p-56) / Lat<Q>::iw(n);
     }
 };
 
@@ -435,9 +472,11 @@ __global__ void __launch_bounds__(256) k_init(typename St::T* __restrict__ fout,
         St::template st<Q>(fout, n, c, p.ncell, (typename St::R)f[n]);
     }
     if (FORCED) {
+        // moments of the stored values (as a reload would return them; the
+        // read-only cache path must not re-read memory this kernel wrote)
         double fs[Q];
 #pragma unroll
-        for (int n = 0; n < Q; ++n) fs[n] = (double)St::template ld<Q>(fout, n, c, p.ncell);
+        for (int n = 0; n < Q; ++n) fs[n] = (double)St::template rt<Q>(n, (typename St::R)f[n]);
         double r, uu[3];
         moments_exact<Q, true>(p, fs, r, uu);
         rho_io[c] = r;

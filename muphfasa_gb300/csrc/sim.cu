@@ -2,6 +2,7 @@
 // populations (two SoA buffers swapped every step, the A/B pattern of
 // SimulationImpl's m_fin/m_fout), one CUDA stream, and the ISimulation
 // operations (ISimulation.H:16-44) mapped onto the kernels.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -16,7 +17,10 @@ struct mph_sim {
     mph_desc d;
     mph_resolved_bc table[27];
     KParams kp;
+    KParamsX kpx;             // fixed-point constants (MPH_PREC_F64X)
     KParams* d_kp = nullptr;  // global copy for the boundary path
+    long long* d_kbb = nullptr;  // fixed-point bounce-back constants [27][27]
+    int* d_flag = nullptr;       // range / validity flag of the fixed-point step
     size_t elem = 8;          // bytes per stored population value
     void* fa = nullptr;       // current populations (m_fin)
     void* fb = nullptr;       // next populations (m_fout)
@@ -47,7 +51,8 @@ int cuda_fail(cudaError_t e, const char* what) {
 size_t elem_size(int prec) {
     switch (prec) {
         case MPH_PREC_F64:
-        case MPH_PREC_F64_FAST: return 8;
+        case MPH_PREC_F64_FAST:
+        case MPH_PREC_F64X: return 8;
         case MPH_PREC_F32: return 4;
         case MPH_PREC_F16S:
         case MPH_PREC_BF16S: return 2;
@@ -93,11 +98,55 @@ void build_params(const mph_desc& d, const mph_resolved_bc* tab, KParams& kp) {
     }
 }
 
+// Q0.64 of the weight 1/iw (iw*8 is an integer for every lattice weight).
+unsigned long long weight_q64(double iw) {
+    const unsigned long long den = (unsigned long long)(iw * 8.0);
+    const unsigned __int128 num = (unsigned __int128)1 << 67;
+    return (unsigned long long)(num / den);
+}
+
+template <int Q>
+void fixed_params(const mph_sim* s, KParamsX& px, long long* kbb) {
+    using L = Lat<Q>;
+    std::memset(&px, 0, sizeof(px));
+    px.W = (unsigned long long)std::ldexp(0.5 * s->d.omega, 64);
+    double iw_class[4] = {L::iw(0), 0.0, 0.0, 0.0};
+    for (int n = 1; n < Q; ++n) iw_class[wclass<Q>(n)] = L::iw(n);
+    for (int k = 0; k < 4; ++k) px.Wc[k] = iw_class[k] > 0.0 ? weight_q64(iw_class[k]) : 0ull;
+    const double pre = 3.0 * (1.0 - 0.5 * s->d.omega);
+    for (int a = 0; a < 3; ++a) {
+        px.hF[a] = std::llrint(std::ldexp(s->kp.hF[a], 56));
+        px.Fp[a] = std::llrint(std::ldexp(pre * s->kp.F[a], 56));
+        if (px.Fp[a] != 0) px.fmask |= 1 << a;
+    }
+    // h-space bounce-back constants: contrib(opp n) / w_n with the
+    // reference's contrib (BCTypes/BounceBack.H:56-63) evaluated in FP64.
+    for (int c = 0; c < 27; ++c)
+        for (int n = 0; n < 27; ++n) {
+            kbb[c * 27 + n] = 0;
+            const int t = s->table[c].type;
+            if (n >= Q || !(t == MPH_BC_MOVING_WALL || t == MPH_BC_NO_SLIP || t == MPH_BC_INFLOW)) continue;
+            const int o = L::opp(n);
+            double rho = 1, U[3] = {0., 0., 0.};
+            if (t != MPH_BC_NO_SLIP) {
+                rho = s->table[c].rho;
+                for (int a = 0; a < 3; ++a) U[a] = s->table[c].U[a];
+            }
+            double cdotu;
+            if (L::D == 2) cdotu = L::cx(o) * U[0] + L::cy(o) * U[1];
+            else cdotu = L::cx(o) * U[0] + L::cy(o) * U[1] + L::cz(o) * U[2];
+            const double contrib = -2. * rho * L::w(o) * cdotu * 3.0;
+            kbb[c * 27 + n] = std::llrint(std::ldexp(contrib * L::iw(n), 56));
+        }
+}
+
 void free_all(mph_sim* s) {
     if (!s) return;
     cudaFree(s->fa);
     cudaFree(s->fb);
     cudaFree(s->d_kp);
+    cudaFree(s->d_kbb);
+    cudaFree(s->d_flag);
     cudaFree(s->d_rho);
     cudaFree(s->d_u);
     cudaFree(s->d_stage);
@@ -135,8 +184,22 @@ cudaError_t launch_one_step(mph_sim* s) {
             return launch_step_fast_f16s(q, forced, s->fa, s->fb, s->kp, s->d_kp, s->stream);
         case MPH_PREC_BF16S:
             return launch_step_fast_bf16s(q, forced, s->fa, s->fb, s->kp, s->d_kp, s->stream);
+        case MPH_PREC_F64X:
+            return launch_step_f64x(q, forced, (const long long*)s->fa, (long long*)s->fb, s->kp, s->kpx, s->d_kp,
+                                    s->d_kbb, s->d_flag, s->stream);
     }
     return cudaErrorInvalidValue;
+}
+
+// Range flag of the fixed-point step: a cell left the representable range.
+int check_flag(mph_sim* s) {
+    if (s->d.precision != MPH_PREC_F64X) return MPH_OK;
+    int flag = 0;
+    MPH_CK(cudaMemcpyAsync(&flag, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "read flag");
+    MPH_CK(cudaStreamSynchronize(s->stream), "read flag");
+    if (flag) return fail(MPH_ERR_NONFINITE, "fixed-point step: a cell left the representable range "
+                                               "(rho outside (1/16, 64) or |J|, |u| >= 4)");
+    return MPH_OK;
 }
 
 int advance_async(mph_sim* s, int nsteps) {
@@ -212,6 +275,10 @@ int mph_create(const mph_desc* desc, mph_sim** out) {
     if ((d.dim == 3 ? d.n[2] : 1) > 65535 || (d.n[1] + 7) / 8 > 65535)
         return fail(MPH_ERR_ARG, "mph_create: ny or nz exceeds the launch grid limit (65535)");
     if (!(d.omega > 0.0 && d.omega < 2.0)) return fail(MPH_ERR_CONFIG, "mph_create: omega must lie in (0, 2)");
+    if (d.precision == MPH_PREC_F64X && d.forced)
+        for (int a = 0; a < d.dim; ++a)
+            if (!(std::fabs(d.force[a]) < 0.5))
+                return fail(MPH_ERR_CONFIG, "mph_create: fixed-point precision needs |force| < 0.5");
     auto* s = new mph_sim();
     s->d = d;
     if (d.dim == 2) s->d.n[2] = 1;
@@ -227,6 +294,19 @@ int mph_create(const mph_desc* desc, mph_sim** out) {
     if (e == cudaSuccess) e = cudaMalloc(&s->fb, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_kp, sizeof(KParams));
     if (e == cudaSuccess) e = cudaMemcpy(s->d_kp, &s->kp, sizeof(KParams), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && d.precision == MPH_PREC_F64X) {
+        long long kbb[27 * 27];
+        switch (d.q) {
+            case 9: fixed_params<9>(s, s->kpx, kbb); break;
+            case 15: fixed_params<15>(s, s->kpx, kbb); break;
+            case 19: fixed_params<19>(s, s->kpx, kbb); break;
+            case 27: fixed_params<27>(s, s->kpx, kbb); break;
+        }
+        e = cudaMalloc(&s->d_kbb, sizeof(kbb));
+        if (e == cudaSuccess) e = cudaMemcpy(s->d_kbb, kbb, sizeof(kbb), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMalloc(&s->d_flag, sizeof(int));
+        if (e == cudaSuccess) e = cudaMemset(s->d_flag, 0, sizeof(int));
+    }
     s->red_blocks = 152 * 4;
     if (e == cudaSuccess) e = cudaMalloc(&s->d_part, sizeof(double) * 4 * s->red_blocks);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_red, sizeof(double) * 4);
@@ -286,7 +366,9 @@ int mph_advance(mph_sim* s, int nsteps) {
     if (!s->has_state) return fail(MPH_ERR_STATE, "mph_advance: no populations yet");
     int rc = advance_async(s, nsteps);
     if (rc) return rc;
-    return sync(s, "mph_advance");
+    rc = sync(s, "mph_advance");
+    if (rc) return rc;
+    return check_flag(s);
 }
 
 int mph_advance_timed(mph_sim* s, int nsteps, float* ms) {
@@ -298,7 +380,7 @@ int mph_advance_timed(mph_sim* s, int nsteps, float* ms) {
     MPH_CK(cudaEventRecord(s->ev1, s->stream), "event record");
     MPH_CK(cudaEventSynchronize(s->ev1), "event sync");
     MPH_CK(cudaEventElapsedTime(ms, s->ev0, s->ev1), "event elapsed");
-    return MPH_OK;
+    return check_flag(s);
 }
 
 int mph_update_macroscopic(mph_sim* s, double* rho, double* u) {
@@ -344,7 +426,9 @@ int mph_step_host(mph_sim* s, const double* f_in, double* f_out, int nsteps) {
     if (rc) return rc;
     rc = download(s, f_out);
     if (rc) return rc;
-    return sync(s, "mph_step_host");
+    rc = sync(s, "mph_step_host");
+    if (rc) return rc;
+    return check_flag(s);
 }
 
 // ---- plugin level ------------------------------------------------------

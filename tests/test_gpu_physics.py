@@ -51,6 +51,38 @@ def channel_init(n, rng):
 CH_FACES = ["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic", "Periodic"]
 
 
+def test_channel_d3q19_64cubed_2000_steps_f64x(mph, oracle_mod):
+    n, steps = (64, 64, 64), 2000
+    O = oracle_mod
+    F = (1e-6, 0.0, 0.0)
+    o = O.OracleSim(O.Config("D3Q19", n, omega=1.0 / 0.6, faces=CH_FACES, force=F), "port")
+    s = mph.Simulation(mph.make_desc("D3Q19", n, 1.0 / 0.6, faces=CH_FACES, force=F, precision="f64x"))
+    rho, u = channel_init(n, np.random.default_rng(2025))
+    o.init_fields(rho, u)
+    s.initialize(rho, u)
+    o.step(steps, nthreads=16)
+    s.advance(steps)
+    fo = o.get_f()
+    err = float(np.max(np.abs(s.f() - fo) / np.abs(fo)))
+    print(f"f64x 64^3 channel {steps} steps: max rel err {err:.3e}")
+    assert err < 1e-12
+
+
+def test_tgv2d_256_5000_steps_f64x(mph, oracle_mod):
+    N, steps, tau, u0 = 256, 5000, 0.8, 0.05
+    o = oracle_mod.OracleSim(oracle_mod.Config("D2Q9", (N, N), omega=1.0 / tau), "port")
+    s = mph.Simulation(mph.make_desc("D2Q9", (N, N), 1.0 / tau, precision="f64x"))
+    rho, u = tgv_fields(N, u0)
+    o.init_fields(rho, u)
+    s.initialize(rho, u)
+    o.step(steps, nthreads=16)
+    s.advance(steps)
+    fo = o.get_f()
+    err = float(np.max(np.abs(s.f() - fo) / np.abs(fo)))
+    print(f"f64x TGV 256^2 {steps} steps: max rel err {err:.3e}")
+    assert err < 1e-12
+
+
 def test_channel_d3q19_64cubed_2000_steps_bitwise(mph, oracle_mod):
     n, steps = (64, 64, 64), 2000
     O = oracle_mod
@@ -66,7 +98,7 @@ def test_channel_d3q19_64cubed_2000_steps_bitwise(mph, oracle_mod):
     assert np.array_equal(o.get_f(), s.f())
 
 
-@pytest.mark.parametrize("prec,tol", [("f64", 1e-12), ("f64_fast", 1e-12)])
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-12), ("f64_fast", 1e-12), ("f64x", 1e-12)])
 def test_channel_d3q19_256cubed_vs_oracle(prec, tol, mph, oracle_mod):
     n, steps = (256, 256, 256), 100
     O = oracle_mod
