@@ -20,9 +20,9 @@
 // difference, so results agree to ~1e-16 per step.  The HBM traffic is the
 // same 2*Q*8 bytes per cell update as FP64 storage.
 //
-// Range: |h| < 128, rho in (1/16, 64), |J|, |u| < 4; a cell outside sets
-// the handle's error flag (reported as MPH_ERR_NONFINITE by the host) instead
-// of producing silent wrap-around.
+// Range: class sums of h within +-128, rho in (1/16, 64), |J|, |u| < 4 and
+// |feq/w - h| < 64; a cell outside sets the handle's error flag (reported as
+// MPH_ERR_NONFINITE by the host) instead of producing silent wrap-around.
 #include "lbm_launch.h"
 
 namespace mph {
@@ -99,6 +99,13 @@ __device__ __forceinline__ void pull_x(const KParams& p, const KParams* __restri
     }
 }
 
+// Products are formed with one or two extra fraction bits and rounded by
+// (t + 1) >> 1 or (t + 2) >> 2: the 64x64 high-half multiply truncates, and a
+// truncation bias would accumulate in the conserved mass over many steps,
+// while rounded errors stay unbiased like the reference's FP64 rounding.
+__device__ __forceinline__ i64 rnd1(i64 t) { return (t + 1) >> 1; }
+__device__ __forceinline__ i64 rnd2(i64 t) { return (t + 2) >> 2; }
+
 template <int Q, bool FORCED>
 __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) {
     using L = Lat<Q>;
@@ -119,14 +126,15 @@ __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) 
     }
     // Classes present in the lattice (compile time).
     constexpr bool has[4] = {true, true, Q == 9 || Q == 19 || Q == 27, Q == 15 || Q == 27};
+    // rho = sum_k w_k S_k and J = sum_k w_k (sum c h) [+ F/2]; Wc holds 2 w_k.
     i64 rho = 0, J[3] = {0, 0, 0};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         if (!has[k]) continue;
-        rho += mulhi_su(sr[k], px.Wc[k]);
+        rho += rnd1(mulhi_su(sr[k], px.Wc[k]));
         if (k > 0)
 #pragma unroll
-            for (int a = 0; a < D; ++a) J[a] += mulhi_su(sj[k][a], px.Wc[k]);
+            for (int a = 0; a < D; ++a) J[a] += rnd1(mulhi_su(sj[k][a], px.Wc[k]));
     }
     if (FORCED)
 #pragma unroll
@@ -141,20 +149,20 @@ __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) 
         const i64 e = (i64)((1ull << 52) - P);           // 1 - rho r in Q.52
         R += (u64)(mulhi_su(e << 11, R) << 1);           // r e in Q.60
     }
-    // u = J r (Q.56) and Pi = J u (Q.56).
+    // u = J r and Pi = J u, Q.56.
     i64 u[3] = {0, 0, 0};
 #pragma unroll
-    for (int a = 0; a < D; ++a) u[a] = mulhi_su(J[a] << 5, R) >> 1;
+    for (int a = 0; a < D; ++a) u[a] = rnd1(mulhi_su(J[a] << 5, R));
     i64 Pd[3] = {0, 0, 0}, Po[3] = {0, 0, 0};  // diagonal; off-diagonal (xy, xz, yz)
 #pragma unroll
-    for (int a = 0; a < D; ++a) Pd[a] = mulhi_ss(J[a] << 5, u[a] << 5) >> 2;
-    Po[0] = mulhi_ss(J[0] << 5, u[1] << 5) >> 2;
+    for (int a = 0; a < D; ++a) Pd[a] = rnd2(mulhi_ss(J[a] << 5, u[a] << 5));
+    Po[0] = rnd2(mulhi_ss(J[0] << 5, u[1] << 5));
     if (D == 3) {
-        Po[1] = mulhi_ss(J[0] << 5, u[2] << 5) >> 2;
-        Po[2] = mulhi_ss(J[1] << 5, u[2] << 5) >> 2;
+        Po[1] = rnd2(mulhi_ss(J[0] << 5, u[2] << 5));
+        Po[2] = rnd2(mulhi_ss(J[1] << 5, u[2] << 5));
     }
     {
-        // range guard for the shifts above
+        // range guard of the shifts above: rho in (1/16, 64), |J|, |u| < 4
         const u64 lim = 4ull << kFxShift;
         bool ok = rho > (1ll << (kFxShift - 4)) && rho < (64ll << kFxShift);
 #pragma unroll
@@ -162,12 +170,12 @@ __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) 
         bad |= !ok;
     }
     const i64 tr = Pd[0] + Pd[1] + Pd[2];
-    const i64 A = rho - (tr + (tr >> 1));
+    const i64 A = rho - (tr + rnd1(tr));
     i64 J3[3], P45[3], P9[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         J3[a] = J[a] + (J[a] << 1);
-        P45[a] = (Pd[a] << 2) + (Pd[a] >> 1);
+        P45[a] = (Pd[a] << 2) + rnd1(Pd[a]);
         P9[a] = (Po[a] << 3) + Po[a];
     }
     // Guo terms: V_ab = u_a F'_b for the nonzero components of F'.
@@ -178,7 +186,7 @@ __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) 
         for (int b = 0; b < D; ++b) {
             if (!(px.fmask & (1 << b))) continue;
 #pragma unroll
-            for (int a = 0; a < D; ++a) V[a][b] = mulhi_ss(u[a] << 5, px.Fp[b] << 5) >> 2;
+            for (int a = 0; a < D; ++a) V[a][b] = rnd2(mulhi_ss(u[a] << 5, px.Fp[b] << 5));
         }
 #pragma unroll
         for (int a = 0; a < D; ++a) {
@@ -191,10 +199,13 @@ __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) 
             To[2] = 3 * (V[1][2] + V[2][1]);
         }
     }
-    const u64 W = px.W;  // omega/2 in Q0.64
+    // omega d = rnd1(mulhi(2 d, omega/2)); |d| < 64 keeps 2 d representable.
+    const u64 W = px.W;
+    u64 dmag = 0;
     {
         const i64 d = A - h[0];
-        i64 o = h[0] + (mulhi_su(d, W) << 1);
+        dmag |= (u64)(d + (1ll << 61));
+        i64 o = h[0] + rnd1(mulhi_su(d << 1, W));
         if (FORCED) o -= uF;
         h[0] = o;
     }
@@ -218,15 +229,16 @@ __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) 
         const int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            const int s = c[pa[k]] * c[pb[k]];
-            if (s == 0) continue;
-            E += (s > 0) ? P9[k] : -P9[k];
-            if (FORCED) Eg += (s > 0) ? To[k] : -To[k];
+            const int sg = c[pa[k]] * c[pb[k]];
+            if (sg == 0) continue;
+            E += (sg > 0) ? P9[k] : -P9[k];
+            if (FORCED) Eg += (sg > 0) ? To[k] : -To[k];
         }
         const i64 dn = (E + O) - h[n];
         const i64 dm = (E - O) - h[m];
-        i64 on = h[n] + (mulhi_su(dn, W) << 1);
-        i64 om = h[m] + (mulhi_su(dm, W) << 1);
+        dmag |= (u64)(dn + (1ll << 61)) | (u64)(dm + (1ll << 61));
+        i64 on = h[n] + rnd1(mulhi_su(dn << 1, W));
+        i64 om = h[m] + rnd1(mulhi_su(dm << 1, W));
         if (FORCED) {
             on += (Eg - uF) + Og;
             om += (Eg - uF) - Og;
@@ -234,6 +246,7 @@ __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) 
         h[n] = on;
         h[m] = om;
     }
+    bad |= (dmag >> 62) != 0;
 }
 
 template <int Q, bool FORCED>

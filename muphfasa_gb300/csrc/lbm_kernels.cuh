@@ -50,7 +50,7 @@ struct KParams {
 // Extra constants of the fixed-point step (k_f64x.cu).
 struct KParamsX {
     unsigned long long W;      // omega / 2 in Q0.64
-    unsigned long long Wc[4];  // weight of the class |c|^2 = 0..3 in Q0.64
+    unsigned long long Wc[4];  // twice the weight of the class |c|^2 = 0..3, Q0.64
     long long hF[3];           // F / 2 in Q.56
     long long Fp[3];           // 3 (1 - omega/2) F in Q.56 (Guo prefactor folded in)
     int fmask;                 // bit b set when Fp[b] != 0

@@ -98,11 +98,12 @@ void build_params(const mph_desc& d, const mph_resolved_bc* tab, KParams& kp) {
     }
 }
 
-// Q0.64 of the weight 1/iw (iw*8 is an integer for every lattice weight).
-unsigned long long weight_q64(double iw) {
-    const unsigned long long den = (unsigned long long)(iw * 8.0);
-    const unsigned __int128 num = (unsigned __int128)1 << 67;
-    return (unsigned long long)(num / den);
+// Q0.64 of twice the weight, 2/iw, rounded to nearest (iw*8 is an integer
+// for every lattice weight and 2 w <= 8/9 < 1).
+unsigned long long weight2_q64(double iw) {
+    const unsigned __int128 den = (unsigned __int128)(iw * 8.0);
+    const unsigned __int128 num = (unsigned __int128)1 << 68;
+    return (unsigned long long)((num + den / 2) / den);
 }
 
 template <int Q>
@@ -112,7 +113,7 @@ void fixed_params(const mph_sim* s, KParamsX& px, long long* kbb) {
     px.W = (unsigned long long)std::ldexp(0.5 * s->d.omega, 64);
     double iw_class[4] = {L::iw(0), 0.0, 0.0, 0.0};
     for (int n = 1; n < Q; ++n) iw_class[wclass<Q>(n)] = L::iw(n);
-    for (int k = 0; k < 4; ++k) px.Wc[k] = iw_class[k] > 0.0 ? weight_q64(iw_class[k]) : 0ull;
+    for (int k = 0; k < 4; ++k) px.Wc[k] = iw_class[k] > 0.0 ? weight2_q64(iw_class[k]) : 0ull;
     const double pre = 3.0 * (1.0 - 0.5 * s->d.omega);
     for (int a = 0; a < 3; ++a) {
         px.hF[a] = std::llrint(std::ldexp(s->kp.hF[a], 56));
