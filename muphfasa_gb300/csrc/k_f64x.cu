@@ -21,7 +21,7 @@
 // same 2*Q*8 bytes per cell update as FP64 storage.
 //
 // Range: class sums of h within +-128, rho in (1/16, 64), |J|, |u| < 4 and
-// |feq/w - h| < 64; a cell outside sets the handle's error flag (reported as
+// |feq/w - h| < 32; a cell outside sets the handle's error flag (reported as
 // MPH_ERR_NONFINITE by the host) instead of producing silent wrap-around.
 #include "lbm_launch.h"
 
@@ -199,13 +199,14 @@ __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) 
             To[2] = 3 * (V[1][2] + V[2][1]);
         }
     }
-    // omega d = rnd1(mulhi(2 d, omega/2)); |d| < 64 keeps 2 d representable.
+    // omega d: mulhi(4 d, omega/2) is omega d with one extra fraction bit,
+    // rounded by rnd1; |d| < 32 keeps 4 d representable (checked below).
     const u64 W = px.W;
     u64 dmag = 0;
     {
         const i64 d = A - h[0];
         dmag |= (u64)(d + (1ll << 61));
-        i64 o = h[0] + rnd1(mulhi_su(d << 1, W));
+        i64 o = h[0] + rnd1(mulhi_su(d << 2, W));
         if (FORCED) o -= uF;
         h[0] = o;
     }
@@ -237,8 +238,8 @@ __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) 
         const i64 dn = (E + O) - h[n];
         const i64 dm = (E - O) - h[m];
         dmag |= (u64)(dn + (1ll << 61)) | (u64)(dm + (1ll << 61));
-        i64 on = h[n] + rnd1(mulhi_su(dn << 1, W));
-        i64 om = h[m] + rnd1(mulhi_su(dm << 1, W));
+        i64 on = h[n] + rnd1(mulhi_su(dn << 2, W));
+        i64 om = h[m] + rnd1(mulhi_su(dm << 2, W));
         if (FORCED) {
             on += (Eg - uF) + Og;
             om += (Eg - uF) - Og;
