@@ -105,11 +105,33 @@ __device__ __forceinline__ void pull_x(const KParams& p, const KParams* __restri
 // while rounded errors stay unbiased like the reference's FP64 rounding.
 __device__ __forceinline__ i64 rnd1(i64 t) { return (t + 1) >> 1; }
 __device__ __forceinline__ i64 rnd2(i64 t) { return (t + 2) >> 2; }
+__device__ __forceinline__ i64 rnd4(i64 t) { return (t + 8) >> 4; }
+
+// omega * d in Q.56, rounded to nearest.  W = omega/2 in Q0.64 with its low
+// bit clear, wh1 = W/2 - 1.  With the sign bit of 4d flipped the operand is
+// 4d + 2^63 >= 0, so one unsigned high multiply gives
+// floor(4 d W / 2^64) + W/2 = floor(2 omega d) + W/2 (omega d with one extra
+// fraction bit plus a known integer), and (t - wh1) >> 1 rounds it.
+__device__ __forceinline__ i64 omega_mul(i64 d, u64 W, u64 wh1) {
+    const u64 t = __umul64hi((u64)(d << 2) ^ (1ull << 63), W);
+    return (i64)(t - wh1) >> 1;
+}
+
+// Weight of class k (|c|^2 = k) as a multiple of the smallest weight of the
+// lattice: every lattice's weights are integer multiples of its smallest.
+template <int Q>
+__device__ __forceinline__ constexpr int wratio(int k) {
+    return Q == 9 ? (k == 0 ? 16 : k == 1 ? 4 : 1)
+         : Q == 15 ? (k == 0 ? 16 : k == 1 ? 8 : 1)
+         : Q == 19 ? (k == 0 ? 12 : k == 1 ? 2 : 1)
+                   : (k == 0 ? 64 : k == 1 ? 16 : k == 2 ? 4 : 1);
+}
 
 template <int Q, bool FORCED>
 __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) {
     using L = Lat<Q>;
     constexpr int D = L::D;
+    constexpr bool has[4] = {true, true, Q == 9 || Q == 19 || Q == 27, Q == 15 || Q == 27};
     // Class sums of h and of c_a h (exact integer arithmetic).
     i64 sr[4] = {0, 0, 0, 0};
     i64 sj[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
@@ -124,42 +146,50 @@ __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) 
             else if (c[a] == -1) sj[k][a] -= h[n];
         }
     }
-    // Classes present in the lattice (compile time).
-    constexpr bool has[4] = {true, true, Q == 9 || Q == 19 || Q == 27, Q == 15 || Q == 27};
-    // rho = sum_k w_k S_k and J = sum_k w_k (sum c h) [+ F/2]; Wc holds 2 w_k.
-    i64 rho = 0, J[3] = {0, 0, 0};
+    // rho = w_min sum_k r_k S_k and J_a = w_min sum_k r_k T_ka (+ F_a/2):
+    // the weighted sums are formed in Q.52 (headroom for r_k up to 64) and
+    // multiplied once by Wm = 32 w_min (Q0.64) -> Q.57, rounded to Q.56.
+    i64 rq = 0, jq[3] = {0, 0, 0};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         if (!has[k]) continue;
-        rho += rnd1(mulhi_su(sr[k], px.Wc[k]));
-        if (k > 0)
+        rq += wratio<Q>(k) * rnd4(sr[k]);
 #pragma unroll
-            for (int a = 0; a < D; ++a) J[a] += rnd1(mulhi_su(sj[k][a], px.Wc[k]));
+        for (int a = 0; a < D; ++a)
+            if (k > 0) jq[a] += wratio<Q>(k) * rnd4(sj[k][a]);
     }
-    if (FORCED)
+    const i64 rho = rnd1(mulhi_su(rq, px.Wm));
+    i64 J[3] = {0, 0, 0};
 #pragma unroll
-        for (int a = 0; a < D; ++a) J[a] += px.hF[a];
-
-    // r = 1/rho in Q.60: FP32 seed, two Newton steps e = 1 - rho r, r += r e.
+    for (int a = 0; a < D; ++a) {
+        J[a] = rnd1(mulhi_su(jq[a], px.Wm));
+        if (FORCED) J[a] += px.hF[a];
+    }
+    // r = 1/rho in Q.60: FP32 seed (~2^-22) and one Newton step (~2^-44);
+    // u only enters through Pi = J u and the force terms, where this
+    // precision contributes < 1e-19 absolute.
     const float rf = (float)(int)(rho >> 32) * 0x1p-24f;
     u64 R = (u64)(unsigned)(rcp_approx(rf) * 0x1p27f) << 33;
-#pragma unroll
-    for (int it = 0; it < 2; ++it) {
+    {
         const u64 P = __umul64hi((u64)rho, R);          // rho r in Q.52
         const i64 e = (i64)((1ull << 52) - P);           // 1 - rho r in Q.52
         R += (u64)(mulhi_su(e << 11, R) << 1);           // r e in Q.60
     }
     // u = J r and Pi = J u, Q.56.
-    i64 u[3] = {0, 0, 0};
+    i64 J5[3] = {0, 0, 0}, u5[3] = {0, 0, 0}, u[3] = {0, 0, 0};
 #pragma unroll
-    for (int a = 0; a < D; ++a) u[a] = rnd1(mulhi_su(J[a] << 5, R));
+    for (int a = 0; a < D; ++a) {
+        J5[a] = J[a] << 5;
+        u[a] = rnd1(mulhi_su(J5[a], R));
+        u5[a] = u[a] << 5;
+    }
     i64 Pd[3] = {0, 0, 0}, Po[3] = {0, 0, 0};  // diagonal; off-diagonal (xy, xz, yz)
 #pragma unroll
-    for (int a = 0; a < D; ++a) Pd[a] = rnd2(mulhi_ss(J[a] << 5, u[a] << 5));
-    Po[0] = rnd2(mulhi_ss(J[0] << 5, u[1] << 5));
+    for (int a = 0; a < D; ++a) Pd[a] = rnd2(mulhi_ss(J5[a], u5[a]));
+    Po[0] = rnd2(mulhi_ss(J5[0], u5[1]));
     if (D == 3) {
-        Po[1] = rnd2(mulhi_ss(J[0] << 5, u[2] << 5));
-        Po[2] = rnd2(mulhi_ss(J[1] << 5, u[2] << 5));
+        Po[1] = rnd2(mulhi_ss(J5[0], u5[2]));
+        Po[2] = rnd2(mulhi_ss(J5[1], u5[2]));
     }
     {
         // range guard of the shifts above: rho in (1/16, 64), |J|, |u| < 4
@@ -169,8 +199,10 @@ __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) 
         for (int a = 0; a < D; ++a) ok = ok && (u64)(J[a] + (i64)lim) < 2 * lim && (u64)(u[a] + (i64)lim) < 2 * lim;
         bad |= !ok;
     }
+    // Equilibrium moments in h-space: feq/w = A + c.J3 + sum_a c_a^2 P45_a
+    // + sum_{a<b} c_a c_b P9_ab.
     const i64 tr = Pd[0] + Pd[1] + Pd[2];
-    const i64 A = rho - (tr + rnd1(tr));
+    i64 A = rho - (tr + rnd1(tr));
     i64 J3[3], P45[3], P9[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -178,76 +210,83 @@ __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) 
         P45[a] = (Pd[a] << 2) + rnd1(Pd[a]);
         P9[a] = (Po[a] << 3) + Po[a];
     }
-    // Guo terms: V_ab = u_a F'_b for the nonzero components of F'.
-    i64 uF = 0, Td[3] = {0, 0, 0}, To[3] = {0, 0, 0};
     if (FORCED) {
+        // The Guo term divided by omega joins the same moments, so that
+        // h' = h + omega (feq/w + guo/(w omega) - h) needs no extra work per
+        // population: guo/(w omega) = c.Fw + 3 (c.u)(c.Fw) - u.Fw with
+        // Fw = 3 (1 - omega/2) F / omega.
         i64 V[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
 #pragma unroll
         for (int b = 0; b < D; ++b) {
             if (!(px.fmask & (1 << b))) continue;
 #pragma unroll
-            for (int a = 0; a < D; ++a) V[a][b] = rnd2(mulhi_ss(u[a] << 5, px.Fp[b] << 5));
+            for (int a = 0; a < D; ++a) V[a][b] = rnd2(mulhi_ss(u5[a], px.Fw[b] << 5));
         }
+        i64 uF = 0;
 #pragma unroll
         for (int a = 0; a < D; ++a) {
             uF += V[a][a];
-            Td[a] = 3 * V[a][a];
+            P45[a] += 3 * V[a][a];
+            J3[a] += px.Fw[a];
         }
-        To[0] = 3 * (V[0][1] + V[1][0]);
+        A -= uF;
+        P9[0] += 3 * (V[0][1] + V[1][0]);
         if (D == 3) {
-            To[1] = 3 * (V[0][2] + V[2][0]);
-            To[2] = 3 * (V[1][2] + V[2][1]);
+            P9[1] += 3 * (V[0][2] + V[2][0]);
+            P9[2] += 3 * (V[1][2] + V[2][1]);
         }
     }
-    // omega d: mulhi(4 d, omega/2) is omega d with one extra fraction bit,
-    // rounded by rnd1; |d| < 32 keeps 4 d representable (checked below).
-    const u64 W = px.W;
-    u64 dmag = 0;
+    // Bases shared by the populations of one face / edge / corner family.
+    i64 Fb[3], Eb[3], Cb = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) Fb[a] = A + P45[a];
+    Eb[0] = Fb[0] + P45[1];
+    Eb[1] = Fb[0] + P45[2];
+    Eb[2] = Fb[1] + P45[2];
+    if (Q == 15 || Q == 27) Cb = Eb[0] + P45[2];
+
+    const u64 W = px.W, wh1 = px.wh1;
+    int dmag = 0;  // |d| < 32 for every population (high words within 2^29)
     {
         const i64 d = A - h[0];
-        dmag |= (u64)(d + (1ll << 61));
-        i64 o = h[0] + rnd1(mulhi_su(d << 2, W));
-        if (FORCED) o -= uF;
-        h[0] = o;
+        const int hi = (int)(d >> 32);
+        dmag |= hi ^ (hi >> 31);
+        h[0] += omega_mul(d, W, wh1);
     }
 #pragma unroll
     for (int n = 1; n < Q; ++n) {
         const int m = L::opp(n);
         if (m < n) continue;
         const int c[3] = {L::cx(n), L::cy(n), L::cz(n)};
-        i64 E = A, O = 0, Eg = 0, Og = 0;
+        const int nz = (c[0] != 0) + (c[1] != 0) + (c[2] != 0);
+        i64 E, O = 0;
+        if (nz == 1) {
+            E = c[0] ? Fb[0] : (c[1] ? Fb[1] : Fb[2]);
+        } else if (nz == 2) {
+            const int k = c[0] == 0 ? 2 : (c[1] == 0 ? 1 : 0);
+            const int sg = c[0] ? (c[1] ? c[0] * c[1] : c[0] * c[2]) : c[1] * c[2];
+            E = (sg > 0) ? Eb[k] + P9[k] : Eb[k] - P9[k];
+        } else {
+            E = Cb;
+            E += (c[0] * c[1] > 0) ? P9[0] : -P9[0];
+            E += (c[0] * c[2] > 0) ? P9[1] : -P9[1];
+            E += (c[1] * c[2] > 0) ? P9[2] : -P9[2];
+        }
+        bool first = true;
 #pragma unroll
         for (int a = 0; a < D; ++a) {
             if (c[a] == 0) continue;
-            E += P45[a];
-            O += (c[a] > 0) ? J3[a] : -J3[a];
-            if (FORCED) {
-                Eg += Td[a];
-                Og += (c[a] > 0) ? px.Fp[a] : -px.Fp[a];
-            }
-        }
-        // off-diagonal pairs (xy, xz, yz)
-        const int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const int sg = c[pa[k]] * c[pb[k]];
-            if (sg == 0) continue;
-            E += (sg > 0) ? P9[k] : -P9[k];
-            if (FORCED) Eg += (sg > 0) ? To[k] : -To[k];
+            if (first) { O = (c[a] > 0) ? J3[a] : -J3[a]; first = false; }
+            else O = (c[a] > 0) ? O + J3[a] : O - J3[a];
         }
         const i64 dn = (E + O) - h[n];
         const i64 dm = (E - O) - h[m];
-        dmag |= (u64)(dn + (1ll << 61)) | (u64)(dm + (1ll << 61));
-        i64 on = h[n] + rnd1(mulhi_su(dn << 2, W));
-        i64 om = h[m] + rnd1(mulhi_su(dm << 2, W));
-        if (FORCED) {
-            on += (Eg - uF) + Og;
-            om += (Eg - uF) - Og;
-        }
-        h[n] = on;
-        h[m] = om;
+        const int hn = (int)(dn >> 32), hm = (int)(dm >> 32);
+        dmag |= (hn ^ (hn >> 31)) | (hm ^ (hm >> 31));
+        h[n] += omega_mul(dn, W, wh1);
+        h[m] += omega_mul(dm, W, wh1);
     }
-    bad |= (dmag >> 62) != 0;
+    bad |= dmag >= (1 << 29);
 }
 
 template <int Q, bool FORCED>

@@ -45,15 +45,36 @@ struct KParams {
     int bc_type[27];      // resolved ghost-class table (BCManager::finalize)
     double bc_rho[27];
     double bc_U[27][3];
+    // FP32 copies for the single-precision collide: a double->float
+    // conversion runs on the FP64 pipe (2 per SM per clock on GB300).
+    float omega_f, hF_f[3], F_f[3], gpref_f[27], gcF_f[27];
+};
+
+// Parameters in the compute type R of a collide.
+template <class R> struct Prm;
+template <> struct Prm<double> {
+    static __device__ __forceinline__ double omega(const KParams& p) { return p.omega; }
+    static __device__ __forceinline__ double hF(const KParams& p, int a) { return p.hF[a]; }
+    static __device__ __forceinline__ double F(const KParams& p, int a) { return p.F[a]; }
+    static __device__ __forceinline__ double gpref(const KParams& p, int n) { return p.gpref[n]; }
+    static __device__ __forceinline__ double gcF(const KParams& p, int n) { return p.gcF[n]; }
+};
+template <> struct Prm<float> {
+    static __device__ __forceinline__ float omega(const KParams& p) { return p.omega_f; }
+    static __device__ __forceinline__ float hF(const KParams& p, int a) { return p.hF_f[a]; }
+    static __device__ __forceinline__ float F(const KParams& p, int a) { return p.F_f[a]; }
+    static __device__ __forceinline__ float gpref(const KParams& p, int n) { return p.gpref_f[n]; }
+    static __device__ __forceinline__ float gcF(const KParams& p, int n) { return p.gcF_f[n]; }
 };
 
 // Extra constants of the fixed-point step (k_f64x.cu).
 struct KParamsX {
-    unsigned long long W;      // omega / 2 in Q0.64
-    unsigned long long Wc[4];  // twice the weight of the class |c|^2 = 0..3, Q0.64
+    unsigned long long W;      // omega / 2 in Q0.64, low bit clear
+    unsigned long long wh1;    // W / 2 - 1 (rounding constant of the omega multiply)
+    unsigned long long Wm;     // 32 x the smallest lattice weight in Q0.64
     long long hF[3];           // F / 2 in Q.56
-    long long Fp[3];           // 3 (1 - omega/2) F in Q.56 (Guo prefactor folded in)
-    int fmask;                 // bit b set when Fp[b] != 0
+    long long Fw[3];           // 3 (1 - omega/2) F / omega in Q.56 (Guo term over omega)
+    int fmask;                 // bit b set when Fw[b] != 0
 };
 
 // ---------------------------------------------------------------------------
@@ -347,6 +368,7 @@ template <> __device__ __forceinline__ float recip<float>(float x) { return __fr
 template <int Q, class R, bool FORCED>
 __device__ __forceinline__ void collide_fast(const KParams& p, R* f) {
     using L = Lat<Q>;
+    using P = Prm<R>;
     R rho = f[0], jx = R(0), jy = R(0), jz = R(0);
 #pragma unroll
     for (int n = 1; n < Q; ++n) {
@@ -362,9 +384,9 @@ __device__ __forceinline__ void collide_fast(const KParams& p, R* f) {
     const R inv = recip<R>(rho);
     R u[3];
     if (FORCED) {
-        u[0] = (jx + (R)p.hF[0]) * inv;
-        u[1] = (jy + (R)p.hF[1]) * inv;
-        u[2] = (L::D == 3) ? (jz + (R)p.hF[2]) * inv : R(0);
+        u[0] = (jx + P::hF(p, 0)) * inv;
+        u[1] = (jy + P::hF(p, 1)) * inv;
+        u[2] = (L::D == 3) ? (jz + P::hF(p, 2)) * inv : R(0);
     } else {
         u[0] = jx * inv;
         u[1] = jy * inv;
@@ -372,13 +394,13 @@ __device__ __forceinline__ void collide_fast(const KParams& p, R* f) {
     }
     const R usq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
     const R B = R(1) - R(1.5) * usq;
-    const R omega = (R)p.omega;
+    const R omega = P::omega(p);
     R udotF = R(0);
-    if (FORCED) udotF = u[0] * (R)p.F[0] + u[1] * (R)p.F[1] + u[2] * (R)p.F[2];
+    if (FORCED) udotF = u[0] * P::F(p, 0) + u[1] * P::F(p, 1) + u[2] * P::F(p, 2);
     {
         const R feq = (R)L::w(0) * rho * B;
         R o = f[0] + omega * (feq - f[0]);
-        if (FORCED) o -= (R)p.gpref[0] * udotF;
+        if (FORCED) o -= P::gpref(p, 0) * udotF;
         f[0] = o;
     }
 #pragma unroll
@@ -394,9 +416,9 @@ __device__ __forceinline__ void collide_fast(const KParams& p, R* f) {
         R on = f[n] + omega * (feq_n - f[n]);
         R om = f[m] + omega * (feq_m - f[m]);
         if (FORCED) {
-            const R cF = (R)p.gcF[n];
-            on += (R)p.gpref[n] * ((cF + b * cF) - udotF);
-            om += (R)p.gpref[m] * ((b * cF - cF) - udotF);
+            const R cF = P::gcF(p, n);
+            on += P::gpref(p, n) * ((cF + b * cF) - udotF);
+            om += P::gpref(p, m) * ((b * cF - cF) - udotF);
         }
         f[n] = on;
         f[m] = om;

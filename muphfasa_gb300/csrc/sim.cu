@@ -96,29 +96,31 @@ void build_params(const mph_desc& d, const mph_resolved_bc* tab, KParams& kp) {
         kp.bc_rho[c] = tab[c].rho;
         for (int a = 0; a < 3; ++a) kp.bc_U[c][a] = tab[c].U[a];
     }
-}
-
-// Q0.64 of twice the weight, 2/iw, rounded to nearest (iw*8 is an integer
-// for every lattice weight and 2 w <= 8/9 < 1).
-unsigned long long weight2_q64(double iw) {
-    const unsigned __int128 den = (unsigned __int128)(iw * 8.0);
-    const unsigned __int128 num = (unsigned __int128)1 << 68;
-    return (unsigned long long)((num + den / 2) / den);
+    kp.omega_f = (float)kp.omega;
+    for (int a = 0; a < 3; ++a) { kp.hF_f[a] = (float)kp.hF[a]; kp.F_f[a] = (float)kp.F[a]; }
+    for (int n = 0; n < 27; ++n) { kp.gpref_f[n] = (float)kp.gpref[n]; kp.gcF_f[n] = (float)kp.gcF[n]; }
 }
 
 template <int Q>
 void fixed_params(const mph_sim* s, KParamsX& px, long long* kbb) {
     using L = Lat<Q>;
     std::memset(&px, 0, sizeof(px));
-    px.W = (unsigned long long)std::ldexp(0.5 * s->d.omega, 64);
-    double iw_class[4] = {L::iw(0), 0.0, 0.0, 0.0};
-    for (int n = 1; n < Q; ++n) iw_class[wclass<Q>(n)] = L::iw(n);
-    for (int k = 0; k < 4; ++k) px.Wc[k] = iw_class[k] > 0.0 ? weight2_q64(iw_class[k]) : 0ull;
-    const double pre = 3.0 * (1.0 - 0.5 * s->d.omega);
+    px.W = (unsigned long long)std::ldexp(0.5 * s->d.omega, 64) & ~1ull;
+    px.wh1 = (px.W >> 1) - 1;
+    // 32 / iw_max, rounded to nearest (iw_max = 1 / smallest weight is an
+    // integer: 36, 72, 36, 216).
+    double iw_max = 0.0;
+    for (int n = 0; n < Q; ++n) iw_max = L::iw(n) > iw_max ? L::iw(n) : iw_max;
+    {
+        const unsigned __int128 den = (unsigned __int128)iw_max;
+        const unsigned __int128 num = (unsigned __int128)1 << 69;
+        px.Wm = (unsigned long long)((num + den / 2) / den);
+    }
+    const double pre = 3.0 * (1.0 - 0.5 * s->d.omega) / s->d.omega;
     for (int a = 0; a < 3; ++a) {
         px.hF[a] = std::llrint(std::ldexp(s->kp.hF[a], 56));
-        px.Fp[a] = std::llrint(std::ldexp(pre * s->kp.F[a], 56));
-        if (px.Fp[a] != 0) px.fmask |= 1 << a;
+        px.Fw[a] = std::llrint(std::ldexp(pre * s->kp.F[a], 56));
+        if (px.Fw[a] != 0) px.fmask |= 1 << a;
     }
     // h-space bounce-back constants: contrib(opp n) / w_n with the
     // reference's contrib (BCTypes/BounceBack.H:56-63) evaluated in FP64.
@@ -278,8 +280,8 @@ int mph_create(const mph_desc* desc, mph_sim** out) {
     if (!(d.omega > 0.0 && d.omega < 2.0)) return fail(MPH_ERR_CONFIG, "mph_create: omega must lie in (0, 2)");
     if (d.precision == MPH_PREC_F64X && d.forced)
         for (int a = 0; a < d.dim; ++a)
-            if (!(std::fabs(d.force[a]) < 0.5))
-                return fail(MPH_ERR_CONFIG, "mph_create: fixed-point precision needs |force| < 0.5");
+            if (!(std::fabs(d.force[a]) < 0.5 * d.omega))
+                return fail(MPH_ERR_CONFIG, "mph_create: fixed-point precision needs |force| < omega / 2");
     auto* s = new mph_sim();
     s->d = d;
     if (d.dim == 2) s->d.n[2] = 1;
