@@ -192,6 +192,25 @@ int mph_bc_fill_arr(int dim, int q, const int dom_lo[3], const int dom_hi[3],
                     const int periodic[3], const mph_resolved_bc* table, const mph_array4* f,
                     void* stream);
 
+/* ---- allocation-free sums ---------------------------------------------- */
+/* No counterpart in the reference.  The FP64 mass and momentum sums of
+ * mph_reduce, for callers that cannot allocate device memory (a solver inside
+ * an application whose memory arena already holds the device, or one with a
+ * no-allocation-after-start-up policy): f is caller-owned device memory in
+ * valid-cell SoA layout (q * ncell doubles), out is caller-owned device
+ * memory for 4 doubles (mass, momentum x, y, z), and the work is queued on
+ * `stream` (NULL: the default stream) without synchronising.
+ * The block partials live in a fixed 64 KiB device array inside the library
+ * (held on every device that loads it until the process exits), which bounds
+ * ncell at 134,217,728 (2048 slots x 65536 cells); larger sizes return
+ * MPH_ERR_ARG.  No cudaMalloc/cudaFree or other allocating call is made.  The
+ * first call on a device looks up the array's device address (once per
+ * device), so that first call should come before any stream capture.  Every
+ * call shares the one array: calls that overlap on the GPU race and must be
+ * ordered by the caller.  Nothing in the array needs to start at zero; every
+ * slot a call reads is written earlier in the same call. */
+int mph_reduce_f64_noalloc(int dim, int q, const double* f, long long ncell, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -37,7 +37,7 @@ EXPORTS = [
     "mph_inputs_get", "mph_inputs_derive", "mph_resolve_bc", "mph_create", "mph_destroy", "mph_set_f",
     "mph_get_f", "mph_init_fields", "mph_advance", "mph_update_macroscopic", "mph_reduce", "mph_time",
     "mph_launches_per_step", "mph_advance_timed", "mph_step_host", "mph_pull_collide_fused_arr",
-    "mph_periodic_fill_arr", "mph_bc_fill_arr",
+    "mph_periodic_fill_arr", "mph_bc_fill_arr", "mph_reduce_f64_noalloc",
 ]
 
 
@@ -109,6 +109,7 @@ def lib():
                                              C.c_double, dp, P]
     L.mph_periodic_fill_arr.argtypes = [C.c_int, C.c_int, ip, ip, ip, C.POINTER(Array4), P]
     L.mph_bc_fill_arr.argtypes = [C.c_int, C.c_int, ip, ip, ip, C.POINTER(ResolvedBC), C.POINTER(Array4), P]
+    L.mph_reduce_f64_noalloc.argtypes = [C.c_int, C.c_int, P, C.c_longlong, P, P]
     _lib = L
     return L
 
