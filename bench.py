@@ -173,6 +173,44 @@ def run_reference(args):
     return 0
 
 
+def run_batch(args):
+    """512 independent lid-driven cavities, D2Q9, side log-uniform in [64, 512],
+    Re log-uniform in [100, 5000] (tau = 0.5 + 3 u_lid N / Re), FP32 storage:
+    one batched kernel per step (CUDA graph) against one launch per domain."""
+    import muphfasa_gb300 as m
+    m.set_device(0)
+    prec = args.precision if args.precision in ("f32", "f16s", "bf16s", "f64", "f64_fast") else "f32"
+    descs = m.cavity_batch_descs(512, precision=prec)
+    batch = m.Batch(descs)
+    for i in range(len(descs)):
+        batch.initialize(i)
+    batch.advance(args.warmup)
+    total, width, ntiles = batch.info()
+    with ClockSampler(0) as clk:
+        ms = batch.advance_timed(args.steps)
+    ms_loop = batch.advance_looped_timed(max(2, args.steps // 4))
+    steps_loop = max(2, args.steps // 4)
+    q, es = 9, ELEM[prec]
+    value = total * args.steps / (ms / 1e3) / 1e6
+    looped = total * steps_loop / (ms_loop / 1e3) / 1e6
+    achieved = 2 * q * es * total / (ms / args.steps / 1e3) / 1e9
+    peak, kind = peaks()
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "MLUPS", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[prec], "data": "synthetic",
+            "config": {"workload": "batch512_cavities_d2q9", "domains": 512, "total_cells": total,
+                       "side": [64, 512], "Re": [100, 5000], "lid": 0.1, "precision": prec,
+                       "tile_width": width, "tiles": ntiles, "graph": "2-step CUDA graph"},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": kind,
+                         "bytes_per_cell_update": 2 * q * es},
+            "looped_single_domain": {"value": round(looped, 3), "unit": "MLUPS", "launches_per_step": 512},
+            "clocks": clk.summary(), "gpu_launches": args.steps}
+    print(json.dumps(line), flush=True)
+    batch.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -180,12 +218,23 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=512, help="cells per side of the channel")
-    ap.add_argument("--precision", default="f64_fast", choices=list(ELEM))
+    ap.add_argument("--precision", default="f64x", choices=list(ELEM))
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--probes", action="store_true", help="build and run bench_probes.cu (pipe rates, pull-copy)")
+    ap.add_argument("--workload", default="channel", choices=["channel", "batch512"],
+                    help="channel: the D3Q19 channel (headline); batch512: 512 uneven D2Q9 cavities")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.probes:
+        exe = os.path.join(ROOT, "muphfasa_gb300", "_build", "bench_probes")
+        os.makedirs(os.path.dirname(exe), exist_ok=True)
+        subprocess.run(["nvcc", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-o", exe,
+                        os.path.join(ROOT, "bench_probes.cu")], check=True)
+        return subprocess.run([exe]).returncode
+    if args.workload == "batch512":
+        return run_batch(args)
 
     import muphfasa_gb300 as m
     from muphfasa_gb300 import replicas

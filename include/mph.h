@@ -192,6 +192,31 @@ int mph_bc_fill_arr(int dim, int q, const int dom_lo[3], const int dom_hi[3],
                     const int periodic[3], const mph_resolved_bc* table, const mph_array4* f,
                     void* stream);
 
+/* ---- batches of independent domains ------------------------------------ */
+/* Many domains of uneven sizes advanced together (an ensemble of solver
+ * instances; no counterpart API in the reference, which runs one domain per
+ * process): one kernel per step covers every domain through a flat tile list,
+ * step pairs are replayed from a CUDA graph, and the tile shape is chosen by
+ * timing the candidates on the batch itself.  All domains share lattice,
+ * precision (not MPH_PREC_F64X) and forcing flag; each has its own size,
+ * omega, boundary faces and force.  Domain d's results equal those of a
+ * single handle created from descs[d]. */
+typedef struct mph_batch mph_batch;
+int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out);
+int mph_batch_destroy(mph_batch* b);
+/* setInitialConditions of one domain (as mph_init_fields). */
+int mph_batch_init_fields(mph_batch* b, int domain, double* rho, double* u);
+int mph_batch_advance(mph_batch* b, int nsteps);
+/* nsteps of the batched kernel timed with CUDA events (autotuning and graph
+ * capture happen before the timed region). */
+int mph_batch_advance_timed(mph_batch* b, int nsteps, float* ms);
+/* The same steps as one single-domain launch per domain per step. */
+int mph_batch_advance_looped_timed(mph_batch* b, int nsteps, float* ms);
+int mph_batch_get_f(mph_batch* b, int domain, double* f);
+int mph_batch_moments(mph_batch* b, int domain, double* rho, double* u);
+/* Total cells, chosen tile width (0 before the first advance), tile count. */
+int mph_batch_info(const mph_batch* b, long long* total_cells, int* tile_width, int* ntiles);
+
 /* ---- allocation-free sums ---------------------------------------------- */
 /* No counterpart in the reference.  The FP64 mass and momentum sums of
  * mph_reduce, for callers that cannot allocate device memory (a solver inside

@@ -17,6 +17,7 @@ device is present the calls raise.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 
 import numpy as np
@@ -37,7 +38,9 @@ EXPORTS = [
     "mph_inputs_get", "mph_inputs_derive", "mph_resolve_bc", "mph_create", "mph_destroy", "mph_set_f",
     "mph_get_f", "mph_init_fields", "mph_advance", "mph_update_macroscopic", "mph_reduce", "mph_time",
     "mph_launches_per_step", "mph_advance_timed", "mph_step_host", "mph_pull_collide_fused_arr",
-    "mph_periodic_fill_arr", "mph_bc_fill_arr", "mph_reduce_f64_noalloc",
+    "mph_periodic_fill_arr", "mph_bc_fill_arr", "mph_reduce_f64_noalloc", "mph_batch_create",
+    "mph_batch_destroy", "mph_batch_init_fields", "mph_batch_advance", "mph_batch_advance_timed",
+    "mph_batch_advance_looped_timed", "mph_batch_get_f", "mph_batch_moments", "mph_batch_info",
 ]
 
 
@@ -110,6 +113,15 @@ def lib():
     L.mph_periodic_fill_arr.argtypes = [C.c_int, C.c_int, ip, ip, ip, C.POINTER(Array4), P]
     L.mph_bc_fill_arr.argtypes = [C.c_int, C.c_int, ip, ip, ip, C.POINTER(ResolvedBC), C.POINTER(Array4), P]
     L.mph_reduce_f64_noalloc.argtypes = [C.c_int, C.c_int, P, C.c_longlong, P, P]
+    L.mph_batch_create.argtypes = [C.c_int, C.POINTER(Desc), C.POINTER(P)]
+    L.mph_batch_destroy.argtypes = [P]
+    L.mph_batch_init_fields.argtypes = [P, C.c_int, dp, dp]
+    L.mph_batch_advance.argtypes = [P, C.c_int]
+    L.mph_batch_advance_timed.argtypes = [P, C.c_int, C.POINTER(C.c_float)]
+    L.mph_batch_advance_looped_timed.argtypes = [P, C.c_int, C.POINTER(C.c_float)]
+    L.mph_batch_get_f.argtypes = [P, C.c_int, dp]
+    L.mph_batch_moments.argtypes = [P, C.c_int, dp, dp]
+    L.mph_batch_info.argtypes = [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     _lib = L
     return L
 
@@ -284,6 +296,86 @@ class Simulation:
         n = C.c_int()
         check(lib().mph_launches_per_step(self._h, C.byref(n)))
         return n.value
+
+
+class Batch:
+    """Independent domains of uneven sizes advanced together (mph_batch_*)."""
+
+    def __init__(self, descs):
+        self.descs = list(descs)
+        arr = (Desc * len(self.descs))(*self.descs)
+        h = C.c_void_p()
+        check(lib().mph_batch_create(len(self.descs), arr, C.byref(h)))
+        self._h = h
+        self.ncells = [int(d.n[0] * d.n[1] * (d.n[2] if d.dim == 3 else 1)) for d in self.descs]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mph_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def initialize(self, domain, rho=None, u=None):
+        d, N = self.descs[domain], self.ncells[domain]
+        rho = np.ones(N) if rho is None else np.ascontiguousarray(rho, dtype=np.float64).reshape(-1).copy()
+        u = np.zeros(d.dim * N) if u is None else np.ascontiguousarray(u, dtype=np.float64).reshape(-1).copy()
+        check(lib().mph_batch_init_fields(self._h, int(domain), _dp(rho), _dp(u)))
+        return rho, u
+
+    def advance(self, nsteps=1):
+        check(lib().mph_batch_advance(self._h, int(nsteps)))
+
+    def advance_timed(self, nsteps):
+        ms = C.c_float()
+        check(lib().mph_batch_advance_timed(self._h, int(nsteps), C.byref(ms)))
+        return float(ms.value)
+
+    def advance_looped_timed(self, nsteps):
+        ms = C.c_float()
+        check(lib().mph_batch_advance_looped_timed(self._h, int(nsteps), C.byref(ms)))
+        return float(ms.value)
+
+    def f(self, domain):
+        out = np.empty(self.descs[domain].q * self.ncells[domain])
+        check(lib().mph_batch_get_f(self._h, int(domain), _dp(out)))
+        return out
+
+    def moments(self, domain):
+        N, dim = self.ncells[domain], self.descs[domain].dim
+        rho, u = np.empty(N), np.empty(dim * N)
+        check(lib().mph_batch_moments(self._h, int(domain), _dp(rho), _dp(u)))
+        return rho, u
+
+    def info(self):
+        tc, tw, nt = C.c_longlong(), C.c_int(), C.c_int()
+        check(lib().mph_batch_info(self._h, C.byref(tc), C.byref(tw), C.byref(nt)))
+        return int(tc.value), int(tw.value), int(nt.value)
+
+
+def cavity_batch_descs(n_domains=512, seed=20261203, lattice="D2Q9", precision="f32", lid=0.1,
+                       side=(64, 512), re=(100.0, 5000.0)):
+    """The uneven lid-driven-cavity ensemble: side and Reynolds number drawn
+    log-uniformly (seeded), tau = 0.5 + 3 lid side / Re; draws with tau
+    outside (0.5, 2) are redrawn.  MovingWall lid at y = hi, NoSlip elsewhere."""
+    rng = np.random.default_rng(seed)
+    descs = []
+    while len(descs) < n_domains:
+        n = int(round(math.exp(rng.uniform(math.log(side[0]), math.log(side[1])))))
+        Re = math.exp(rng.uniform(math.log(re[0]), math.log(re[1])))
+        tau = 0.5 + 3.0 * lid * n / Re
+        if not (0.5 < tau < 2.0):
+            continue
+        U = [[0.0] * 3 for _ in range(6)]
+        U[3] = [lid, 0.0, 0.0]
+        descs.append(make_desc(lattice, (n, n), 1.0 / tau,
+                               faces=["NoSlip", "NoSlip", "NoSlip", "MovingWall", "Periodic", "Periodic"],
+                               face_U=U, precision=precision))
+    return descs
 
 
 def make_simulation(inputs: InputParser, precision: str = "f64") -> Simulation:

@@ -1,0 +1,464 @@
+// batch.cu -- many independent domains of uneven sizes advanced together.
+//
+// The reference advances one domain per process; a parameter sweep or an
+// ensemble (hundreds of lid-driven cavities of different size and Reynolds
+// number) would run hundreds of solver instances.  Here all domains share one
+// population buffer (domain-major, then population, then cell) and one kernel
+// per step covers every domain: the grid is a flat list of tiles, each tile
+// naming its domain, so the work is balanced across the 152 SMs however
+// uneven the domains are.  Each domain's constants (KParams: size, omega,
+// boundary table) sit in global memory and are read by the same pull /
+// collide device code as a single domain, so every domain's result is
+// bit-identical to a single-domain handle with the same description.
+//
+// Step pairs (A->B, B->A) are captured once in a CUDA graph and replayed.
+// The tile shape is chosen by an autotuner that times the candidate shapes on
+// the batch itself and caches the winner per (Q, precision, size class).
+// mph_batch_advance_looped_timed runs the same steps as one launch per domain
+// per step, the baseline the batched kernel is compared with.
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <utility>
+#include <vector>
+
+#include "lbm_launch.h"
+#include "mph_internal.h"
+
+using namespace mph;
+
+namespace {
+
+struct Tile {
+    int dom, x0, y0, z0;
+};
+
+template <int Q, class St, int ARITH, bool FORCED>
+__global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __restrict__ fin_base,
+                                                    typename St::T* __restrict__ fout_base,
+                                                    const Tile* __restrict__ tiles, const KParams* __restrict__ dp,
+                                                    const long long* __restrict__ offs) {
+    using R = typename St::R;
+    const Tile t = tiles[blockIdx.x];
+    const KParams& p = dp[t.dom];
+    const int x = t.x0 + threadIdx.x;
+    const int y = t.y0 + threadIdx.y;
+    const int z = t.z0;
+    if (x >= p.nx || y >= p.ny) return;
+    const long long off = offs[t.dom];
+    const typename St::T* fin = fin_base + off;
+    typename St::T* fout = fout_base + off;
+    const long long c = ((long long)z * p.ny + y) * p.nx + x;
+    R f[Q];
+    pull<Q, St>(p, &p, fin, x, y, z, c, f);
+    if constexpr (ARITH == kExact) collide_exact<Q, FORCED>(p, f);
+    else collide_fast<Q, R, FORCED>(p, f);
+#pragma unroll
+    for (int n = 0; n < Q; ++n) St::template st<Q>(fout, n, c, p.ncell, f[n]);
+}
+
+template <class F>
+cudaError_t with_q(int q, F&& f) {
+    switch (q) {
+        case 9: return f(std::integral_constant<int, 9>{});
+        case 15: return f(std::integral_constant<int, 15>{});
+        case 19: return f(std::integral_constant<int, 19>{});
+        case 27: return f(std::integral_constant<int, 27>{});
+    }
+    return cudaErrorInvalidValue;
+}
+
+template <class St, int ARITH>
+cudaError_t launch_batch_t(int q, bool forced, const void* fin, void* fout, const Tile* tiles, int ntiles, dim3 block,
+                           const KParams* dp, const long long* offs, cudaStream_t s) {
+    return with_q(q, [&](auto qc) {
+        constexpr int Q = decltype(qc)::value;
+        auto in = static_cast<const typename St::T*>(fin);
+        auto out = static_cast<typename St::T*>(fout);
+        if (forced) k_batch_step<Q, St, ARITH, true><<<ntiles, block, 0, s>>>(in, out, tiles, dp, offs);
+        else k_batch_step<Q, St, ARITH, false><<<ntiles, block, 0, s>>>(in, out, tiles, dp, offs);
+        return cudaGetLastError();
+    });
+}
+
+cudaError_t launch_batch(int prec, int q, bool forced, const void* fin, void* fout, const Tile* tiles, int ntiles,
+                         dim3 block, const KParams* dp, const long long* offs, cudaStream_t s) {
+    switch (prec) {
+        case MPH_PREC_F64: return launch_batch_t<StF64, kExact>(q, forced, fin, fout, tiles, ntiles, block, dp, offs, s);
+        case MPH_PREC_F64_FAST: return launch_batch_t<StF64, kFast>(q, forced, fin, fout, tiles, ntiles, block, dp, offs, s);
+        case MPH_PREC_F32: return launch_batch_t<StF32, kFast>(q, forced, fin, fout, tiles, ntiles, block, dp, offs, s);
+        case MPH_PREC_F16S: return launch_batch_t<StF16S, kFast>(q, forced, fin, fout, tiles, ntiles, block, dp, offs, s);
+        case MPH_PREC_BF16S: return launch_batch_t<StBF16S, kFast>(q, forced, fin, fout, tiles, ntiles, block, dp, offs, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+size_t elem_of(int prec) {
+    switch (prec) {
+        case MPH_PREC_F64:
+        case MPH_PREC_F64_FAST: return 8;
+        case MPH_PREC_F32: return 4;
+        case MPH_PREC_F16S:
+        case MPH_PREC_BF16S: return 2;
+    }
+    return 0;
+}
+
+// Tile widths tried by the autotuner (block = width x 256/width threads).
+constexpr int kWidths[4] = {32, 64, 128, 256};
+
+// Autotuner cache: (q, precision, log2 of the total cell count) -> width.
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int>, int> g_tune;
+
+}  // namespace
+
+// Defined in sim.cu (shared with single domains).
+namespace mph {
+void build_params_public(const mph_desc& d, const mph_resolved_bc* tab, KParams& kp);
+}
+
+struct mph_batch {
+    int ndom = 0, q = 0, dim = 0, prec = 0;
+    bool forced = false;
+    std::vector<mph_desc> descs;
+    std::vector<long long> offs_h;  // element offset of each domain
+    long long total_elems = 0, total_cells = 0;
+    KParams* d_params = nullptr;
+    long long* d_offs = nullptr;
+    void* fa = nullptr;
+    void* fb = nullptr;
+    double* d_stage = nullptr;
+    double* d_rho = nullptr;
+    double* d_u = nullptr;
+    long long max_cells = 0;
+    std::vector<KParams> params_h;
+    // tiles per candidate width
+    Tile* d_tiles[4] = {nullptr, nullptr, nullptr, nullptr};
+    int ntiles[4] = {0, 0, 0, 0};
+    int width_idx = -1;  // chosen by the autotuner
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaGraphExec_t graph = nullptr;  // two steps A->B->A
+    int graph_width = -1;
+    double time = 0.0;
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(MPH_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define MPH_CK(call, what)                                   \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_fail(e_, (what)); \
+    } while (0)
+
+void free_batch(mph_batch* b) {
+    cudaFree(b->d_params);
+    cudaFree(b->d_offs);
+    cudaFree(b->fa);
+    cudaFree(b->fb);
+    cudaFree(b->d_stage);
+    cudaFree(b->d_rho);
+    cudaFree(b->d_u);
+    for (auto* t : b->d_tiles) cudaFree(t);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+int ensure_tiles(mph_batch* b, int wi) {
+    if (b->d_tiles[wi]) return MPH_OK;
+    const int tx = kWidths[wi], ty = 256 / tx;
+    std::vector<Tile> tiles;
+    for (int d = 0; d < b->ndom; ++d) {
+        const mph_desc& ds = b->descs[d];
+        const int nz = ds.dim == 3 ? ds.n[2] : 1;
+        for (int z = 0; z < nz; ++z)
+            for (int y = 0; y < ds.n[1]; y += ty)
+                for (int x = 0; x < ds.n[0]; x += tx) tiles.push_back(Tile{d, x, y, z});
+    }
+    if (tiles.size() > 0x7fffffffu) return fail(MPH_ERR_ARG, "batch: too many tiles");
+    MPH_CK(cudaMalloc(&b->d_tiles[wi], sizeof(Tile) * tiles.size()), "batch tiles");
+    MPH_CK(cudaMemcpy(b->d_tiles[wi], tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice), "batch tiles");
+    b->ntiles[wi] = (int)tiles.size();
+    return MPH_OK;
+}
+
+int step_once(mph_batch* b, int wi) {
+    const int tx = kWidths[wi];
+    MPH_CK(launch_batch(b->prec, b->q, b->forced, b->fa, b->fb, b->d_tiles[wi], b->ntiles[wi], dim3(tx, 256 / tx),
+                        b->d_params, b->d_offs, b->stream),
+           "batch step launch");
+    std::swap(b->fa, b->fb);
+    return MPH_OK;
+}
+
+// Times each candidate width on the batch itself (3 steps after 1) and keeps
+// the fastest; the choice is cached per (q, precision, size class).  An even
+// number of steps is run per candidate so the state ends in buffer A.
+int autotune(mph_batch* b) {
+    if (b->width_idx >= 0) return MPH_OK;
+    const int cls = (int)std::floor(std::log2((double)b->total_cells));
+    const auto key = std::make_tuple(b->q, b->prec, cls);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) b->width_idx = it->second;
+    }
+    if (b->width_idx >= 0) return ensure_tiles(b, b->width_idx);
+    // Snapshot the state so tuning does not advance the simulation.
+    void* save = nullptr;
+    const size_t bytes = elem_of(b->prec) * (size_t)b->total_elems;
+    MPH_CK(cudaMalloc(&save, bytes), "autotune snapshot");
+    cudaError_t e = cudaMemcpyAsync(save, b->fa, bytes, cudaMemcpyDeviceToDevice, b->stream);
+    float best = 1e30f;
+    int besti = 0;
+    for (int wi = 0; wi < 4 && e == cudaSuccess; ++wi) {
+        int rc = ensure_tiles(b, wi);
+        if (rc) { cudaFree(save); return rc; }
+        rc = step_once(b, wi);
+        if (!rc) rc = step_once(b, wi);
+        if (rc) { cudaFree(save); return rc; }
+        e = cudaEventRecord(b->ev0, b->stream);
+        for (int k = 0; k < 4 && !rc; ++k) rc = step_once(b, wi);
+        if (rc) { cudaFree(save); return rc; }
+        if (e == cudaSuccess) e = cudaEventRecord(b->ev1, b->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(b->ev1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+        if (e == cudaSuccess && ms < best) { best = ms; besti = wi; }
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->fa, save, bytes, cudaMemcpyDeviceToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    cudaFree(save);
+    if (e != cudaSuccess) return cuda_fail(e, "autotune");
+    b->width_idx = besti;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = besti;
+    return MPH_OK;
+}
+
+// Two steps (A->B, B->A) captured once as a CUDA graph.
+int ensure_graph(mph_batch* b) {
+    if (b->graph && b->graph_width == b->width_idx) return MPH_OK;
+    if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+    cudaGraph_t g = nullptr;
+    MPH_CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "graph capture begin");
+    int rc = step_once(b, b->width_idx);
+    if (!rc) rc = step_once(b, b->width_idx);
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return cuda_fail(e, "graph capture end");
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
+    b->graph_width = b->width_idx;
+    return MPH_OK;
+}
+
+int advance_batch(mph_batch* b, int nsteps) {
+    int rc = autotune(b);
+    if (rc) return rc;
+    rc = ensure_graph(b);
+    if (rc) return rc;
+    for (int t = 0; t + 1 < nsteps; t += 2) MPH_CK(cudaGraphLaunch(b->graph, b->stream), "graph launch");
+    if (nsteps % 2) {
+        rc = step_once(b, b->width_idx);
+        if (rc) return rc;
+    }
+    b->time += nsteps;
+    return MPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out) {
+    if (ndomains < 1 || !descs || !out) return fail(MPH_ERR_ARG, "mph_batch_create: bad argument");
+    *out = nullptr;
+    auto* b = new mph_batch();
+    b->ndom = ndomains;
+    b->q = descs[0].q;
+    b->dim = descs[0].dim;
+    b->prec = descs[0].precision;
+    b->forced = descs[0].forced != 0;
+    if (elem_of(b->prec) == 0) { delete b; return fail(MPH_ERR_UNSUPPORTED, "mph_batch_create: precision not supported in a batch"); }
+    b->descs.assign(descs, descs + ndomains);
+    b->params_h.resize(ndomains);
+    long long off = 0;
+    for (int d = 0; d < ndomains; ++d) {
+        mph_desc& ds = b->descs[d];
+        if (ds.q != b->q || ds.dim != b->dim || ds.precision != b->prec || (ds.forced != 0) != b->forced) {
+            delete b;
+            return fail(MPH_ERR_ARG, "mph_batch_create: all domains must share lattice, precision and forcing");
+        }
+        if (!lattice_ok(ds.dim, ds.q)) { delete b; return fail(MPH_ERR_ARG, "mph_batch_create: unsupported lattice"); }
+        if (ds.dim == 2) ds.n[2] = 1;
+        for (int a = 0; a < ds.dim; ++a)
+            if (ds.n[a] < 1) { delete b; return fail(MPH_ERR_ARG, "mph_batch_create: cell counts must be positive"); }
+        if (!(ds.omega > 0.0 && ds.omega < 2.0)) { delete b; return fail(MPH_ERR_CONFIG, "mph_batch_create: omega must lie in (0, 2)"); }
+        mph_resolved_bc tab[27];
+        int rc = resolve_table(ds, tab);
+        if (rc) { delete b; return rc; }
+        build_params_public(ds, tab, b->params_h[d]);
+        const long long cells = (long long)ds.n[0] * ds.n[1] * ds.n[2];
+        b->offs_h.push_back(off);
+        off += cells * ds.q;
+        b->total_cells += cells;
+        b->max_cells = cells > b->max_cells ? cells : b->max_cells;
+    }
+    b->total_elems = off;
+    const size_t bytes = elem_of(b->prec) * (size_t)off;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
+    if (e == cudaSuccess) e = cudaMalloc(&b->fa, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&b->fb, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_params, sizeof(KParams) * ndomains);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_params, b->params_h.data(), sizeof(KParams) * ndomains, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_offs, sizeof(long long) * ndomains);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_offs, b->offs_h.data(), sizeof(long long) * ndomains, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        int rc = cuda_fail(e, "mph_batch_create");
+        free_batch(b);
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return MPH_OK;
+}
+
+int mph_batch_destroy(mph_batch* b) {
+    if (!b) return MPH_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    free_batch(b);
+    delete b;
+    return MPH_OK;
+}
+
+int mph_batch_init_fields(mph_batch* b, int domain, double* rho, double* u) {
+    if (!b || !rho || !u || domain < 0 || domain >= b->ndom) return fail(MPH_ERR_ARG, "mph_batch_init_fields: bad argument");
+    const mph_desc& ds = b->descs[domain];
+    const KParams& kp = b->params_h[domain];
+    const long long N = kp.ncell;
+    if (!b->d_rho || N > b->max_cells) {
+        // sized for the largest domain
+    }
+    if (!b->d_rho) MPH_CK(cudaMalloc(&b->d_rho, sizeof(double) * b->max_cells), "batch rho");
+    if (!b->d_u) MPH_CK(cudaMalloc(&b->d_u, sizeof(double) * 3 * b->max_cells), "batch u");
+    MPH_CK(cudaMemcpyAsync(b->d_rho, rho, sizeof(double) * N, cudaMemcpyHostToDevice, b->stream), "batch init rho");
+    MPH_CK(cudaMemcpyAsync(b->d_u, u, sizeof(double) * ds.dim * N, cudaMemcpyHostToDevice, b->stream), "batch init u");
+    void* base = static_cast<char*>(b->fa) + elem_of(b->prec) * b->offs_h[domain];
+    MPH_CK(launch_init(b->prec, b->q, b->forced, base, b->d_rho, b->d_u, kp, b->stream), "batch init");
+    if (b->forced) {
+        MPH_CK(cudaMemcpyAsync(rho, b->d_rho, sizeof(double) * N, cudaMemcpyDeviceToHost, b->stream), "batch init rho");
+        MPH_CK(cudaMemcpyAsync(u, b->d_u, sizeof(double) * ds.dim * N, cudaMemcpyDeviceToHost, b->stream), "batch init u");
+    }
+    MPH_CK(cudaStreamSynchronize(b->stream), "batch init");
+    b->time = 0.0;
+    return MPH_OK;
+}
+
+int mph_batch_advance(mph_batch* b, int nsteps) {
+    if (!b || nsteps < 0) return fail(MPH_ERR_ARG, "mph_batch_advance: bad argument");
+    int rc = advance_batch(b, nsteps);
+    if (rc) return rc;
+    MPH_CK(cudaStreamSynchronize(b->stream), "mph_batch_advance");
+    return MPH_OK;
+}
+
+int mph_batch_advance_timed(mph_batch* b, int nsteps, float* ms) {
+    if (!b || nsteps < 0 || !ms) return fail(MPH_ERR_ARG, "mph_batch_advance_timed: bad argument");
+    int rc = autotune(b);
+    if (!rc) rc = ensure_graph(b);
+    if (rc) return rc;
+    MPH_CK(cudaEventRecord(b->ev0, b->stream), "event");
+    rc = advance_batch(b, nsteps);
+    if (rc) return rc;
+    MPH_CK(cudaEventRecord(b->ev1, b->stream), "event");
+    MPH_CK(cudaEventSynchronize(b->ev1), "event sync");
+    MPH_CK(cudaEventElapsedTime(ms, b->ev0, b->ev1), "event elapsed");
+    return MPH_OK;
+}
+
+int mph_batch_advance_looped_timed(mph_batch* b, int nsteps, float* ms) {
+    if (!b || nsteps < 0 || !ms) return fail(MPH_ERR_ARG, "mph_batch_advance_looped_timed: bad argument");
+    MPH_CK(cudaEventRecord(b->ev0, b->stream), "event");
+    const size_t es = elem_of(b->prec);
+    for (int t = 0; t < nsteps; ++t) {
+        for (int d = 0; d < b->ndom; ++d) {
+            const KParams& kp = b->params_h[d];
+            const void* in = static_cast<const char*>(b->fa) + es * b->offs_h[d];
+            void* outp = static_cast<char*>(b->fb) + es * b->offs_h[d];
+            cudaError_t e = cudaErrorInvalidValue;
+            const KParams* pg = b->d_params + d;
+            switch (b->prec) {
+                case MPH_PREC_F64: e = launch_step_exact(b->q, b->forced, (const double*)in, (double*)outp, kp, pg, b->stream); break;
+                case MPH_PREC_F64_FAST: e = launch_step_fast_f64(b->q, b->forced, (const double*)in, (double*)outp, kp, pg, b->stream); break;
+                case MPH_PREC_F32: e = launch_step_fast_f32(b->q, b->forced, (const float*)in, (float*)outp, kp, pg, b->stream); break;
+                case MPH_PREC_F16S: e = launch_step_fast_f16s(b->q, b->forced, in, outp, kp, pg, b->stream); break;
+                case MPH_PREC_BF16S: e = launch_step_fast_bf16s(b->q, b->forced, in, outp, kp, pg, b->stream); break;
+            }
+            if (e != cudaSuccess) return cuda_fail(e, "looped step launch");
+        }
+        std::swap(b->fa, b->fb);
+    }
+    b->time += nsteps;
+    MPH_CK(cudaEventRecord(b->ev1, b->stream), "event");
+    MPH_CK(cudaEventSynchronize(b->ev1), "event sync");
+    MPH_CK(cudaEventElapsedTime(ms, b->ev0, b->ev1), "event elapsed");
+    return MPH_OK;
+}
+
+int mph_batch_get_f(mph_batch* b, int domain, double* f) {
+    if (!b || !f || domain < 0 || domain >= b->ndom) return fail(MPH_ERR_ARG, "mph_batch_get_f: bad argument");
+    const KParams& kp = b->params_h[domain];
+    const long long N = kp.ncell;
+    const size_t es = elem_of(b->prec);
+    void* base = static_cast<char*>(b->fa) + es * b->offs_h[domain];
+    if (es == 8 && (b->prec == MPH_PREC_F64 || b->prec == MPH_PREC_F64_FAST)) {
+        MPH_CK(cudaMemcpyAsync(f, base, sizeof(double) * b->q * N, cudaMemcpyDeviceToHost, b->stream), "batch get f");
+    } else {
+        if (!b->d_stage) MPH_CK(cudaMalloc(&b->d_stage, sizeof(double) * b->max_cells), "batch stage");
+        for (int q = 0; q < b->q; ++q) {
+            MPH_CK(launch_convert(b->prec, b->q, false, base, b->d_stage, q, N, b->stream), "batch convert");
+            MPH_CK(cudaMemcpyAsync(f + (size_t)q * N, b->d_stage, sizeof(double) * N, cudaMemcpyDeviceToHost, b->stream),
+                   "batch get f");
+        }
+    }
+    MPH_CK(cudaStreamSynchronize(b->stream), "batch get f");
+    return MPH_OK;
+}
+
+int mph_batch_moments(mph_batch* b, int domain, double* rho, double* u) {
+    if (!b || !rho || !u || domain < 0 || domain >= b->ndom) return fail(MPH_ERR_ARG, "mph_batch_moments: bad argument");
+    const KParams& kp = b->params_h[domain];
+    const long long N = kp.ncell;
+    if (!b->d_rho) MPH_CK(cudaMalloc(&b->d_rho, sizeof(double) * b->max_cells), "batch rho");
+    if (!b->d_u) MPH_CK(cudaMalloc(&b->d_u, sizeof(double) * 3 * b->max_cells), "batch u");
+    const void* base = static_cast<const char*>(b->fa) + elem_of(b->prec) * b->offs_h[domain];
+    MPH_CK(launch_moments(b->prec, b->q, b->forced, base, b->d_rho, b->d_u, kp, b->d_params + domain, b->stream),
+           "batch moments");
+    MPH_CK(cudaMemcpyAsync(rho, b->d_rho, sizeof(double) * N, cudaMemcpyDeviceToHost, b->stream), "batch rho");
+    MPH_CK(cudaMemcpyAsync(u, b->d_u, sizeof(double) * b->dim * N, cudaMemcpyDeviceToHost, b->stream), "batch u");
+    MPH_CK(cudaStreamSynchronize(b->stream), "batch moments");
+    return MPH_OK;
+}
+
+int mph_batch_info(const mph_batch* b, long long* total_cells, int* tile_width, int* ntiles) {
+    if (!b) return fail(MPH_ERR_ARG, "mph_batch_info: NULL batch");
+    if (total_cells) *total_cells = b->total_cells;
+    if (tile_width) *tile_width = b->width_idx >= 0 ? kWidths[b->width_idx] : 0;
+    if (ntiles) *ntiles = b->width_idx >= 0 ? b->ntiles[b->width_idx] : 0;
+    return MPH_OK;
+}
+
+}  // extern "C"

@@ -70,12 +70,11 @@ template <int Q>
 __device__ __forceinline__ void pull_x(const KParams& p, const KParams* __restrict__ pg, const i64* __restrict__ kbb,
                                        const i64* __restrict__ fin, int x, int y, int z, long long c, i64* h) {
     using L = Lat<Q>;
-    const bool interior = x > 0 && x < p.nx - 1 && y > 0 && y < p.ny - 1 && (L::D == 2 || (z > 0 && z < p.nz - 1));
-    if (interior) {
-        const long long plane = (long long)p.nx * p.ny;
+    const Nbr o = neighbours<L::D>(p, x, y, z);
+    if (!o.wall) {
+        const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
 #pragma unroll
-        for (int n = 0; n < Q; ++n)
-            h[n] = __ldg(fin + n * p.ncell + c - (L::cx(n) + (long long)L::cy(n) * p.nx + L::cz(n) * plane));
+        for (int n = 0; n < Q; ++n) h[n] = __ldg(fin + ((unsigned)n * N + (unsigned)((int)ci + upstream<Q>(o, n))));
         return;
     }
 #pragma unroll
@@ -303,8 +302,9 @@ __global__ void __launch_bounds__(256) k_step_x(const i64* __restrict__ fin, i64
     int bad = 0;
     collide_x<Q, FORCED>(px, h, bad);
     if (bad) atomicOr(flag, 1);
+    const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
 #pragma unroll
-    for (int n = 0; n < Q; ++n) fout[n * p.ncell + c] = h[n];
+    for (int n = 0; n < Q; ++n) fout[(unsigned)n * N + ci] = h[n];
 }
 
 }  // namespace

@@ -83,6 +83,8 @@ struct KParamsX {
 struct StF64 {
     using T = double;
     using R = double;
+    template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int, unsigned e) { return __ldg(f + e); }
+    template <int Q> static __device__ __forceinline__ void ste(T* __restrict__ f, int, unsigned e, R v) { f[e] = v; }
     template <int Q> static __device__ __forceinline__ R ld(const T* __restrict__ f, int n, long long i, long long N) {
         return __ldg(f + n * N + i);
     }
@@ -95,6 +97,8 @@ struct StF64 {
 struct StF32 {
     using T = float;
     using R = float;
+    template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int, unsigned e) { return __ldg(f + e); }
+    template <int Q> static __device__ __forceinline__ void ste(T* __restrict__ f, int, unsigned e, R v) { f[e] = v; }
     template <int Q> static __device__ __forceinline__ R ld(const T* __restrict__ f, int n, long long i, long long N) {
         return __ldg(f + n * N + i);
     }
@@ -109,6 +113,12 @@ struct StF32 {
 struct StF16S {
     using T = __half;
     using R = float;
+    template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int n, unsigned e) {
+        return __half2float(f[e]) + (float)Lat<Q>::w(n);
+    }
+    template <int Q> static __device__ __forceinline__ void ste(T* __restrict__ f, int n, unsigned e, R v) {
+        f[e] = __float2half_rn(v - (float)Lat<Q>::w(n));
+    }
     template <int Q> static __device__ __forceinline__ R ld(const T* __restrict__ f, int n, long long i, long long N) {
         return __half2float(f[n * N + i]) + (float)Lat<Q>::w(n);
     }
@@ -122,6 +132,12 @@ struct StF16S {
 struct StBF16S {
     using T = __nv_bfloat16;
     using R = float;
+    template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int n, unsigned e) {
+        return __bfloat162float(f[e]) + (float)Lat<Q>::w(n);
+    }
+    template <int Q> static __device__ __forceinline__ void ste(T* __restrict__ f, int n, unsigned e, R v) {
+        f[e] = __float2bfloat16_rn(v - (float)Lat<Q>::w(n));
+    }
     template <int Q> static __device__ __forceinline__ R ld(const T* __restrict__ f, int n, long long i, long long N) {
         return __bfloat162float(f[n * N + i]) + (float)Lat<Q>::w(n);
     }
@@ -141,6 +157,12 @@ constexpr int kFxShift = 56;
 struct StF64X {
     using T = long long;
     using R = double;
+    template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int n, unsigned e) {
+        return ((double)__ldg(f + e) * 0x1p-56) / Lat<Q>::iw(n);
+    }
+    template <int Q> static __device__ __forceinline__ void ste(T* __restrict__ f, int n, unsigned e, R v) {
+        f[e] = __double2ll_rn(v * Lat<Q>::iw(n) * 0x1p56);
+    }
     template <int Q> static __device__ __forceinline__ R ld(const T* __restrict__ f, int n, long long i, long long N) {
         return ((double)__ldg(f + n * N + i) * 0x1p-56) / Lat<Q>::iw(n);
     }
@@ -242,17 +264,61 @@ __device__ __forceinline__ void pull_edge(const KParams& p, const KParams* __res
     }
 }
 
+// Offsets (in cells) of the upstream neighbour along each axis, with the
+// periodic wrap folded in: xm is the offset of x-1, xp of x+1, etc.  `wall`
+// marks a cell next to a non-periodic face, which needs the boundary rules.
+struct Nbr {
+    int xm, xp, ym, yp, zm, zp;
+    bool wall;
+};
+
+template <int D>
+__device__ __forceinline__ Nbr neighbours(const KParams& p, int x, int y, int z) {
+    Nbr o;
+    const int nx = p.nx, ny = p.ny, nz = p.nz, plane = nx * ny;
+    const bool x0 = x == 0, x1 = x == nx - 1, y0 = y == 0, y1 = y == ny - 1;
+    o.xm = x0 ? nx - 1 : -1;
+    o.xp = x1 ? -(nx - 1) : 1;
+    o.ym = y0 ? (ny - 1) * nx : -nx;
+    o.yp = y1 ? -(ny - 1) * nx : nx;
+    o.wall = (!p.periodic[0] && (x0 || x1)) || (!p.periodic[1] && (y0 || y1));
+    if (D == 3) {
+        const bool z0 = z == 0, z1 = z == nz - 1;
+        o.zm = z0 ? (nz - 1) * plane : -plane;
+        o.zp = z1 ? -(nz - 1) * plane : plane;
+        o.wall = o.wall || (!p.periodic[2] && (z0 || z1));
+    } else {
+        o.zm = o.zp = 0;
+    }
+    return o;
+}
+
+// Offset of the cell population n streams from: x - c_n.
+template <int Q>
+__device__ __forceinline__ int upstream(const Nbr& o, int n) {
+    using L = Lat<Q>;
+    const int ox = L::cx(n) == 1 ? o.xm : (L::cx(n) == -1 ? o.xp : 0);
+    const int oy = L::cy(n) == 1 ? o.ym : (L::cy(n) == -1 ? o.yp : 0);
+    const int oz = L::cz(n) == 1 ? o.zm : (L::cz(n) == -1 ? o.zp : 0);
+    return ox + oy + oz;
+}
+
+// Pull of all Q populations into f.  Cells away from non-periodic faces use
+// 32-bit element indices (Q * N < 2^32 is checked when a handle is created);
+// cells next to a wall take pull_edge.
 template <int Q, class St>
 __device__ __forceinline__ void pull(const KParams& p, const KParams* __restrict__ pg,
                                      const typename St::T* __restrict__ fin, int x, int y, int z, long long c,
                                      typename St::R* f) {
     using L = Lat<Q>;
-    const bool interior = x > 0 && x < p.nx - 1 && y > 0 && y < p.ny - 1 && (L::D == 2 || (z > 0 && z < p.nz - 1));
-    if (interior) {
-        const long long plane = (long long)p.nx * p.ny;
+    const Nbr o = neighbours<L::D>(p, x, y, z);
+    if (!o.wall) {
+        const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
 #pragma unroll
-        for (int n = 0; n < Q; ++n)
-            f[n] = St::template ld<Q>(fin, n, c - (L::cx(n) + (long long)L::cy(n) * p.nx + L::cz(n) * plane), p.ncell);
+        for (int n = 0; n < Q; ++n) {
+            const unsigned e = (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(o, n));
+            f[n] = St::template lde<Q>(fin, n, e);
+        }
     } else {
         pull_edge<Q, St>(p, pg, fin, x, y, z, c, f);
     }
@@ -442,8 +508,9 @@ __global__ void __launch_bounds__(256) k_step(const typename St::T* __restrict__
     pull<Q, St>(p, pg, fin, x, y, z, c, f);
     if constexpr (ARITH == kExact) collide_exact<Q, FORCED>(p, f);
     else collide_fast<Q, R, FORCED>(p, f);
+    const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
 #pragma unroll
-    for (int n = 0; n < Q; ++n) St::template st<Q>(fout, n, c, p.ncell, f[n]);
+    for (int n = 0; n < Q; ++n) St::template ste<Q>(fout, n, (unsigned)n * N + ci, f[n]);
 }
 
 // updateMacroscopic (SimulationSetup.cpp:142-166): moments of the streamed

@@ -143,6 +143,15 @@ void fixed_params(const mph_sim* s, KParamsX& px, long long* kbb) {
         }
 }
 
+}  // namespace
+
+namespace mph {
+// KParams of one domain, shared with the batch (batch.cu).
+void build_params_public(const mph_desc& d, const mph_resolved_bc* tab, KParams& kp) { build_params(d, tab, kp); }
+}  // namespace mph
+
+namespace {
+
 void free_all(mph_sim* s) {
     if (!s) return;
     cudaFree(s->fa);
@@ -275,6 +284,8 @@ int mph_create(const mph_desc* desc, mph_sim** out) {
     if (d.dim == 2 && d.n[2] != 1) return fail(MPH_ERR_ARG, "mph_create: n[2] must be 1 for a 2-D lattice");
     const long long ncell = (long long)d.n[0] * d.n[1] * (d.dim == 3 ? d.n[2] : 1);
     if (ncell >= (1LL << 31)) return fail(MPH_ERR_ARG, "mph_create: more than 2^31-1 cells");
+    if ((long long)d.q * ncell >= (1LL << 32))
+        return fail(MPH_ERR_ARG, "mph_create: q * cells must stay below 2^32 (32-bit element indices)");
     if ((d.dim == 3 ? d.n[2] : 1) > 65535 || (d.n[1] + 7) / 8 > 65535)
         return fail(MPH_ERR_ARG, "mph_create: ny or nz exceeds the launch grid limit (65535)");
     if (!(d.omega > 0.0 && d.omega < 2.0)) return fail(MPH_ERR_CONFIG, "mph_create: omega must lie in (0, 2)");

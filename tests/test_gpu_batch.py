@@ -1,0 +1,82 @@
+"""Batches of independent domains: every domain of a batch matches a
+single-domain handle with the same description bit for bit (the same device
+code runs on per-domain constants), the looped per-domain launches match the
+batched kernel, and the uneven cavity ensemble of the benchmark is drawn with
+tau inside (0.5, 2)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _cavity(mph, n, omega, lid, precision, lattice="D2Q9"):
+    U = [[0.0] * 3 for _ in range(6)]
+    U[3] = [lid, 0.0, 0.0]
+    faces = ["NoSlip", "NoSlip", "NoSlip", "MovingWall"] + ["Periodic", "Periodic"]
+    if lattice != "D2Q9":
+        faces = ["NoSlip", "NoSlip", "NoSlip", "MovingWall", "Periodic", "Periodic"]
+    return mph.make_desc(lattice, n, omega, faces=faces, face_U=U, precision=precision)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32", "f16s"])
+def test_batch_domains_equal_single_handles(precision, mph):
+    descs = [_cavity(mph, (17, 17), 1.2, 0.1, precision), _cavity(mph, (64, 48), 1.7, 0.05, precision),
+             _cavity(mph, (100, 100), 0.9, 0.1, precision), _cavity(mph, (33, 65), 1.9, 0.08, precision)]
+    batch = mph.Batch(descs)
+    singles = [mph.Simulation(d) for d in descs]
+    rng = np.random.default_rng(5)
+    for i, d in enumerate(descs):
+        N = batch.ncells[i]
+        rho, u = 1 + 0.01 * rng.standard_normal(N), 0.02 * rng.standard_normal(2 * N)
+        batch.initialize(i, rho, u)
+        singles[i].initialize(rho, u)
+    batch.advance(57)
+    for s in singles:
+        s.advance(57)
+    for i, s in enumerate(singles):
+        assert np.array_equal(batch.f(i), s.f()), i
+        rb, ub = batch.moments(i)
+        rs, us = s.update_macroscopic()
+        assert np.array_equal(rb, rs) and np.array_equal(ub, us)
+    total, width, ntiles = batch.info()
+    assert total == sum(batch.ncells) and width in (32, 64, 128, 256) and ntiles > 0
+
+
+def test_batch_3d_forced_mixed_boundaries(mph):
+    faces_a = ["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic", "Periodic"]
+    faces_b = ["Inflow", "PressureOutlet", "NoSlip", "MovingWall", "Periodic", "Periodic"]
+    Ub = [[0.0] * 3 for _ in range(6)]
+    Ub[0][0] = 0.02
+    Ub[3][0] = 0.05
+    descs = [mph.make_desc("D3Q19", (20, 12, 9), 1.3, faces=faces_a, force=(1e-5, 0, 0), precision="f64"),
+             mph.make_desc("D3Q19", (7, 16, 11), 1.6, faces=faces_b, face_U=Ub, face_rho=[1, 1.01, 1, 1, 1, 1],
+                           force=(2e-5, 1e-6, 0), precision="f64")]
+    batch = mph.Batch(descs)
+    singles = [mph.Simulation(d) for d in descs]
+    for i in range(2):
+        batch.initialize(i)
+        singles[i].initialize()
+    batch.advance(31)
+    for i, s in enumerate(singles):
+        s.advance(31)
+        assert np.array_equal(batch.f(i), s.f())
+
+
+def test_looped_launches_equal_batched(mph):
+    descs = mph.cavity_batch_descs(12, seed=3, side=(16, 80))
+    a, b = mph.Batch(descs), mph.Batch(descs)
+    for i in range(len(descs)):
+        a.initialize(i)
+        b.initialize(i)
+    a.advance(10)
+    b.advance_looped_timed(10)
+    for i in range(len(descs)):
+        assert np.array_equal(a.f(i), b.f(i))
+
+
+def test_cavity_ensemble_draw(mph):
+    descs = mph.cavity_batch_descs(512)
+    taus = np.array([1.0 / d.omega for d in descs])
+    sides = np.array([d.n[0] for d in descs])
+    assert len(descs) == 512 and np.all((taus > 0.5) & (taus < 2.0))
+    assert sides.min() >= 64 and sides.max() <= 512
