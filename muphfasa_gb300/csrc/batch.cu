@@ -25,6 +25,7 @@
 #include <utility>
 #include <vector>
 
+#include "batch_kernel.cuh"
 #include "lbm_launch.h"
 #include "mph_internal.h"
 
@@ -32,62 +33,11 @@ using namespace mph;
 
 namespace {
 
-struct Tile {
-    int dom, x0, y0, z0;
-};
-
-template <int Q, class St, int ARITH, bool FORCED>
-__global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __restrict__ fin_base,
-                                                    typename St::T* __restrict__ fout_base,
-                                                    const Tile* __restrict__ tiles, const KParams* __restrict__ dp,
-                                                    const long long* __restrict__ offs) {
-    using R = typename St::R;
-    const Tile t = tiles[blockIdx.x];
-    const KParams& p = dp[t.dom];
-    const int x = t.x0 + threadIdx.x;
-    const int y = t.y0 + threadIdx.y;
-    const int z = t.z0;
-    if (x >= p.nx || y >= p.ny) return;
-    const long long off = offs[t.dom];
-    const typename St::T* fin = fin_base + off;
-    typename St::T* fout = fout_base + off;
-    const long long c = ((long long)z * p.ny + y) * p.nx + x;
-    R f[Q];
-    pull<Q, St>(p, &p, fin, x, y, z, c, f);
-    if constexpr (ARITH == kExact) collide_exact<Q, FORCED>(p, f);
-    else collide_fast<Q, R, FORCED>(p, f);
-#pragma unroll
-    for (int n = 0; n < Q; ++n) St::template st<Q>(fout, n, c, p.ncell, f[n]);
-}
-
-template <class F>
-cudaError_t with_q(int q, F&& f) {
-    switch (q) {
-        case 9: return f(std::integral_constant<int, 9>{});
-        case 15: return f(std::integral_constant<int, 15>{});
-        case 19: return f(std::integral_constant<int, 19>{});
-        case 27: return f(std::integral_constant<int, 27>{});
-    }
-    return cudaErrorInvalidValue;
-}
-
-template <class St, int ARITH>
-cudaError_t launch_batch_t(int q, bool forced, const void* fin, void* fout, const Tile* tiles, int ntiles, dim3 block,
-                           const KParams* dp, const long long* offs, cudaStream_t s) {
-    return with_q(q, [&](auto qc) {
-        constexpr int Q = decltype(qc)::value;
-        auto in = static_cast<const typename St::T*>(fin);
-        auto out = static_cast<typename St::T*>(fout);
-        if (forced) k_batch_step<Q, St, ARITH, true><<<ntiles, block, 0, s>>>(in, out, tiles, dp, offs);
-        else k_batch_step<Q, St, ARITH, false><<<ntiles, block, 0, s>>>(in, out, tiles, dp, offs);
-        return cudaGetLastError();
-    });
-}
-
 cudaError_t launch_batch(int prec, int q, bool forced, const void* fin, void* fout, const Tile* tiles, int ntiles,
                          dim3 block, const KParams* dp, const long long* offs, cudaStream_t s) {
     switch (prec) {
-        case MPH_PREC_F64: return launch_batch_t<StF64, kExact>(q, forced, fin, fout, tiles, ntiles, block, dp, offs, s);
+        case MPH_PREC_F64:
+            return launch_batch_exact(q, forced, (const double*)fin, (double*)fout, tiles, ntiles, block, dp, offs, s);
         case MPH_PREC_F64_FAST: return launch_batch_t<StF64, kFast>(q, forced, fin, fout, tiles, ntiles, block, dp, offs, s);
         case MPH_PREC_F32: return launch_batch_t<StF32, kFast>(q, forced, fin, fout, tiles, ntiles, block, dp, offs, s);
         case MPH_PREC_F16S: return launch_batch_t<StF16S, kFast>(q, forced, fin, fout, tiles, ntiles, block, dp, offs, s);

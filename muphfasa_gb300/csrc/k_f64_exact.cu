@@ -10,6 +10,7 @@
 // ghost fill).
 #include <type_traits>
 
+#include "batch_kernel.cuh"
 #include "lbm_launch.h"
 #include "mph.h"
 
@@ -305,6 +306,11 @@ cudaError_t launch_bc_fill_arr(int dim, int q, const int dlo[3], const int dhi[3
         k_bc_fill_arr<Q><<<g, b, 0, s>>>(f, dm, pg);
         return cudaGetLastError();
     });
+}
+
+cudaError_t launch_batch_exact(int q, bool forced, const double* fin, double* fout, const Tile* tiles, int ntiles,
+                               dim3 block, const KParams* dp, const long long* offs, cudaStream_t s) {
+    return launch_batch_t<StF64, kExact>(q, forced, fin, fout, tiles, ntiles, block, dp, offs, s);
 }
 
 }  // namespace mph

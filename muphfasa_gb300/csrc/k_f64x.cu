@@ -307,7 +307,148 @@ __global__ void __launch_bounds__(256) k_step_x(const i64* __restrict__ fin, i64
     for (int n = 0; n < Q; ++n) fout[(unsigned)n * N + ci] = h[n];
 }
 
+// Persistent, software-pipelined variant.  A tile is 256 consecutive cells of
+// one row (y, z); each CTA walks the tiles with a grid stride.  Before the
+// collide of tile t every thread issues cp.async copies of the Q values its
+// cell of tile t + gridDim.x will pull into the other shared-memory stage, so
+// the HBM latency of the next tile overlaps the integer arithmetic of this
+// one without extra warps.  Each thread only reads what it copied itself, so
+// the per-thread cp.async.wait_group is the only synchronisation.  Cells next
+// to a non-periodic face (and lanes past the row end) skip the staging and
+// use the direct boundary pull.
+constexpr int kPipeThreads = 256;
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+template <int Q>
+__device__ __forceinline__ void tile_cell(const KParams& p, int tiles_per_row, int tile, int& x, int& y, int& z) {
+    const int row = tile / tiles_per_row;
+    x = (tile - row * tiles_per_row) * kPipeThreads + threadIdx.x;
+    y = row % p.ny;
+    z = row / p.ny;
+}
+
+template <int Q>
+__device__ __forceinline__ void stage_tile(const KParams& p, const i64* __restrict__ fin, int tiles_per_row, int tile,
+                                           i64* __restrict__ buf) {
+    using L = Lat<Q>;
+    int x, y, z;
+    tile_cell<Q>(p, tiles_per_row, tile, x, y, z);
+    if (x < p.nx) {
+        const Nbr o = neighbours<L::D>(p, x, y, z);
+        if (!o.wall) {
+            const unsigned N = (unsigned)p.ncell;
+            const int ci = (z * p.ny + y) * p.nx + x;
+#pragma unroll
+            for (int n = 0; n < Q; ++n)
+                cp_async8(buf + n * kPipeThreads + threadIdx.x, fin + ((unsigned)n * N + (unsigned)(ci + upstream<Q>(o, n))));
+        }
+    }
+    cp_async_commit();
+}
+
+template <int Q, bool FORCED>
+__global__ void __launch_bounds__(kPipeThreads) k_step_x_pipe(const i64* __restrict__ fin, i64* __restrict__ fout,
+                                                              const KParams p, const KParamsX px,
+                                                              const KParams* __restrict__ pg,
+                                                              const i64* __restrict__ kbb, int* __restrict__ flag,
+                                                              int tiles_per_row, int ntiles) {
+    using L = Lat<Q>;
+    extern __shared__ i64 smem[];  // [2][Q][kPipeThreads]
+    int stage = 0;
+    int tile = blockIdx.x;
+    if (tile < ntiles) stage_tile<Q>(p, fin, tiles_per_row, tile, smem);
+    int bad = 0;
+    for (; tile < ntiles; tile += gridDim.x) {
+        const int next = tile + gridDim.x;
+        if (next < ntiles) stage_tile<Q>(p, fin, tiles_per_row, next, smem + (stage ^ 1) * Q * kPipeThreads);
+        else cp_async_commit();
+        cp_async_wait1();
+        int x, y, z;
+        tile_cell<Q>(p, tiles_per_row, tile, x, y, z);
+        if (x < p.nx) {
+            const long long c = ((long long)z * p.ny + y) * p.nx + x;
+            const Nbr o = neighbours<L::D>(p, x, y, z);
+            i64 h[Q];
+            if (!o.wall) {
+                const i64* b = smem + stage * Q * kPipeThreads + threadIdx.x;
+#pragma unroll
+                for (int n = 0; n < Q; ++n) h[n] = b[n * kPipeThreads];
+            } else {
+                pull_x<Q>(p, pg, kbb, fin, x, y, z, c, h);
+            }
+            collide_x<Q, FORCED>(px, h, bad);
+            const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
+#pragma unroll
+            for (int n = 0; n < Q; ++n) fout[(unsigned)n * N + ci] = h[n];
+        }
+        stage ^= 1;
+    }
+    if (bad) atomicOr(flag, 1);
+}
+
 }  // namespace
+
+namespace {
+template <int Q, bool FORCED>
+cudaError_t pipe_setup(size_t& smem) {
+    smem = 2 * Q * kPipeThreads * sizeof(long long);
+    return cudaFuncSetAttribute(k_step_x_pipe<Q, FORCED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+}  // namespace
+
+int f64x_pipe_ctas(int q, bool forced) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    size_t smem = 0;
+    cudaError_t e = cudaErrorInvalidValue;
+#define MPH_XP_OCC(QQ)                                                                                         \
+    case QQ:                                                                                                   \
+        e = forced ? pipe_setup<QQ, true>(smem) : pipe_setup<QQ, false>(smem);                                 \
+        if (e == cudaSuccess)                                                                                  \
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(                                                 \
+                &per_sm, forced ? k_step_x_pipe<QQ, true> : k_step_x_pipe<QQ, false>, kPipeThreads, smem);    \
+        break;
+    switch (q) {
+        MPH_XP_OCC(9)
+        MPH_XP_OCC(15)
+        MPH_XP_OCC(19)
+        MPH_XP_OCC(27)
+    }
+#undef MPH_XP_OCC
+    if (e != cudaSuccess) return 0;
+    return per_sm * sms;
+}
+
+cudaError_t launch_step_f64x_pipe(int q, bool forced, const long long* fin, long long* fout, const KParams& p,
+                                  const KParamsX& px, const KParams* pg, const long long* kbb, int* flag,
+                                  int ctas, cudaStream_t s) {
+    const int tiles_per_row = (p.nx + kPipeThreads - 1) / kPipeThreads;
+    const int ntiles = tiles_per_row * p.ny * p.nz;
+    const int grid = ctas < ntiles ? ctas : ntiles;
+    const size_t sm = 2 * (size_t)q * kPipeThreads * sizeof(long long);
+#define MPH_XP_CASE(QQ)                                                                                       \
+    case QQ:                                                                                                  \
+        if (forced)                                                                                           \
+            k_step_x_pipe<QQ, true><<<grid, kPipeThreads, sm, s>>>(fin, fout, p, px, pg, kbb, flag, tiles_per_row, ntiles);  \
+        else                                                                                                  \
+            k_step_x_pipe<QQ, false><<<grid, kPipeThreads, sm, s>>>(fin, fout, p, px, pg, kbb, flag, tiles_per_row, ntiles); \
+        return cudaGetLastError();
+    switch (q) {
+        MPH_XP_CASE(9)
+        MPH_XP_CASE(15)
+        MPH_XP_CASE(19)
+        MPH_XP_CASE(27)
+    }
+#undef MPH_XP_CASE
+    return cudaErrorInvalidValue;
+}
 
 cudaError_t launch_step_f64x(int q, bool forced, const long long* fin, long long* fout, const KParams& p,
                              const KParamsX& px, const KParams* pg, const long long* kbb, int* flag,

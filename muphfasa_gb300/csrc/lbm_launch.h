@@ -65,5 +65,12 @@ cudaError_t launch_step_fast_bf16s(int q, bool forced, const void* fin, void* fo
 cudaError_t launch_step_f64x(int q, bool forced, const long long* fin, long long* fout, const KParams& p,
                              const KParamsX& px, const KParams* pg, const long long* kbb, int* flag,
                              cudaStream_t s);
+// Persistent cp.async-pipelined variant; ctas = number of resident CTAs, as
+// returned by f64x_pipe_ctas (which also raises the kernel's shared-memory
+// limit, so it must run once before the first launch; 0 on error).
+int f64x_pipe_ctas(int q, bool forced);
+cudaError_t launch_step_f64x_pipe(int q, bool forced, const long long* fin, long long* fout, const KParams& p,
+                                  const KParamsX& px, const KParams* pg, const long long* kbb, int* flag,
+                                  int ctas, cudaStream_t s);
 
 }  // namespace mph

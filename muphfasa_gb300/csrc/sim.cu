@@ -4,6 +4,7 @@
 // operations (ISimulation.H:16-44) mapped onto the kernels.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <utility>
@@ -21,6 +22,7 @@ struct mph_sim {
     KParams* d_kp = nullptr;  // global copy for the boundary path
     long long* d_kbb = nullptr;  // fixed-point bounce-back constants [27][27]
     int* d_flag = nullptr;       // range / validity flag of the fixed-point step
+    int pipe_ctas = 0;           // resident CTAs of the pipelined fixed-point kernel (0: direct kernel)
     size_t elem = 8;          // bytes per stored population value
     void* fa = nullptr;       // current populations (m_fin)
     void* fb = nullptr;       // next populations (m_fout)
@@ -197,6 +199,9 @@ cudaError_t launch_one_step(mph_sim* s) {
         case MPH_PREC_BF16S:
             return launch_step_fast_bf16s(q, forced, s->fa, s->fb, s->kp, s->d_kp, s->stream);
         case MPH_PREC_F64X:
+            if (s->pipe_ctas > 0)
+                return launch_step_f64x_pipe(q, forced, (const long long*)s->fa, (long long*)s->fb, s->kp, s->kpx,
+                                             s->d_kp, s->d_kbb, s->d_flag, s->pipe_ctas, s->stream);
             return launch_step_f64x(q, forced, (const long long*)s->fa, (long long*)s->fb, s->kp, s->kpx, s->d_kp,
                                     s->d_kbb, s->d_flag, s->stream);
     }
@@ -320,6 +325,16 @@ int mph_create(const mph_desc* desc, mph_sim** out) {
         if (e == cudaSuccess) e = cudaMemcpy(s->d_kbb, kbb, sizeof(kbb), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMalloc(&s->d_flag, sizeof(int));
         if (e == cudaSuccess) e = cudaMemset(s->d_flag, 0, sizeof(int));
+        // Kernel choice: the persistent cp.async pipeline unless
+        // MPH_F64X_KERNEL=direct asks for the one-cell-per-thread grid.
+        const char* kv = std::getenv("MPH_F64X_KERNEL");
+        if (e == cudaSuccess && !(kv && std::strcmp(kv, "direct") == 0)) {
+            s->pipe_ctas = f64x_pipe_ctas(d.q, d.forced != 0);
+            if (s->pipe_ctas <= 0) {
+                e = cudaGetLastError();
+                if (e == cudaSuccess) e = cudaErrorInvalidConfiguration;
+            }
+        }
     }
     s->red_blocks = 152 * 4;
     if (e == cudaSuccess) e = cudaMalloc(&s->d_part, sizeof(double) * 4 * s->red_blocks);

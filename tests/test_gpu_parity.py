@@ -124,6 +124,41 @@ def test_f64x_golden_within_1e12(idx, mph):
     assert err < 1e-12, err
 
 
+PIPE = [
+    ("D2Q9", (300, 37), ["Periodic"] * 6, 1.3, None, None),
+    ("D2Q9", (257, 20), ["NoSlip", "NoSlip", "NoSlip", "MovingWall", "Periodic", "Periodic"], 1.5, None,
+     {3: [0.08, 0, 0]}),
+    ("D3Q19", (40, 24, 18), ["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic", "Periodic"], 1.6,
+     (1e-5, 0.0, 0.0), None),
+    ("D3Q15", (19, 12, 10), ["Inflow", "PressureOutlet", "Periodic", "Periodic", "NoSlip", "NoSlip"], 1.25,
+     (2e-5, 0, 0), {0: [0.02, 0, 0]}),
+    ("D3Q27", (270, 6, 5), ["Inflow", "Outflow", "NoSlip", "MovingWall", "Periodic", "Periodic"], 1.6, None,
+     {0: [0.03, 0, 0], 3: [0.05, 0, 0.02]}),
+]
+
+
+@pytest.mark.parametrize("case", PIPE, ids=[f"{c[0]}_{c[1][0]}" for c in PIPE])
+def test_f64x_pipelined_kernel_equals_direct_kernel(case, mph, monkeypatch):
+    """The persistent cp.async kernel (the default) and the one-cell-per-thread
+    kernel (MPH_F64X_KERNEL=direct) compute the same integers."""
+    lat, n, faces, omega, force, U = case
+    face_U = [[0.0] * 3 for _ in range(6)]
+    for k, v in (U or {}).items():
+        face_U[k] = v
+    d = mph.make_desc(lat, n, omega, faces=faces, face_U=face_U, force=force, precision="f64x")
+    rng = np.random.default_rng(13)
+    N = int(np.prod(n))
+    rho, u = _fields(rng, N, len(n))
+    out = []
+    for kernel in ("pipe", "direct"):
+        monkeypatch.setenv("MPH_F64X_KERNEL", kernel)
+        s = mph.Simulation(d)
+        s.initialize(rho.copy(), u.copy())
+        s.advance(37)
+        out.append(s.f())
+    assert np.array_equal(out[0], out[1])
+
+
 def test_f64x_range_flag_reports_instead_of_wrapping(mph):
     """Fault injection on the host: a near-vacuum state (rho = 1e-3, below the
     fixed-point range) makes the step report MPH_ERR_NONFINITE."""
