@@ -20,7 +20,6 @@ __global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __rest
                                                     typename St::T* __restrict__ fout_base,
                                                     const Tile* __restrict__ tiles, const KParams* __restrict__ dp,
                                                     const long long* __restrict__ offs) {
-    using R = typename St::R;
     const Tile t = tiles[blockIdx.x];
     const KParams& p = dp[t.dom];
     const int x = t.x0 + threadIdx.x;
@@ -28,15 +27,7 @@ __global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __rest
     const int z = t.z0;
     if (x >= p.nx || y >= p.ny) return;
     const long long off = offs[t.dom];
-    const typename St::T* fin = fin_base + off;
-    typename St::T* fout = fout_base + off;
-    const long long c = ((long long)z * p.ny + y) * p.nx + x;
-    R f[Q];
-    pull<Q, St>(p, &p, fin, x, y, z, c, f);
-    if constexpr (ARITH == kExact) collide_exact<Q, FORCED>(p, f);
-    else collide_fast<Q, R, FORCED>(p, f);
-#pragma unroll
-    for (int n = 0; n < Q; ++n) St::template st<Q>(fout, n, c, p.ncell, f[n]);
+    step_cell<Q, St, ARITH, FORCED>(p, &p, fin_base + off, fout_base + off, x, y, z);
 }
 
 template <class F>

@@ -13,6 +13,26 @@ cudaError_t launch_step_fast(int q, bool forced, const void* fin, void* fout, co
     step_shape(p, g, b);
     auto in = static_cast<const typename St::T*>(fin);
     auto out = static_cast<typename St::T*>(fout);
+    if constexpr (St::kShift) {
+        if (p.nx % 2 == 0) {
+            KParams half = p;
+            half.nx = p.nx / 2;
+            step_shape(half, g, b);  // one thread per cell pair
+#define MPH_PAIR_CASE(QQ)                                                              \
+    case QQ:                                                                           \
+        if (forced) k_step_pair<QQ, St, true><<<g, b, 0, s>>>(in, out, p, pg);         \
+        else k_step_pair<QQ, St, false><<<g, b, 0, s>>>(in, out, p, pg);               \
+        return cudaGetLastError();
+            switch (q) {
+                MPH_PAIR_CASE(9)
+                MPH_PAIR_CASE(15)
+                MPH_PAIR_CASE(19)
+                MPH_PAIR_CASE(27)
+            }
+#undef MPH_PAIR_CASE
+            return cudaErrorInvalidValue;
+        }
+    }
 #define MPH_FAST_CASE(QQ)                                                              \
     case QQ:                                                                           \
         if (forced) k_step<QQ, St, kFast, true><<<g, b, 0, s>>>(in, out, p, pg);      \

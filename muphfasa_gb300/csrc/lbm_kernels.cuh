@@ -82,6 +82,7 @@ struct KParamsX {
 // ---------------------------------------------------------------------------
 struct StF64 {
     using T = double;
+    static constexpr bool kShift = false;
     using R = double;
     template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int, unsigned e) { return __ldg(f + e); }
     template <int Q> static __device__ __forceinline__ void ste(T* __restrict__ f, int, unsigned e, R v) { f[e] = v; }
@@ -96,6 +97,7 @@ struct StF64 {
 };
 struct StF32 {
     using T = float;
+    static constexpr bool kShift = false;
     using R = float;
     template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int, unsigned e) { return __ldg(f + e); }
     template <int Q> static __device__ __forceinline__ void ste(T* __restrict__ f, int, unsigned e, R v) { f[e] = v; }
@@ -113,6 +115,17 @@ struct StF32 {
 struct StF16S {
     using T = __half;
     using R = float;
+    // Shifted kernels work on g = f - w directly: one value (ldr1/str1) or an
+    // aligned pair of neighbouring cells (ldr2/str2, e even).
+    static constexpr bool kShift = true;
+    static __device__ __forceinline__ float ldr1(const T* __restrict__ f, unsigned e) { return __half2float(f[e]); }
+    static __device__ __forceinline__ float2 ldr2(const T* __restrict__ f, unsigned e) {
+        return __half22float2(*reinterpret_cast<const __half2*>(f + e));
+    }
+    static __device__ __forceinline__ void str1(T* __restrict__ f, unsigned e, float v) { f[e] = __float2half_rn(v); }
+    static __device__ __forceinline__ void str2(T* __restrict__ f, unsigned e, float2 v) {
+        *reinterpret_cast<__half2*>(f + e) = __floats2half2_rn(v.x, v.y);
+    }
     template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int n, unsigned e) {
         return __half2float(f[e]) + (float)Lat<Q>::w(n);
     }
@@ -132,6 +145,19 @@ struct StF16S {
 struct StBF16S {
     using T = __nv_bfloat16;
     using R = float;
+    static constexpr bool kShift = true;
+    // bf16 is the high half of an FP32 word: widening is a shift / mask.
+    static __device__ __forceinline__ float ldr1(const T* __restrict__ f, unsigned e) {
+        return __uint_as_float((unsigned)__ldg(reinterpret_cast<const unsigned short*>(f) + e) << 16);
+    }
+    static __device__ __forceinline__ float2 ldr2(const T* __restrict__ f, unsigned e) {
+        const unsigned w = __ldg(reinterpret_cast<const unsigned*>(f + e));
+        return make_float2(__uint_as_float(w << 16), __uint_as_float(w & 0xffff0000u));
+    }
+    static __device__ __forceinline__ void str1(T* __restrict__ f, unsigned e, float v) { f[e] = __float2bfloat16_rn(v); }
+    static __device__ __forceinline__ void str2(T* __restrict__ f, unsigned e, float2 v) {
+        *reinterpret_cast<__nv_bfloat162*>(f + e) = __floats2bfloat162_rn(v.x, v.y);
+    }
     template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int n, unsigned e) {
         return __bfloat162float(f[e]) + (float)Lat<Q>::w(n);
     }
@@ -156,6 +182,7 @@ struct StBF16S {
 constexpr int kFxShift = 56;
 struct StF64X {
     using T = long long;
+    static constexpr bool kShift = false;
     using R = double;
     template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int n, unsigned e) {
         return ((double)__ldg(f + e) * 0x1p-56) / Lat<Q>::iw(n);
@@ -491,6 +518,176 @@ __device__ __forceinline__ void collide_fast(const KParams& p, R* f) {
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// Shifted FP32 collide for the 16-bit storage policies: the state is
+// g_n = f_n - w_n, so rho = 1 + sum g and j = sum c g (sum w = 1, sum c w = 0),
+// and the post-collision value is
+//   g'_n = (1 - omega) g_n + omega (feq_n - w_n) [+ Guo term],
+//   omega (feq_n - w_n) = (omega w_n rho) (3 c.u + 4.5 (c.u)^2 - 1.5 u.u)
+//                         + omega w_n (rho - 1),
+// one FMA per population after the per-pair terms.  The arithmetic is
+// written with explicitly rounded operations over a value type V: float (one
+// cell per thread) or float2 (two cells per thread, packed FP32x2
+// instructions of sm_100 and later), so both forms round identically.
+// ---------------------------------------------------------------------------
+struct A1 {
+    using V = float;
+    static __device__ __forceinline__ V add(V a, V b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ V mul(V a, V b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ V fma(V a, V b, V c) { return __fmaf_rn(a, b, c); }
+    static __device__ __forceinline__ V splat(float c) { return c; }
+    static __device__ __forceinline__ V rcp(V a) { return rcp_nr(a); }
+    // 1/x for x near 1: hardware approximation refined by one Newton step.
+    static __device__ __forceinline__ float rcp_nr(float x) {
+        float r;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+        const float e = __fmaf_rn(-x, r, 1.0f);
+        return __fmaf_rn(r, e, r);
+    }
+};
+struct A2 {
+    using V = float2;
+    static __device__ __forceinline__ V add(V a, V b) { return __fadd2_rn(a, b); }
+    static __device__ __forceinline__ V mul(V a, V b) { return __fmul2_rn(a, b); }
+    static __device__ __forceinline__ V fma(V a, V b, V c) { return __ffma2_rn(a, b, c); }
+    static __device__ __forceinline__ V splat(float c) { return make_float2(c, c); }
+    static __device__ __forceinline__ V rcp(V a) { return make_float2(A1::rcp_nr(a.x), A1::rcp_nr(a.y)); }
+};
+
+// acc (+/-)= v; `have` says whether acc holds a value yet (folded at compile
+// time after unrolling).
+template <class A>
+__device__ __forceinline__ void acc_signed(typename A::V& acc, bool& have, int sign, typename A::V v) {
+    if (sign == 0) return;
+    const typename A::V m1 = A::splat(-1.0f);
+    if (sign > 0) acc = have ? A::add(acc, v) : v;
+    else acc = have ? A::fma(m1, v, acc) : A::mul(m1, v);
+    have = true;
+}
+
+template <int Q, class A>
+__device__ __forceinline__ typename A::V cdot_s(int n, const typename A::V* u) {
+    using L = Lat<Q>;
+    typename A::V r = A::splat(0.0f);
+    bool have = false;
+    acc_signed<A>(r, have, L::cx(n), u[0]);
+    acc_signed<A>(r, have, L::cy(n), u[1]);
+    if (L::D == 3) acc_signed<A>(r, have, L::cz(n), u[2]);
+    return r;
+}
+
+template <int Q, class A, bool FORCED>
+__device__ __forceinline__ void collide_shift(const KParams& p, typename A::V* g) {
+    using L = Lat<Q>;
+    using V = typename A::V;
+    const V m1 = A::splat(-1.0f);
+    V dr = g[0], j[3] = {A::splat(0.0f), A::splat(0.0f), A::splat(0.0f)};
+    bool hj[3] = {false, false, false};
+#pragma unroll
+    for (int n = 1; n < Q; ++n) {
+        const int m = L::opp(n);
+        if (m < n) continue;
+        const V sm = A::add(g[n], g[m]);
+        const V df = A::fma(m1, g[m], g[n]);
+        dr = A::add(dr, sm);
+        acc_signed<A>(j[0], hj[0], L::cx(n), df);
+        acc_signed<A>(j[1], hj[1], L::cy(n), df);
+        if (L::D == 3) acc_signed<A>(j[2], hj[2], L::cz(n), df);
+    }
+    const V rho = A::add(A::splat(1.0f), dr);
+    const V inv = A::rcp(rho);
+    V u[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (a == 2 && L::D == 2) { u[a] = A::splat(0.0f); continue; }
+        u[a] = FORCED ? A::mul(A::add(j[a], A::splat(p.hF_f[a])), inv) : A::mul(j[a], inv);
+    }
+    V usq = A::mul(u[0], u[0]);
+    usq = A::fma(u[1], u[1], usq);
+    if (L::D == 3) usq = A::fma(u[2], u[2], usq);
+    const V Bp = A::mul(A::splat(-1.5f), usq);
+    const float om = p.omega_f;
+    const V omc = A::splat(1.0f - om);
+    V U = A::splat(0.0f);
+    if (FORCED) {
+        U = A::mul(u[0], A::splat(p.F_f[0]));
+        U = A::fma(u[1], A::splat(p.F_f[1]), U);
+        if (L::D == 3) U = A::fma(u[2], A::splat(p.F_f[2]), U);
+    }
+    {
+        const float ow = om * (float)L::w(0);
+        V e = A::fma(A::mul(A::splat(ow), rho), Bp, A::mul(A::splat(ow), dr));
+        if (FORCED) e = A::fma(A::splat(-p.gpref_f[0]), U, e);
+        g[0] = A::fma(omc, g[0], e);
+    }
+#pragma unroll
+    for (int n = 1; n < Q; ++n) {
+        const int m = L::opp(n);
+        if (m < n) continue;
+        const float ow = om * (float)L::w(n);
+        const V Ak = A::mul(A::splat(ow), rho);
+        const V Ck = A::mul(A::splat(ow), dr);
+        const V cu = cdot_s<Q, A>(n, u);
+        const V b = A::mul(A::splat(3.0f), cu);
+        const V ap = A::fma(A::mul(A::splat(4.5f), cu), cu, Bp);
+        V en = A::fma(Ak, A::add(ap, b), Ck);
+        V em = A::fma(Ak, A::fma(m1, b, ap), Ck);
+        if (FORCED) {
+            // Guo: gpref_n ((c_n.F)(1 + 3 c_n.u) - u.F); c_m = -c_n.
+            const float qn = p.gpref_f[n] * p.gcF_f[n];
+            const V nGU = A::mul(A::splat(-p.gpref_f[n]), U);
+            en = A::add(en, A::fma(b, A::splat(qn), A::add(nGU, A::splat(qn))));
+            em = A::add(em, A::fma(b, A::splat(qn), A::add(nGU, A::splat(-qn))));
+        }
+        g[n] = A::fma(omc, g[n], en);
+        g[m] = A::fma(omc, g[m], em);
+    }
+}
+
+// Pull of g = f - w for the shifted policies: raw values away from walls, the
+// boundary rules (on f) next to them.
+template <int Q, class St>
+__device__ __forceinline__ void pull_shift(const KParams& p, const KParams* __restrict__ pg,
+                                           const typename St::T* __restrict__ fin, int x, int y, int z, long long c,
+                                           float* g) {
+    using L = Lat<Q>;
+    const Nbr o = neighbours<L::D>(p, x, y, z);
+    if (!o.wall) {
+        const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
+#pragma unroll
+        for (int n = 0; n < Q; ++n) g[n] = St::ldr1(fin, (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(o, n)));
+    } else {
+        pull_edge<Q, St>(p, pg, fin, x, y, z, c, g);
+#pragma unroll
+        for (int n = 0; n < Q; ++n) g[n] = __fadd_rn(g[n], -(float)L::w(n));
+    }
+}
+
+// One step of one cell for any storage policy: pull, collide, store.
+template <int Q, class St, int ARITH, bool FORCED>
+__device__ __forceinline__ void step_cell(const KParams& p, const KParams* __restrict__ pg,
+                                          const typename St::T* __restrict__ fin, typename St::T* __restrict__ fout,
+                                          int x, int y, int z) {
+    using R = typename St::R;
+    const long long c = ((long long)z * p.ny + y) * p.nx + x;
+    const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
+    if constexpr (St::kShift) {
+        float g[Q];
+        pull_shift<Q, St>(p, pg, fin, x, y, z, c, g);
+        collide_shift<Q, A1, FORCED>(p, g);
+#pragma unroll
+        for (int n = 0; n < Q; ++n) St::str1(fout, (unsigned)n * N + ci, g[n]);
+    } else {
+        R f[Q];
+        pull<Q, St>(p, pg, fin, x, y, z, c, f);
+        if constexpr (ARITH == kExact) collide_exact<Q, FORCED>(p, f);
+        else collide_fast<Q, R, FORCED>(p, f);
+#pragma unroll
+        for (int n = 0; n < Q; ++n) St::template ste<Q>(fout, n, (unsigned)n * N + ci, f[n]);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Kernels on the handle's SoA state (no ghost layer).
 // Block (BX, BY): lanes run along x so every warp shares (y, z).
@@ -498,19 +695,51 @@ __device__ __forceinline__ void collide_fast(const KParams& p, R* f) {
 template <int Q, class St, int ARITH, bool FORCED>
 __global__ void __launch_bounds__(256) k_step(const typename St::T* __restrict__ fin, typename St::T* __restrict__ fout,
                                               const KParams p, const KParams* __restrict__ pg) {
-    using R = typename St::R;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int z = blockIdx.z;
     if (x >= p.nx || y >= p.ny) return;
+    step_cell<Q, St, ARITH, FORCED>(p, pg, fin, fout, x, y, z);
+}
+
+// Shifted 16-bit policies with nx even: each thread advances the cell pair
+// (x, x+1), x even, with packed FP32x2 arithmetic.  Populations with c_x = 0
+// come from an aligned pair and are read as one 32-bit word; all stores are
+// 32-bit words.  (nx even makes every row, plane and population offset even.)
+template <int Q, class St, bool FORCED>
+__global__ void __launch_bounds__(256) k_step_pair(const typename St::T* __restrict__ fin,
+                                                   typename St::T* __restrict__ fout, const KParams p,
+                                                   const KParams* __restrict__ pg) {
+    using L = Lat<Q>;
+    const int x = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x >= p.nx || y >= p.ny) return;
     const long long c = ((long long)z * p.ny + y) * p.nx + x;
-    R f[Q];
-    pull<Q, St>(p, pg, fin, x, y, z, c, f);
-    if constexpr (ARITH == kExact) collide_exact<Q, FORCED>(p, f);
-    else collide_fast<Q, R, FORCED>(p, f);
     const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
+    const Nbr oa = neighbours<L::D>(p, x, y, z), ob = neighbours<L::D>(p, x + 1, y, z);
+    float2 g[Q];
+    if (!oa.wall && !ob.wall) {
 #pragma unroll
-    for (int n = 0; n < Q; ++n) St::template ste<Q>(fout, n, (unsigned)n * N + ci, f[n]);
+        for (int n = 0; n < Q; ++n) {
+            const unsigned ea = (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(oa, n));
+            if (L::cx(n) == 0) {
+                g[n] = St::ldr2(fin, ea);
+            } else {
+                const unsigned eb = (unsigned)n * N + (unsigned)((int)ci + 1 + upstream<Q>(ob, n));
+                g[n] = make_float2(St::ldr1(fin, ea), St::ldr1(fin, eb));
+            }
+        }
+    } else {
+        float ga[Q], gb[Q];
+        pull_shift<Q, St>(p, pg, fin, x, y, z, c, ga);
+        pull_shift<Q, St>(p, pg, fin, x + 1, y, z, c + 1, gb);
+#pragma unroll
+        for (int n = 0; n < Q; ++n) g[n] = make_float2(ga[n], gb[n]);
+    }
+    collide_shift<Q, A2, FORCED>(p, g);
+#pragma unroll
+    for (int n = 0; n < Q; ++n) St::str2(fout, (unsigned)n * N + ci, g[n]);
 }
 
 // updateMacroscopic (SimulationSetup.cpp:142-166): moments of the streamed

@@ -325,10 +325,11 @@ int mph_create(const mph_desc* desc, mph_sim** out) {
         if (e == cudaSuccess) e = cudaMemcpy(s->d_kbb, kbb, sizeof(kbb), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMalloc(&s->d_flag, sizeof(int));
         if (e == cudaSuccess) e = cudaMemset(s->d_flag, 0, sizeof(int));
-        // Kernel choice: the persistent cp.async pipeline unless
-        // MPH_F64X_KERNEL=direct asks for the one-cell-per-thread grid.
+        // Kernel choice: one cell per thread (measured faster on GB300: 18.0
+        // vs 16.5 GLUPS at 512^3 D3Q19), or the persistent cp.async pipeline
+        // with MPH_F64X_KERNEL=pipe.
         const char* kv = std::getenv("MPH_F64X_KERNEL");
-        if (e == cudaSuccess && !(kv && std::strcmp(kv, "direct") == 0)) {
+        if (e == cudaSuccess && kv && std::strcmp(kv, "pipe") == 0) {
             s->pipe_ctas = f64x_pipe_ctas(d.q, d.forced != 0);
             if (s->pipe_ctas <= 0) {
                 e = cudaGetLastError();

@@ -42,18 +42,21 @@ def test_batch_domains_equal_single_handles(precision, mph):
     assert total == sum(batch.ncells) and width in (32, 64, 128, 256) and ntiles > 0
 
 
-def test_batch_3d_forced_mixed_boundaries(mph):
+@pytest.mark.parametrize("precision", ["f64", "f16s", "bf16s"])
+def test_batch_3d_forced_mixed_boundaries(precision, mph):
     faces_a = ["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic", "Periodic"]
     faces_b = ["Inflow", "PressureOutlet", "NoSlip", "MovingWall", "Periodic", "Periodic"]
     Ub = [[0.0] * 3 for _ in range(6)]
     Ub[0][0] = 0.02
     Ub[3][0] = 0.05
-    descs = [mph.make_desc("D3Q19", (20, 12, 9), 1.3, faces=faces_a, force=(1e-5, 0, 0), precision="f64"),
+    descs = [mph.make_desc("D3Q19", (20, 12, 9), 1.3, faces=faces_a, force=(1e-5, 0, 0), precision=precision),
              mph.make_desc("D3Q19", (7, 16, 11), 1.6, faces=faces_b, face_U=Ub, face_rho=[1, 1.01, 1, 1, 1, 1],
-                           force=(2e-5, 1e-6, 0), precision="f64")]
+                           force=(2e-5, 1e-6, 0), precision=precision),
+             mph.make_desc("D3Q19", (10, 8, 6), 1.1, faces=faces_b, face_U=Ub, face_rho=[1, 1.01, 1, 1, 1, 1],
+                           force=(1e-5, 0, 2e-6), precision=precision)]
     batch = mph.Batch(descs)
     singles = [mph.Simulation(d) for d in descs]
-    for i in range(2):
+    for i in range(len(descs)):
         batch.initialize(i)
         singles[i].initialize()
     batch.advance(31)

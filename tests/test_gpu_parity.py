@@ -139,8 +139,8 @@ PIPE = [
 
 @pytest.mark.parametrize("case", PIPE, ids=[f"{c[0]}_{c[1][0]}" for c in PIPE])
 def test_f64x_pipelined_kernel_equals_direct_kernel(case, mph, monkeypatch):
-    """The persistent cp.async kernel (the default) and the one-cell-per-thread
-    kernel (MPH_F64X_KERNEL=direct) compute the same integers."""
+    """The persistent cp.async kernel (MPH_F64X_KERNEL=pipe) and the default
+    one-cell-per-thread kernel compute the same integers."""
     lat, n, faces, omega, force, U = case
     face_U = [[0.0] * 3 for _ in range(6)]
     for k, v in (U or {}).items():
