@@ -261,7 +261,10 @@ int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out) {
         build_params_public(ds, tab, b->params_h[d]);
         const long long cells = (long long)ds.n[0] * ds.n[1] * ds.n[2];
         b->offs_h.push_back(off);
-        off += cells * ds.q;
+        // Each domain starts on a 128-element boundary (>= 256 B): aligned
+        // rows for every precision and the 32-bit pair accesses of the
+        // 16-bit kernels in the per-domain (looped) launches.
+        off += (cells * ds.q + 127) / 128 * 128;
         b->total_cells += cells;
         b->max_cells = cells > b->max_cells ? cells : b->max_cells;
     }

@@ -14,7 +14,10 @@ cudaError_t launch_step_fast(int q, bool forced, const void* fin, void* fout, co
     auto in = static_cast<const typename St::T*>(fin);
     auto out = static_cast<typename St::T*>(fout);
     if constexpr (St::kShift) {
-        if (p.nx % 2 == 0) {
+        // Pairs of cells are read and written as 32-bit words: nx even makes
+        // every pair offset even, and both arrays must be 4-byte aligned.
+        const bool aligned = ((reinterpret_cast<unsigned long long>(fin) | reinterpret_cast<unsigned long long>(fout)) & 3) == 0;
+        if (p.nx % 2 == 0 && aligned) {
             KParams half = p;
             half.nx = p.nx / 2;
             step_shape(half, g, b);  // one thread per cell pair

@@ -707,7 +707,7 @@ __global__ void __launch_bounds__(256) k_step(const typename St::T* __restrict__
 // come from an aligned pair and are read as one 32-bit word; all stores are
 // 32-bit words.  (nx even makes every row, plane and population offset even.)
 template <int Q, class St, bool FORCED>
-__global__ void __launch_bounds__(256) k_step_pair(const typename St::T* __restrict__ fin,
+__global__ void __launch_bounds__(256, 3) k_step_pair(const typename St::T* __restrict__ fin,
                                                    typename St::T* __restrict__ fout, const KParams p,
                                                    const KParams* __restrict__ pg) {
     using L = Lat<Q>;

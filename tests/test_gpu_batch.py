@@ -65,8 +65,14 @@ def test_batch_3d_forced_mixed_boundaries(precision, mph):
         assert np.array_equal(batch.f(i), s.f())
 
 
-def test_looped_launches_equal_batched(mph):
-    descs = mph.cavity_batch_descs(12, seed=3, side=(16, 80))
+@pytest.mark.parametrize("precision", ["f32", "f16s", "bf16s"])
+def test_looped_launches_equal_batched(precision, mph):
+    """Per-domain launches (the single-domain kernels, two cells per thread
+    for the 16-bit policies on even sides) against the batched kernel; the
+    draw mixes odd and even sides."""
+    descs = mph.cavity_batch_descs(12, seed=3, side=(16, 80), precision=precision)
+    sides = [d.n[0] for d in descs]
+    assert any(n % 2 for n in sides) and any(n % 2 == 0 for n in sides)
     a, b = mph.Batch(descs), mph.Batch(descs)
     for i in range(len(descs)):
         a.initialize(i)
