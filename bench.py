@@ -180,12 +180,12 @@ def run_batch(args):
     import muphfasa_gb300 as m
     m.set_device(0)
     prec = args.precision if args.precision in ("f32", "f16s", "bf16s", "f64", "f64_fast") else "f32"
-    descs = m.cavity_batch_descs(512, precision=prec)
+    descs = m.cavity_batch_descs(args.domains, precision=prec)
     batch = m.Batch(descs)
     for i in range(len(descs)):
         batch.initialize(i)
     batch.advance(args.warmup)
-    total, width, ntiles = batch.info()
+    total, kcells, nchunks = batch.info()
     with ClockSampler(0) as clk:
         ms = batch.advance_timed(args.steps)
     ms_loop = batch.advance_looped_timed(max(2, args.steps // 4))
@@ -198,13 +198,13 @@ def run_batch(args):
     line = {"metric": METRIC, "value": round(value, 3), "unit": "MLUPS", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[prec], "data": "synthetic",
-            "config": {"workload": "batch512_cavities_d2q9", "domains": 512, "total_cells": total,
+            "config": {"workload": f"batch{args.domains}_cavities_d2q9", "domains": args.domains, "total_cells": total,
                        "side": [64, 512], "Re": [100, 5000], "lid": 0.1, "precision": prec,
-                       "tile_width": width, "tiles": ntiles, "graph": "2-step CUDA graph"},
+                       "cells_per_thread": kcells, "chunks": nchunks, "graph": "2-step CUDA graph"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": kind,
                          "bytes_per_cell_update": 2 * q * es},
-            "looped_single_domain": {"value": round(looped, 3), "unit": "MLUPS", "launches_per_step": 512},
+            "looped_single_domain": {"value": round(looped, 3), "unit": "MLUPS", "launches_per_step": args.domains},
             "clocks": clk.summary(), "gpu_launches": args.steps}
     print(json.dumps(line), flush=True)
     batch.close()
@@ -221,6 +221,7 @@ def main():
     ap.add_argument("--precision", default="f64x", choices=list(ELEM))
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--domains", type=int, default=512, help="domains of the batch512 workload")
     ap.add_argument("--probes", action="store_true", help="build and run bench_probes.cu (pipe rates, pull-copy)")
     ap.add_argument("--workload", default="channel", choices=["channel", "batch512"],
                     help="channel: the D3Q19 channel (headline); batch512: 512 uneven D2Q9 cavities")

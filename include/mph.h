@@ -214,8 +214,9 @@ int mph_batch_advance_timed(mph_batch* b, int nsteps, float* ms);
 int mph_batch_advance_looped_timed(mph_batch* b, int nsteps, float* ms);
 int mph_batch_get_f(mph_batch* b, int domain, double* f);
 int mph_batch_moments(mph_batch* b, int domain, double* rho, double* u);
-/* Total cells, chosen tile width (0 before the first advance), tile count. */
-int mph_batch_info(const mph_batch* b, long long* total_cells, int* tile_width, int* ntiles);
+/* Total cells, cells per thread chosen by the autotuner (0 before the first
+ * advance) and the number of 256-thread chunks per step. */
+int mph_batch_info(const mph_batch* b, long long* total_cells, int* cells_per_thread, int* nchunks);
 
 /* ---- allocation-free sums ---------------------------------------------- */
 /* No counterpart in the reference.  The FP64 mass and momentum sums of

@@ -352,6 +352,7 @@ class Batch:
         return rho, u
 
     def info(self):
+        """(total cells, cells per thread chosen by the autotuner, chunks per step)."""
         tc, tw, nt = C.c_longlong(), C.c_int(), C.c_int()
         check(lib().mph_batch_info(self._h, C.byref(tc), C.byref(tw), C.byref(nt)))
         return int(tc.value), int(tw.value), int(nt.value)

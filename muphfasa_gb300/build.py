@@ -26,7 +26,7 @@ NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-X
 # Translation units that must keep the reference's operation order.
 EXACT_TUS = {"k_f64_exact.cu"}
 HOST_TUS = ["host_config.cpp"]
-DEVICE_TUS = ["k_f64_exact.cu", "k_fast_f64.cu", "k_fast_f32.cu", "k_fast_f16.cu", "k_f64x.cu", "noalloc.cu", "batch.cu", "sim.cu"]
+DEVICE_TUS = ["k_f64_exact.cu", "k_fast_f64.cu", "k_fast_f32.cu", "k_fast_f16.cu", "k_fast_bf16.cu", "k_f64x.cu", "noalloc.cu", "batch.cu", "sim.cu"]
 
 
 def _nvcc() -> str:
@@ -71,7 +71,7 @@ def _compile(src_name: str, verbose: bool):
 def build(verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     tus = DEVICE_TUS + HOST_TUS
-    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(12, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), tus))
     if os.path.exists(LIB) and all(os.path.getmtime(o) <= os.path.getmtime(LIB) for o in objs):
         return LIB

@@ -4,16 +4,17 @@
 // ensemble (hundreds of lid-driven cavities of different size and Reynolds
 // number) would run hundreds of solver instances.  Here all domains share one
 // population buffer (domain-major, then population, then cell) and one kernel
-// per step covers every domain: the grid is a flat list of tiles, each tile
-// naming its domain, so the work is balanced across the 152 SMs however
-// uneven the domains are.  Each domain's constants (KParams: size, omega,
+// per step covers every domain: the grid is a flat list of chunks of 256 K
+// consecutive cells, each naming its domain, so the work is balanced across
+// the 152 SMs however uneven the domains are, and no lane idles on a ragged
+// domain edge.  Each domain's constants (KParams: size, omega,
 // boundary table) sit in global memory and are read by the same pull /
 // collide device code as a single domain, so every domain's result is
 // bit-identical to a single-domain handle with the same description.
 //
 // Step pairs (A->B, B->A) are captured once in a CUDA graph and replayed.
-// The tile shape is chosen by an autotuner that times the candidate shapes on
-// the batch itself and caches the winner per (Q, precision, size class).
+// K (cells per thread) is chosen by an autotuner that times the candidates
+// on the batch itself and caches the winner per (Q, precision, size class).
 // mph_batch_advance_looped_timed runs the same steps as one launch per domain
 // per step, the baseline the batched kernel is compared with.
 #include <cmath>
@@ -33,15 +34,15 @@ using namespace mph;
 
 namespace {
 
-cudaError_t launch_batch(int prec, int q, bool forced, const void* fin, void* fout, const Tile* tiles, int ntiles,
-                         dim3 block, const KParams* dp, const long long* offs, cudaStream_t s) {
+cudaError_t launch_batch(int prec, int q, bool forced, int K, const void* fin, void* fout, const Chunk* chunks,
+                         int nchunks, const KParams* dp, const long long* offs, cudaStream_t s) {
     switch (prec) {
         case MPH_PREC_F64:
-            return launch_batch_exact(q, forced, (const double*)fin, (double*)fout, tiles, ntiles, block, dp, offs, s);
-        case MPH_PREC_F64_FAST: return launch_batch_t<StF64, kFast>(q, forced, fin, fout, tiles, ntiles, block, dp, offs, s);
-        case MPH_PREC_F32: return launch_batch_t<StF32, kFast>(q, forced, fin, fout, tiles, ntiles, block, dp, offs, s);
-        case MPH_PREC_F16S: return launch_batch_t<StF16S, kFast>(q, forced, fin, fout, tiles, ntiles, block, dp, offs, s);
-        case MPH_PREC_BF16S: return launch_batch_t<StBF16S, kFast>(q, forced, fin, fout, tiles, ntiles, block, dp, offs, s);
+            return launch_batch_exact(q, forced, K, (const double*)fin, (double*)fout, chunks, nchunks, dp, offs, s);
+        case MPH_PREC_F64_FAST: return launch_batch_fast_f64(q, forced, K, fin, fout, chunks, nchunks, dp, offs, s);
+        case MPH_PREC_F32: return launch_batch_f32(q, forced, K, fin, fout, chunks, nchunks, dp, offs, s);
+        case MPH_PREC_F16S: return launch_batch_f16s(q, forced, K, fin, fout, chunks, nchunks, dp, offs, s);
+        case MPH_PREC_BF16S: return launch_batch_bf16s(q, forced, K, fin, fout, chunks, nchunks, dp, offs, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -57,12 +58,15 @@ size_t elem_of(int prec) {
     return 0;
 }
 
-// Tile widths tried by the autotuner (block = width x 256/width threads).
-constexpr int kWidths[4] = {32, 64, 128, 256};
+// Cells per thread tried by the autotuner (a chunk is 256 K cells); the
+// shifted 16-bit policies take cells in pairs, so K = 1 is skipped for them.
+constexpr int kCells[3] = {1, 2, 4};
 
-// Autotuner cache: (q, precision, log2 of the total cell count) -> width.
+bool shifted(int prec) { return prec == MPH_PREC_F16S || prec == MPH_PREC_BF16S; }
+
+// Autotuner cache: (q, precision, log2 total cells, log2 domains) -> K index.
 std::mutex g_tune_mu;
-std::map<std::tuple<int, int, int>, int> g_tune;
+std::map<std::tuple<int, int, int, int>, int> g_tune;
 
 }  // namespace
 
@@ -86,14 +90,14 @@ struct mph_batch {
     double* d_u = nullptr;
     long long max_cells = 0;
     std::vector<KParams> params_h;
-    // tiles per candidate width
-    Tile* d_tiles[4] = {nullptr, nullptr, nullptr, nullptr};
-    int ntiles[4] = {0, 0, 0, 0};
-    int width_idx = -1;  // chosen by the autotuner
+    // chunk lists per candidate K
+    Chunk* d_chunks[3] = {nullptr, nullptr, nullptr};
+    int nchunks[3] = {0, 0, 0};
+    int k_idx = -1;  // chosen by the autotuner
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaGraphExec_t graph = nullptr;  // two steps A->B->A
-    int graph_width = -1;
+    int graph_k = -1;
     double time = 0.0;
 };
 
@@ -116,62 +120,66 @@ void free_batch(mph_batch* b) {
     cudaFree(b->d_stage);
     cudaFree(b->d_rho);
     cudaFree(b->d_u);
-    for (auto* t : b->d_tiles) cudaFree(t);
+    for (auto* t : b->d_chunks) cudaFree(t);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
 }
 
-int ensure_tiles(mph_batch* b, int wi) {
-    if (b->d_tiles[wi]) return MPH_OK;
-    const int tx = kWidths[wi], ty = 256 / tx;
-    std::vector<Tile> tiles;
+int ensure_chunks(mph_batch* b, int ki) {
+    if (b->d_chunks[ki]) return MPH_OK;
+    const long long len = 256LL * kCells[ki];
+    std::vector<Chunk> chunks;
     for (int d = 0; d < b->ndom; ++d) {
         const mph_desc& ds = b->descs[d];
-        const int nz = ds.dim == 3 ? ds.n[2] : 1;
-        for (int z = 0; z < nz; ++z)
-            for (int y = 0; y < ds.n[1]; y += ty)
-                for (int x = 0; x < ds.n[0]; x += tx) tiles.push_back(Tile{d, x, y, z});
+        const long long nx = ds.n[0], ny = ds.n[1];
+        const long long cells = nx * ny * (ds.dim == 3 ? ds.n[2] : 1);
+        for (long long c = 0; c < cells; c += len) {
+            const long long row = c / nx;
+            chunks.push_back(Chunk{d, (int)c, (int)(c - row * nx), (int)((row % ny) | ((row / ny) << 16))});
+        }
     }
-    if (tiles.size() > 0x7fffffffu) return fail(MPH_ERR_ARG, "batch: too many tiles");
-    MPH_CK(cudaMalloc(&b->d_tiles[wi], sizeof(Tile) * tiles.size()), "batch tiles");
-    MPH_CK(cudaMemcpy(b->d_tiles[wi], tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice), "batch tiles");
-    b->ntiles[wi] = (int)tiles.size();
+    if (chunks.size() > 0x7fffffffu) return fail(MPH_ERR_ARG, "batch: too many chunks");
+    MPH_CK(cudaMalloc(&b->d_chunks[ki], sizeof(Chunk) * chunks.size()), "batch chunks");
+    MPH_CK(cudaMemcpy(b->d_chunks[ki], chunks.data(), sizeof(Chunk) * chunks.size(), cudaMemcpyHostToDevice),
+           "batch chunks");
+    b->nchunks[ki] = (int)chunks.size();
     return MPH_OK;
 }
 
-int step_once(mph_batch* b, int wi) {
-    const int tx = kWidths[wi];
-    MPH_CK(launch_batch(b->prec, b->q, b->forced, b->fa, b->fb, b->d_tiles[wi], b->ntiles[wi], dim3(tx, 256 / tx),
+int step_once(mph_batch* b, int ki) {
+    MPH_CK(launch_batch(b->prec, b->q, b->forced, kCells[ki], b->fa, b->fb, b->d_chunks[ki], b->nchunks[ki],
                         b->d_params, b->d_offs, b->stream),
            "batch step launch");
     std::swap(b->fa, b->fb);
     return MPH_OK;
 }
 
-// Times each candidate width on the batch itself (3 steps after 1) and keeps
-// the fastest; the choice is cached per (q, precision, size class).  An even
-// number of steps is run per candidate so the state ends in buffer A.
+// Times each candidate K on the batch itself (4 steps after 2) and keeps the
+// fastest; the choice is cached per (q, precision, size class, domain-count
+// class).  An even number of steps is run per candidate so the state ends in
+// buffer A, and the state is restored afterwards.
 int autotune(mph_batch* b) {
-    if (b->width_idx >= 0) return MPH_OK;
+    if (b->k_idx >= 0) return MPH_OK;
     const int cls = (int)std::floor(std::log2((double)b->total_cells));
-    const auto key = std::make_tuple(b->q, b->prec, cls);
+    const int dcls = (int)std::floor(std::log2((double)b->ndom));
+    const auto key = std::make_tuple(b->q, b->prec, cls, dcls);
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune.find(key);
-        if (it != g_tune.end()) b->width_idx = it->second;
+        if (it != g_tune.end()) b->k_idx = it->second;
     }
-    if (b->width_idx >= 0) return ensure_tiles(b, b->width_idx);
+    if (b->k_idx >= 0) return ensure_chunks(b, b->k_idx);
     // Snapshot the state so tuning does not advance the simulation.
     void* save = nullptr;
     const size_t bytes = elem_of(b->prec) * (size_t)b->total_elems;
     MPH_CK(cudaMalloc(&save, bytes), "autotune snapshot");
     cudaError_t e = cudaMemcpyAsync(save, b->fa, bytes, cudaMemcpyDeviceToDevice, b->stream);
     float best = 1e30f;
-    int besti = 0;
-    for (int wi = 0; wi < 4 && e == cudaSuccess; ++wi) {
-        int rc = ensure_tiles(b, wi);
+    int besti = shifted(b->prec) ? 1 : 0;
+    for (int wi = shifted(b->prec) ? 1 : 0; wi < 3 && e == cudaSuccess; ++wi) {
+        int rc = ensure_chunks(b, wi);
         if (rc) { cudaFree(save); return rc; }
         rc = step_once(b, wi);
         if (!rc) rc = step_once(b, wi);
@@ -189,7 +197,7 @@ int autotune(mph_batch* b) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     cudaFree(save);
     if (e != cudaSuccess) return cuda_fail(e, "autotune");
-    b->width_idx = besti;
+    b->k_idx = besti;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune[key] = besti;
     return MPH_OK;
@@ -197,19 +205,19 @@ int autotune(mph_batch* b) {
 
 // Two steps (A->B, B->A) captured once as a CUDA graph.
 int ensure_graph(mph_batch* b) {
-    if (b->graph && b->graph_width == b->width_idx) return MPH_OK;
+    if (b->graph && b->graph_k == b->k_idx) return MPH_OK;
     if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
     cudaGraph_t g = nullptr;
     MPH_CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "graph capture begin");
-    int rc = step_once(b, b->width_idx);
-    if (!rc) rc = step_once(b, b->width_idx);
+    int rc = step_once(b, b->k_idx);
+    if (!rc) rc = step_once(b, b->k_idx);
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (rc) { if (g) cudaGraphDestroy(g); return rc; }
     if (e != cudaSuccess) return cuda_fail(e, "graph capture end");
     e = cudaGraphInstantiate(&b->graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
-    b->graph_width = b->width_idx;
+    b->graph_k = b->k_idx;
     return MPH_OK;
 }
 
@@ -220,7 +228,7 @@ int advance_batch(mph_batch* b, int nsteps) {
     if (rc) return rc;
     for (int t = 0; t + 1 < nsteps; t += 2) MPH_CK(cudaGraphLaunch(b->graph, b->stream), "graph launch");
     if (nsteps % 2) {
-        rc = step_once(b, b->width_idx);
+        rc = step_once(b, b->k_idx);
         if (rc) return rc;
     }
     b->time += nsteps;
@@ -255,6 +263,14 @@ int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out) {
         for (int a = 0; a < ds.dim; ++a)
             if (ds.n[a] < 1) { delete b; return fail(MPH_ERR_ARG, "mph_batch_create: cell counts must be positive"); }
         if (!(ds.omega > 0.0 && ds.omega < 2.0)) { delete b; return fail(MPH_ERR_CONFIG, "mph_batch_create: omega must lie in (0, 2)"); }
+        // Chunk coordinates pack y | z << 16 and divide by float reciprocals;
+        // element indices within a domain are 32-bit.
+        if (ds.n[0] > (1 << 23) || ds.n[1] > 65535 || ds.n[2] > 32767 ||
+            (long long)ds.q * ds.n[0] * ds.n[1] * ds.n[2] >= (1LL << 32)) {
+            delete b;
+            return fail(MPH_ERR_ARG, "mph_batch_create: domain too large for a batch (nx <= 2^23, ny <= 65535, "
+                                     "nz <= 32767, q * cells < 2^32)");
+        }
         mph_resolved_bc tab[27];
         int rc = resolve_table(ds, tab);
         if (rc) { delete b; return rc; }
@@ -406,11 +422,11 @@ int mph_batch_moments(mph_batch* b, int domain, double* rho, double* u) {
     return MPH_OK;
 }
 
-int mph_batch_info(const mph_batch* b, long long* total_cells, int* tile_width, int* ntiles) {
+int mph_batch_info(const mph_batch* b, long long* total_cells, int* cells_per_thread, int* nchunks) {
     if (!b) return fail(MPH_ERR_ARG, "mph_batch_info: NULL batch");
     if (total_cells) *total_cells = b->total_cells;
-    if (tile_width) *tile_width = b->width_idx >= 0 ? kWidths[b->width_idx] : 0;
-    if (ntiles) *ntiles = b->width_idx >= 0 ? b->ntiles[b->width_idx] : 0;
+    if (cells_per_thread) *cells_per_thread = b->k_idx >= 0 ? kCells[b->k_idx] : 0;
+    if (nchunks) *nchunks = b->k_idx >= 0 ? b->nchunks[b->k_idx] : 0;
     return MPH_OK;
 }
 

@@ -1,7 +1,15 @@
-// batch_kernel.cuh -- the step kernel over a flat list of tiles of many
-// independent domains (batch.cu).  Shared between batch.cu and the FP64
-// exact translation unit, which instantiates it with the reference's
-// arithmetic (no FMA contraction).
+// batch_kernel.cuh -- the step kernel over many independent domains
+// (batch.cu).  Shared between batch.cu and the FP64 exact translation unit,
+// which instantiates it with the reference's arithmetic (no FMA contraction).
+//
+// Work unit: a chunk of 256 x K consecutive cells (linear index x + nx (y +
+// ny z)) of one domain, so every lane has a cell whatever the domain's
+// shape; only each domain's last chunk is partial.  A thread owns K cells
+// 256 apart (coalesced per k) and issues the pulls of all K before the first
+// collide, K x Q independent loads in flight.  The 16-bit shifted policies
+// take the K cells as K/2 adjacent pairs and collide them with packed FP32x2
+// arithmetic.  Each cell runs the same pull / collide device code as a
+// single-domain handle, so the results are bit-identical to it.
 #pragma once
 #include <utility>
 
@@ -9,25 +17,107 @@
 
 namespace mph {
 
-struct Tile {  // one block: a width x (256 / width) patch of one z-plane of domain dom
-    int dom, x0, y0, z0;
+struct Chunk {
+    int dom;  // domain index
+    int c0;   // first cell (linear index within the domain)
+    int x0;   // c0's coordinates: x0, and y0 | z0 << 16
+    int yz;
 };
 
 namespace {
 
-template <int Q, class St, int ARITH, bool FORCED>
+// Coordinates of cell c0 + l of the chunk's domain.  v / n by a float
+// reciprocal is exact after one correction for v < 2^24.
+__device__ __forceinline__ void chunk_cell(const KParams& p, const Chunk& ch, int l, int& x, int& y, int& z) {
+    const int v = ch.x0 + l;
+    int q = __float2int_rz(__int2float_rn(v) * p.inv_nx_f);
+    int r = v - q * p.nx;
+    if (r < 0) { r += p.nx; --q; } else if (r >= p.nx) { r -= p.nx; ++q; }
+    x = r;
+    const int w = (ch.yz & 0xffff) + q;
+    int q2 = __float2int_rz(__int2float_rn(w) * p.inv_ny_f);
+    int r2 = w - q2 * p.ny;
+    if (r2 < 0) { r2 += p.ny; --q2; } else if (r2 >= p.ny) { r2 -= p.ny; ++q2; }
+    y = r2;
+    z = (ch.yz >> 16) + q2;
+}
+
+template <int Q, class St, int ARITH, bool FORCED, int K>
 __global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __restrict__ fin_base,
                                                     typename St::T* __restrict__ fout_base,
-                                                    const Tile* __restrict__ tiles, const KParams* __restrict__ dp,
+                                                    const Chunk* __restrict__ chunks, const KParams* __restrict__ dp,
                                                     const long long* __restrict__ offs) {
-    const Tile t = tiles[blockIdx.x];
-    const KParams& p = dp[t.dom];
-    const int x = t.x0 + threadIdx.x;
-    const int y = t.y0 + threadIdx.y;
-    const int z = t.z0;
-    if (x >= p.nx || y >= p.ny) return;
-    const long long off = offs[t.dom];
-    step_cell<Q, St, ARITH, FORCED>(p, &p, fin_base + off, fout_base + off, x, y, z);
+    using R = typename St::R;
+    const Chunk ch = chunks[blockIdx.x];
+    const KParams& p = dp[ch.dom];
+    const long long off = offs[ch.dom];
+    const typename St::T* fin = fin_base + off;
+    typename St::T* fout = fout_base + off;
+    const unsigned N = (unsigned)p.ncell;
+    if constexpr (St::kShift) {
+        static_assert(K % 2 == 0, "shifted policies take cells in pairs");
+        constexpr int P = K / 2;
+        float2 g[P][Q];
+        int ca[P];
+        bool oka[P], okb[P];
+#pragma unroll
+        for (int j = 0; j < P; ++j) {
+            const int l = 2 * (threadIdx.x + 256 * j);
+            ca[j] = ch.c0 + l;
+            oka[j] = ca[j] < (int)N;
+            okb[j] = ca[j] + 1 < (int)N;
+            if (oka[j]) {
+                float a[Q], b[Q];
+                int x, y, z;
+                chunk_cell(p, ch, l, x, y, z);
+                pull_shift<Q, St>(p, &p, fin, x, y, z, ca[j], a);
+                if (okb[j]) {
+                    chunk_cell(p, ch, l + 1, x, y, z);
+                    pull_shift<Q, St>(p, &p, fin, x, y, z, ca[j] + 1, b);
+                }
+#pragma unroll
+                for (int n = 0; n < Q; ++n) g[j][n] = make_float2(a[n], okb[j] ? b[n] : a[n]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < P; ++j) {
+            if (!oka[j]) continue;
+            collide_shift<Q, A2, FORCED>(p, g[j]);
+#pragma unroll
+            for (int n = 0; n < Q; ++n) {
+                const unsigned e = (unsigned)n * N + (unsigned)ca[j];
+                if (okb[j] && (e & 1u) == 0) {
+                    St::str2(fout, e, g[j][n]);
+                } else {
+                    St::str1(fout, e, g[j][n].x);
+                    if (okb[j]) St::str1(fout, e + 1, g[j][n].y);
+                }
+            }
+        }
+    } else {
+        R f[K][Q];
+        int cc[K];
+        bool ok[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int l = threadIdx.x + 256 * k;
+            cc[k] = ch.c0 + l;
+            ok[k] = cc[k] < (int)N;
+            if (ok[k]) {
+                int x, y, z;
+                chunk_cell(p, ch, l, x, y, z);
+                pull<Q, St>(p, &p, fin, x, y, z, cc[k], f[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (!ok[k]) continue;
+            if constexpr (ARITH == kExact) collide_exact<Q, FORCED>(p, f[k]);
+            else collide_fast<Q, R, FORCED>(p, f[k]);
+#pragma unroll
+            for (int n = 0; n < Q; ++n) St::template ste<Q>(fout, n, (unsigned)n * N + (unsigned)cc[k], f[k][n]);
+        }
+    }
 }
 
 template <class F>
@@ -41,23 +131,43 @@ cudaError_t batch_with_q(int q, F&& f) {
     return cudaErrorInvalidValue;
 }
 
+// Cells per thread offered to the autotuner: K in {1, 2, 4} (pairs only for
+// the shifted policies).
 template <class St, int ARITH>
-cudaError_t launch_batch_t(int q, bool forced, const void* fin, void* fout, const Tile* tiles, int ntiles, dim3 block,
+cudaError_t launch_batch_t(int q, bool forced, int K, const void* fin, void* fout, const Chunk* chunks, int nchunks,
                            const KParams* dp, const long long* offs, cudaStream_t s) {
     return batch_with_q(q, [&](auto qc) {
         constexpr int Q = decltype(qc)::value;
         auto in = static_cast<const typename St::T*>(fin);
         auto out = static_cast<typename St::T*>(fout);
-        if (forced) k_batch_step<Q, St, ARITH, true><<<ntiles, block, 0, s>>>(in, out, tiles, dp, offs);
-        else k_batch_step<Q, St, ARITH, false><<<ntiles, block, 0, s>>>(in, out, tiles, dp, offs);
+#define MPH_BK(KK)                                                                                          \
+    if (forced) k_batch_step<Q, St, ARITH, true, KK><<<nchunks, 256, 0, s>>>(in, out, chunks, dp, offs);    \
+    else k_batch_step<Q, St, ARITH, false, KK><<<nchunks, 256, 0, s>>>(in, out, chunks, dp, offs);
+        if (K == 4) { MPH_BK(4) }
+        else if (K == 2) { MPH_BK(2) }
+        else {
+            if constexpr (St::kShift) return cudaErrorInvalidValue;
+            else { MPH_BK(1) }
+        }
+#undef MPH_BK
         return cudaGetLastError();
     });
 }
 
 }  // namespace
 
-// The FP64 exact instantiation, defined in the exact translation unit.
-cudaError_t launch_batch_exact(int q, bool forced, const double* fin, double* fout, const Tile* tiles, int ntiles,
-                               dim3 block, const KParams* dp, const long long* offs, cudaStream_t s);
+// Instantiations, one per storage precision, each defined in the kernel
+// translation unit of that precision (k_f64_exact.cu, k_fast_*.cu) so the
+// builds run in parallel.
+cudaError_t launch_batch_exact(int q, bool forced, int K, const double* fin, double* fout, const Chunk* chunks,
+                               int nchunks, const KParams* dp, const long long* offs, cudaStream_t s);
+#define MPH_DECL_BATCH(NAME)                                                                                    \
+    cudaError_t NAME(int q, bool forced, int K, const void* fin, void* fout, const Chunk* chunks, int nchunks,  \
+                     const KParams* dp, const long long* offs, cudaStream_t s);
+MPH_DECL_BATCH(launch_batch_fast_f64)
+MPH_DECL_BATCH(launch_batch_f32)
+MPH_DECL_BATCH(launch_batch_f16s)
+MPH_DECL_BATCH(launch_batch_bf16s)
+#undef MPH_DECL_BATCH
 
 }  // namespace mph

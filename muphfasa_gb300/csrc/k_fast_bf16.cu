@@ -1,0 +1,15 @@
+// k_fast_bf16.cu -- shifted BF16 storage (f - w), FP32 arithmetic (single
+// domain and batch).
+#include "batch_kernel.cuh"
+#include "k_fast_common.cuh"
+
+namespace mph {
+cudaError_t launch_step_fast_bf16s(int q, bool forced, const void* fin, void* fout, const KParams& p,
+                                   const KParams* pg, cudaStream_t s) {
+    return launch_step_fast<StBF16S>(q, forced, fin, fout, p, pg, s);
+}
+cudaError_t launch_batch_bf16s(int q, bool forced, int K, const void* fin, void* fout, const Chunk* chunks,
+                               int nchunks, const KParams* dp, const long long* offs, cudaStream_t s) {
+    return launch_batch_t<StBF16S, kFast>(q, forced, K, fin, fout, chunks, nchunks, dp, offs, s);
+}
+}  // namespace mph

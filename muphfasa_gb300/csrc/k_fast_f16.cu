@@ -1,4 +1,6 @@
-// k_fast_f16.cu -- shifted FP16 / BF16 storage (f - w), FP32 arithmetic.
+// k_fast_f16.cu -- shifted FP16 storage (f - w), FP32 arithmetic (single
+// domain and batch).
+#include "batch_kernel.cuh"
 #include "k_fast_common.cuh"
 
 namespace mph {
@@ -6,8 +8,8 @@ cudaError_t launch_step_fast_f16s(int q, bool forced, const void* fin, void* fou
                                   const KParams* pg, cudaStream_t s) {
     return launch_step_fast<StF16S>(q, forced, fin, fout, p, pg, s);
 }
-cudaError_t launch_step_fast_bf16s(int q, bool forced, const void* fin, void* fout, const KParams& p,
-                                   const KParams* pg, cudaStream_t s) {
-    return launch_step_fast<StBF16S>(q, forced, fin, fout, p, pg, s);
+cudaError_t launch_batch_f16s(int q, bool forced, int K, const void* fin, void* fout, const Chunk* chunks,
+                              int nchunks, const KParams* dp, const long long* offs, cudaStream_t s) {
+    return launch_batch_t<StF16S, kFast>(q, forced, K, fin, fout, chunks, nchunks, dp, offs, s);
 }
 }  // namespace mph

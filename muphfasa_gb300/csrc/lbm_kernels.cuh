@@ -48,6 +48,7 @@ struct KParams {
     // FP32 copies for the single-precision collide: a double->float
     // conversion runs on the FP64 pipe (2 per SM per clock on GB300).
     float omega_f, hF_f[3], F_f[3], gpref_f[27], gcF_f[27];
+    float inv_nx_f, inv_ny_f;  // 1/nx, 1/ny (cell coordinates in the batch kernel)
 };
 
 // Parameters in the compute type R of a collide.

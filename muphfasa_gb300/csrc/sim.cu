@@ -99,6 +99,8 @@ void build_params(const mph_desc& d, const mph_resolved_bc* tab, KParams& kp) {
         for (int a = 0; a < 3; ++a) kp.bc_U[c][a] = tab[c].U[a];
     }
     kp.omega_f = (float)kp.omega;
+    kp.inv_nx_f = 1.0f / (float)kp.nx;
+    kp.inv_ny_f = 1.0f / (float)kp.ny;
     for (int a = 0; a < 3; ++a) { kp.hF_f[a] = (float)kp.hF[a]; kp.F_f[a] = (float)kp.F[a]; }
     for (int n = 0; n < 27; ++n) { kp.gpref_f[n] = (float)kp.gpref[n]; kp.gcF_f[n] = (float)kp.gcF[n]; }
 }
