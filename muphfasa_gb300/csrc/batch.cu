@@ -35,14 +35,17 @@ using namespace mph;
 namespace {
 
 cudaError_t launch_batch(int prec, int q, bool forced, int K, const void* fin, void* fout, const Chunk* chunks,
-                         int nchunks, const KParams* dp, const long long* offs, cudaStream_t s) {
+                         int nchunks, const int2* walls, int nwalls, const KParams* dp, const long long* offs,
+                         cudaStream_t s) {
     switch (prec) {
         case MPH_PREC_F64:
-            return launch_batch_exact(q, forced, K, (const double*)fin, (double*)fout, chunks, nchunks, dp, offs, s);
-        case MPH_PREC_F64_FAST: return launch_batch_fast_f64(q, forced, K, fin, fout, chunks, nchunks, dp, offs, s);
-        case MPH_PREC_F32: return launch_batch_f32(q, forced, K, fin, fout, chunks, nchunks, dp, offs, s);
-        case MPH_PREC_F16S: return launch_batch_f16s(q, forced, K, fin, fout, chunks, nchunks, dp, offs, s);
-        case MPH_PREC_BF16S: return launch_batch_bf16s(q, forced, K, fin, fout, chunks, nchunks, dp, offs, s);
+            return launch_batch_exact(q, forced, K, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
+        case MPH_PREC_F64_FAST:
+            return launch_batch_fast_f64(q, forced, K, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
+        case MPH_PREC_F32: return launch_batch_f32(q, forced, K, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
+        case MPH_PREC_F16S: return launch_batch_f16s(q, forced, K, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
+        case MPH_PREC_BF16S:
+            return launch_batch_bf16s(q, forced, K, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -90,6 +93,9 @@ struct mph_batch {
     double* d_u = nullptr;
     long long max_cells = 0;
     std::vector<KParams> params_h;
+    // cells next to non-periodic faces {domain, cell}
+    int2* d_walls = nullptr;
+    int nwalls = 0;
     // chunk lists per candidate K
     Chunk* d_chunks[3] = {nullptr, nullptr, nullptr};
     int nchunks[3] = {0, 0, 0};
@@ -121,6 +127,7 @@ void free_batch(mph_batch* b) {
     cudaFree(b->d_rho);
     cudaFree(b->d_u);
     for (auto* t : b->d_chunks) cudaFree(t);
+    cudaFree(b->d_walls);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
@@ -148,9 +155,36 @@ int ensure_chunks(mph_batch* b, int ki) {
     return MPH_OK;
 }
 
+// The list of cells next to a non-periodic face (the boundary rules apply
+// to their pulls): whole rows on y / z faces, the row ends on x faces.
+int build_walls(mph_batch* b) {
+    std::vector<int2> walls;
+    for (int d = 0; d < b->ndom; ++d) {
+        const KParams& p = b->params_h[d];
+        for (int z = 0; z < p.nz; ++z)
+            for (int y = 0; y < p.ny; ++y) {
+                const int row = (z * p.ny + y) * p.nx;
+                const bool face = (!p.periodic[1] && (y == 0 || y == p.ny - 1)) ||
+                                  (b->dim == 3 && !p.periodic[2] && (z == 0 || z == p.nz - 1));
+                if (face) {
+                    for (int x = 0; x < p.nx; ++x) walls.push_back(make_int2(d, row + x));
+                } else if (!p.periodic[0]) {
+                    walls.push_back(make_int2(d, row));
+                    if (p.nx > 1) walls.push_back(make_int2(d, row + p.nx - 1));
+                }
+            }
+    }
+    if (walls.size() > 0x7fffffffu) return fail(MPH_ERR_ARG, "batch: too many wall cells");
+    b->nwalls = (int)walls.size();
+    if (walls.empty()) return MPH_OK;
+    MPH_CK(cudaMalloc(&b->d_walls, sizeof(int2) * walls.size()), "batch wall list");
+    MPH_CK(cudaMemcpy(b->d_walls, walls.data(), sizeof(int2) * walls.size(), cudaMemcpyHostToDevice), "batch wall list");
+    return MPH_OK;
+}
+
 int step_once(mph_batch* b, int ki) {
     MPH_CK(launch_batch(b->prec, b->q, b->forced, kCells[ki], b->fa, b->fb, b->d_chunks[ki], b->nchunks[ki],
-                        b->d_params, b->d_offs, b->stream),
+                        b->d_walls, b->nwalls, b->d_params, b->d_offs, b->stream),
            "batch step launch");
     std::swap(b->fa, b->fb);
     return MPH_OK;
@@ -297,6 +331,12 @@ int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out) {
     if (e == cudaSuccess) e = cudaMemcpy(b->d_offs, b->offs_h.data(), sizeof(long long) * ndomains, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         int rc = cuda_fail(e, "mph_batch_create");
+        free_batch(b);
+        delete b;
+        return rc;
+    }
+    int rc = build_walls(b);
+    if (rc) {
         free_batch(b);
         delete b;
         return rc;

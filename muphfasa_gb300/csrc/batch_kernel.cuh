@@ -8,8 +8,13 @@
 // 256 apart (coalesced per k) and issues the pulls of all K before the first
 // collide, K x Q independent loads in flight.  The 16-bit shifted policies
 // take the K cells as K/2 adjacent pairs and collide them with packed FP32x2
-// arithmetic.  Each cell runs the same pull / collide device code as a
-// single-domain handle, so the results are bit-identical to it.
+// arithmetic.  The chunk kernel pulls every cell through the wrapped
+// neighbour offsets (no divergent boundary branch: in 2-D cavities every row
+// starts and ends at a wall); a second kernel then recomputes the cells next
+// to non-periodic faces from a list with the full boundary rules, writing
+// over the chunk kernel's values for them.  Each cell runs the same pull /
+// collide device code as a single-domain handle, so the results are
+// bit-identical to it.
 #pragma once
 #include <utility>
 
@@ -70,10 +75,10 @@ __global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __rest
                 float a[Q], b[Q];
                 int x, y, z;
                 chunk_cell(p, ch, l, x, y, z);
-                pull_shift<Q, St>(p, &p, fin, x, y, z, ca[j], a);
+                pull_shift_interior<Q, St>(p, fin, x, y, z, ca[j], a);
                 if (okb[j]) {
                     chunk_cell(p, ch, l + 1, x, y, z);
-                    pull_shift<Q, St>(p, &p, fin, x, y, z, ca[j] + 1, b);
+                    pull_shift_interior<Q, St>(p, fin, x, y, z, ca[j] + 1, b);
                 }
 #pragma unroll
                 for (int n = 0; n < Q; ++n) g[j][n] = make_float2(a[n], okb[j] ? b[n] : a[n]);
@@ -106,7 +111,7 @@ __global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __rest
             if (ok[k]) {
                 int x, y, z;
                 chunk_cell(p, ch, l, x, y, z);
-                pull<Q, St>(p, &p, fin, x, y, z, cc[k], f[k]);
+                pull_interior<Q, St>(p, fin, x, y, z, cc[k], f[k]);
             }
         }
 #pragma unroll
@@ -118,6 +123,24 @@ __global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __rest
             for (int n = 0; n < Q; ++n) St::template ste<Q>(fout, n, (unsigned)n * N + (unsigned)cc[k], f[k][n]);
         }
     }
+}
+
+// Cells next to a non-periodic face: {domain, linear cell index}, one per
+// thread, with the boundary rules (runs after k_batch_step on the same
+// stream and overwrites those cells).
+template <int Q, class St, int ARITH, bool FORCED>
+__global__ void __launch_bounds__(256) k_batch_walls(const typename St::T* __restrict__ fin_base,
+                                                     typename St::T* __restrict__ fout_base,
+                                                     const int2* __restrict__ cells, int ncells,
+                                                     const KParams* __restrict__ dp,
+                                                     const long long* __restrict__ offs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ncells) return;
+    const int2 w = cells[i];
+    const KParams& p = dp[w.x];
+    const long long off = offs[w.x];
+    const int c = w.y, row = c / p.nx;
+    step_cell<Q, St, ARITH, FORCED>(p, &p, fin_base + off, fout_base + off, c - row * p.nx, row % p.ny, row / p.ny);
 }
 
 template <class F>
@@ -132,10 +155,10 @@ cudaError_t batch_with_q(int q, F&& f) {
 }
 
 // Cells per thread offered to the autotuner: K in {1, 2, 4} (pairs only for
-// the shifted policies).
+// the shifted policies).  Launches the chunk kernel, then the wall cells.
 template <class St, int ARITH>
 cudaError_t launch_batch_t(int q, bool forced, int K, const void* fin, void* fout, const Chunk* chunks, int nchunks,
-                           const KParams* dp, const long long* offs, cudaStream_t s) {
+                           const int2* walls, int nwalls, const KParams* dp, const long long* offs, cudaStream_t s) {
     return batch_with_q(q, [&](auto qc) {
         constexpr int Q = decltype(qc)::value;
         auto in = static_cast<const typename St::T*>(fin);
@@ -150,6 +173,11 @@ cudaError_t launch_batch_t(int q, bool forced, int K, const void* fin, void* fou
             else { MPH_BK(1) }
         }
 #undef MPH_BK
+        if (nwalls > 0) {
+            const int nb = (nwalls + 255) / 256;
+            if (forced) k_batch_walls<Q, St, ARITH, true><<<nb, 256, 0, s>>>(in, out, walls, nwalls, dp, offs);
+            else k_batch_walls<Q, St, ARITH, false><<<nb, 256, 0, s>>>(in, out, walls, nwalls, dp, offs);
+        }
         return cudaGetLastError();
     });
 }
@@ -159,11 +187,10 @@ cudaError_t launch_batch_t(int q, bool forced, int K, const void* fin, void* fou
 // Instantiations, one per storage precision, each defined in the kernel
 // translation unit of that precision (k_f64_exact.cu, k_fast_*.cu) so the
 // builds run in parallel.
-cudaError_t launch_batch_exact(int q, bool forced, int K, const double* fin, double* fout, const Chunk* chunks,
-                               int nchunks, const KParams* dp, const long long* offs, cudaStream_t s);
 #define MPH_DECL_BATCH(NAME)                                                                                    \
     cudaError_t NAME(int q, bool forced, int K, const void* fin, void* fout, const Chunk* chunks, int nchunks,  \
-                     const KParams* dp, const long long* offs, cudaStream_t s);
+                     const int2* walls, int nwalls, const KParams* dp, const long long* offs, cudaStream_t s);
+MPH_DECL_BATCH(launch_batch_exact)
 MPH_DECL_BATCH(launch_batch_fast_f64)
 MPH_DECL_BATCH(launch_batch_f32)
 MPH_DECL_BATCH(launch_batch_f16s)

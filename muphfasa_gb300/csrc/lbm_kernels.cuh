@@ -331,6 +331,29 @@ __device__ __forceinline__ int upstream(const Nbr& o, int n) {
     return ox + oy + oz;
 }
 
+// Pull through the wrapped neighbour offsets only, for callers that compute
+// the cells next to non-periodic faces separately (the batch): every address
+// stays inside the domain, and a wall cell's result is overwritten.
+template <int Q, class St>
+__device__ __forceinline__ void pull_interior(const KParams& p, const typename St::T* __restrict__ fin, int x, int y,
+                                              int z, long long c, typename St::R* f) {
+    using L = Lat<Q>;
+    const Nbr o = neighbours<L::D>(p, x, y, z);
+    const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
+#pragma unroll
+    for (int n = 0; n < Q; ++n)
+        f[n] = St::template lde<Q>(fin, n, (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(o, n)));
+}
+template <int Q, class St>
+__device__ __forceinline__ void pull_shift_interior(const KParams& p, const typename St::T* __restrict__ fin, int x,
+                                                    int y, int z, long long c, float* g) {
+    using L = Lat<Q>;
+    const Nbr o = neighbours<L::D>(p, x, y, z);
+    const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
+#pragma unroll
+    for (int n = 0; n < Q; ++n) g[n] = St::ldr1(fin, (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(o, n)));
+}
+
 // Pull of all Q populations into f.  Cells away from non-periodic faces use
 // 32-bit element indices (Q * N < 2^32 is checked when a handle is created);
 // cells next to a wall take pull_edge.
