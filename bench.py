@@ -185,7 +185,7 @@ def run_batch(args):
     for i in range(len(descs)):
         batch.initialize(i)
     batch.advance(args.warmup)
-    total, kcells, nchunks = batch.info()
+    total, kcells, nchunks, persistent = batch.info()
     with ClockSampler(0) as clk:
         ms = batch.advance_timed(args.steps)
     ms_loop = batch.advance_looped_timed(max(2, args.steps // 4))
@@ -200,7 +200,8 @@ def run_batch(args):
             "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[prec], "data": "synthetic",
             "config": {"workload": f"batch{args.domains}_cavities_d2q9", "domains": args.domains, "total_cells": total,
                        "side": [64, 512], "Re": [100, 5000], "lid": 0.1, "precision": prec,
-                       "cells_per_thread": kcells, "chunks": nchunks, "graph": "2-step CUDA graph"},
+                       "cells_per_thread": kcells, "chunks": nchunks, "persistent_grid": persistent,
+                       "graph": "2-step CUDA graph"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": kind,
                          "bytes_per_cell_update": 2 * q * es},

@@ -152,6 +152,16 @@ int mph_update_macroscopic(mph_sim* sim, double* rho, double* u);
 /* FP64 sums of the stored populations: out[0] = sum f (mass),
  * out[1..3] = sum c f (momentum). */
 int mph_reduce(mph_sim* sim, double* out);
+/* Steady-state residual (no counterpart in the reference), FP64 on the GPU:
+ * with u = (sum c f) / (sum f) of the stored populations,
+ *   out[0] = ||u - u_prev||_2 / ||u||_2, out[1] = ||u||_2,
+ * where u_prev is the field saved by the previous call (out[0] = +inf on the
+ * first call after mph_create / mph_init_fields / mph_set_f).  Calling it
+ * every k steps gives the relative change over k steps. */
+int mph_residual(mph_sim* sim, double* out);
+/* Velocity set of a lattice (LatticeDescriptor.H:23-263): c[3 n + d],
+ * w[n], opp[n] for n < q; any pointer may be NULL. */
+int mph_lattice(int q, int* c, double* w, int* opp);
 /* Lattice time (number of completed advance() calls since init). */
 int mph_time(const mph_sim* sim, double* t);
 /* Number of step-kernel launches one advance() issues. */
@@ -214,9 +224,14 @@ int mph_batch_advance_timed(mph_batch* b, int nsteps, float* ms);
 int mph_batch_advance_looped_timed(mph_batch* b, int nsteps, float* ms);
 int mph_batch_get_f(mph_batch* b, int domain, double* f);
 int mph_batch_moments(mph_batch* b, int domain, double* rho, double* u);
+/* Per-domain steady-state residual (as mph_residual): out[2 d] = relative
+ * change of domain d's stored-population velocity since the previous call
+ * (+inf on the first call after an init), out[2 d + 1] = ||u_d||_2. */
+int mph_batch_residual(mph_batch* b, double* out);
 /* Total cells, cells per thread chosen by the autotuner (0 before the first
- * advance) and the number of 256-thread chunks per step. */
-int mph_batch_info(const mph_batch* b, long long* total_cells, int* cells_per_thread, int* nchunks);
+ * advance), the number of 256-thread chunks per step, and whether the chosen
+ * launch is a persistent grid (1) or one block per chunk (0). */
+int mph_batch_info(const mph_batch* b, long long* total_cells, int* cells_per_thread, int* nchunks, int* persistent);
 
 /* ---- allocation-free sums ---------------------------------------------- */
 /* No counterpart in the reference.  The FP64 mass and momentum sums of

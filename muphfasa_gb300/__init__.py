@@ -41,6 +41,7 @@ EXPORTS = [
     "mph_periodic_fill_arr", "mph_bc_fill_arr", "mph_reduce_f64_noalloc", "mph_batch_create",
     "mph_batch_destroy", "mph_batch_init_fields", "mph_batch_advance", "mph_batch_advance_timed",
     "mph_batch_advance_looped_timed", "mph_batch_get_f", "mph_batch_moments", "mph_batch_info",
+    "mph_residual", "mph_batch_residual", "mph_lattice",
 ]
 
 
@@ -104,6 +105,9 @@ def lib():
     L.mph_advance.argtypes = [P, C.c_int]
     L.mph_update_macroscopic.argtypes = [P, dp, dp]
     L.mph_reduce.argtypes = [P, dp]
+    L.mph_residual.argtypes = [P, dp]
+    L.mph_lattice.argtypes = [C.c_int, C.POINTER(C.c_int), dp, C.POINTER(C.c_int)]
+    L.mph_batch_residual.argtypes = [P, dp]
     L.mph_time.argtypes = [P, dp]
     L.mph_launches_per_step.argtypes = [P, ip]
     L.mph_advance_timed.argtypes = [P, C.c_int, C.POINTER(C.c_float)]
@@ -121,7 +125,8 @@ def lib():
     L.mph_batch_advance_looped_timed.argtypes = [P, C.c_int, C.POINTER(C.c_float)]
     L.mph_batch_get_f.argtypes = [P, C.c_int, dp]
     L.mph_batch_moments.argtypes = [P, C.c_int, dp, dp]
-    L.mph_batch_info.argtypes = [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.mph_batch_info.argtypes = [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                 C.POINTER(C.c_int)]
     _lib = L
     return L
 
@@ -134,6 +139,16 @@ def check(rc: int):
 def _dp(a: np.ndarray):
     assert a.dtype == np.float64 and a.flags.c_contiguous
     return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def lattice_tables(lattice: str):
+    """(c [q, 3] int, w [q] float64, opp [q] int) of a velocity set, from the library."""
+    q = LATTICE_DQ[lattice][1]
+    c = (C.c_int * (3 * q))()
+    w = np.zeros(q)
+    opp = (C.c_int * q)()
+    check(lib().mph_lattice(q, c, _dp(w), opp))
+    return np.array(list(c), dtype=np.int64).reshape(q, 3), w, np.array(list(opp), dtype=np.int64)
 
 
 def make_desc(lattice: str, n, omega: float, faces=None, face_rho=None, face_U=None, force=None,
@@ -284,6 +299,13 @@ class Simulation:
         check(lib().mph_reduce(self._h, _dp(out)))
         return out
 
+    def residual(self):
+        """(||u - u_prev|| / ||u||, ||u||) of the stored-population velocity
+        against the previous call (inf on the first call after an init)."""
+        out = np.zeros(2)
+        check(lib().mph_residual(self._h, _dp(out)))
+        return float(out[0]), float(out[1])
+
     def time(self) -> float:
         t = C.c_double()
         check(lib().mph_time(self._h, C.byref(t)))
@@ -351,11 +373,18 @@ class Batch:
         check(lib().mph_batch_moments(self._h, int(domain), _dp(rho), _dp(u)))
         return rho, u
 
+    def residual(self):
+        """Per-domain (relative change, norm) arrays, as Simulation.residual."""
+        out = np.zeros(2 * len(self.descs))
+        check(lib().mph_batch_residual(self._h, _dp(out)))
+        return out[0::2].copy(), out[1::2].copy()
+
     def info(self):
-        """(total cells, cells per thread chosen by the autotuner, chunks per step)."""
-        tc, tw, nt = C.c_longlong(), C.c_int(), C.c_int()
-        check(lib().mph_batch_info(self._h, C.byref(tc), C.byref(tw), C.byref(nt)))
-        return int(tc.value), int(tw.value), int(nt.value)
+        """(total cells, cells per thread, chunks per step, persistent grid) of
+        the launch the autotuner chose (zeros before the first advance)."""
+        tc, tw, nt, pe = C.c_longlong(), C.c_int(), C.c_int(), C.c_int()
+        check(lib().mph_batch_info(self._h, C.byref(tc), C.byref(tw), C.byref(nt), C.byref(pe)))
+        return int(tc.value), int(tw.value), int(nt.value), bool(pe.value)
 
 
 def cavity_batch_descs(n_domains=512, seed=20261203, lattice="D2Q9", precision="f32", lid=0.1,

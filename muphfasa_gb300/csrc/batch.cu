@@ -18,6 +18,7 @@
 // mph_batch_advance_looped_timed runs the same steps as one launch per domain
 // per step, the baseline the batched kernel is compared with.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -34,18 +35,18 @@ using namespace mph;
 
 namespace {
 
-cudaError_t launch_batch(int prec, int q, bool forced, int K, const void* fin, void* fout, const Chunk* chunks,
+cudaError_t launch_batch(int prec, int q, bool forced, int K, bool P, const void* fin, void* fout, const Chunk* chunks,
                          int nchunks, const int2* walls, int nwalls, const KParams* dp, const long long* offs,
                          cudaStream_t s) {
     switch (prec) {
         case MPH_PREC_F64:
-            return launch_batch_exact(q, forced, K, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
+            return launch_batch_exact(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
         case MPH_PREC_F64_FAST:
-            return launch_batch_fast_f64(q, forced, K, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
-        case MPH_PREC_F32: return launch_batch_f32(q, forced, K, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
-        case MPH_PREC_F16S: return launch_batch_f16s(q, forced, K, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
+            return launch_batch_fast_f64(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
+        case MPH_PREC_F32: return launch_batch_f32(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
+        case MPH_PREC_F16S: return launch_batch_f16s(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
         case MPH_PREC_BF16S:
-            return launch_batch_bf16s(q, forced, K, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
+            return launch_batch_bf16s(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -61,9 +62,11 @@ size_t elem_of(int prec) {
     return 0;
 }
 
-// Cells per thread tried by the autotuner (a chunk is 256 K cells); the
-// shifted 16-bit policies take cells in pairs, so K = 1 is skipped for them.
+// Candidates of the autotuner: cand % 3 selects K, the cells per thread (a
+// chunk is 256 K cells), cand / 3 a persistent grid; the shifted 16-bit
+// policies take cells in pairs, so K = 1 is skipped for them.
 constexpr int kCells[3] = {1, 2, 4};
+constexpr int kCands = 6;
 
 bool shifted(int prec) { return prec == MPH_PREC_F16S || prec == MPH_PREC_BF16S; }
 
@@ -96,10 +99,18 @@ struct mph_batch {
     // cells next to non-periodic faces {domain, cell}
     int2* d_walls = nullptr;
     int nwalls = 0;
-    // chunk lists per candidate K
+    // chunk lists per candidate K, and the index of each domain's first chunk
     Chunk* d_chunks[3] = {nullptr, nullptr, nullptr};
     int nchunks[3] = {0, 0, 0};
-    int k_idx = -1;  // chosen by the autotuner
+    int* d_chunk_first[3] = {nullptr, nullptr, nullptr};
+    // steady-state residual: saved velocity (dim x cells, domain-major), cell
+    // offsets, partials per chunk and per-domain sums
+    double* d_uprev = nullptr;
+    long long* d_coffs = nullptr;
+    double* d_rpart = nullptr;
+    double* d_rout = nullptr;
+    bool has_uprev = false;
+    int k_idx = -1;  // candidate chosen by the autotuner
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaGraphExec_t graph = nullptr;  // two steps A->B->A
@@ -127,6 +138,11 @@ void free_batch(mph_batch* b) {
     cudaFree(b->d_rho);
     cudaFree(b->d_u);
     for (auto* t : b->d_chunks) cudaFree(t);
+    for (auto* t : b->d_chunk_first) cudaFree(t);
+    cudaFree(b->d_uprev);
+    cudaFree(b->d_coffs);
+    cudaFree(b->d_rpart);
+    cudaFree(b->d_rout);
     cudaFree(b->d_walls);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->ev0) cudaEventDestroy(b->ev0);
@@ -138,7 +154,9 @@ int ensure_chunks(mph_batch* b, int ki) {
     if (b->d_chunks[ki]) return MPH_OK;
     const long long len = 256LL * kCells[ki];
     std::vector<Chunk> chunks;
+    std::vector<int> first(b->ndom + 1, 0);
     for (int d = 0; d < b->ndom; ++d) {
+        first[d] = (int)chunks.size();
         const mph_desc& ds = b->descs[d];
         const long long nx = ds.n[0], ny = ds.n[1];
         const long long cells = nx * ny * (ds.dim == 3 ? ds.n[2] : 1);
@@ -148,6 +166,10 @@ int ensure_chunks(mph_batch* b, int ki) {
         }
     }
     if (chunks.size() > 0x7fffffffu) return fail(MPH_ERR_ARG, "batch: too many chunks");
+    first[b->ndom] = (int)chunks.size();
+    MPH_CK(cudaMalloc(&b->d_chunk_first[ki], sizeof(int) * first.size()), "batch chunk index");
+    MPH_CK(cudaMemcpy(b->d_chunk_first[ki], first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice),
+           "batch chunk index");
     MPH_CK(cudaMalloc(&b->d_chunks[ki], sizeof(Chunk) * chunks.size()), "batch chunks");
     MPH_CK(cudaMemcpy(b->d_chunks[ki], chunks.data(), sizeof(Chunk) * chunks.size(), cudaMemcpyHostToDevice),
            "batch chunks");
@@ -182,8 +204,9 @@ int build_walls(mph_batch* b) {
     return MPH_OK;
 }
 
-int step_once(mph_batch* b, int ki) {
-    MPH_CK(launch_batch(b->prec, b->q, b->forced, kCells[ki], b->fa, b->fb, b->d_chunks[ki], b->nchunks[ki],
+int step_once(mph_batch* b, int cand) {
+    const int ki = cand % 3;
+    MPH_CK(launch_batch(b->prec, b->q, b->forced, kCells[ki], cand >= 3, b->fa, b->fb, b->d_chunks[ki], b->nchunks[ki],
                         b->d_walls, b->nwalls, b->d_params, b->d_offs, b->stream),
            "batch step launch");
     std::swap(b->fa, b->fb);
@@ -196,6 +219,14 @@ int step_once(mph_batch* b, int ki) {
 // buffer A, and the state is restored afterwards.
 int autotune(mph_batch* b) {
     if (b->k_idx >= 0) return MPH_OK;
+    // MPH_BATCH_CANDIDATE=c (0..5) fixes the launch instead of timing.
+    if (const char* env = std::getenv("MPH_BATCH_CANDIDATE")) {
+        const int c = std::atoi(env);
+        if (c < 0 || c >= kCands || (shifted(b->prec) && c % 3 == 0))
+            return fail(MPH_ERR_ARG, "MPH_BATCH_CANDIDATE must be 0..5 (1, 2, 4, 5 for 16-bit storage)");
+        b->k_idx = c;
+        return ensure_chunks(b, c % 3);
+    }
     const int cls = (int)std::floor(std::log2((double)b->total_cells));
     const int dcls = (int)std::floor(std::log2((double)b->ndom));
     const auto key = std::make_tuple(b->q, b->prec, cls, dcls);
@@ -204,7 +235,7 @@ int autotune(mph_batch* b) {
         auto it = g_tune.find(key);
         if (it != g_tune.end()) b->k_idx = it->second;
     }
-    if (b->k_idx >= 0) return ensure_chunks(b, b->k_idx);
+    if (b->k_idx >= 0) return ensure_chunks(b, b->k_idx % 3);
     // Snapshot the state so tuning does not advance the simulation.
     void* save = nullptr;
     const size_t bytes = elem_of(b->prec) * (size_t)b->total_elems;
@@ -212,8 +243,9 @@ int autotune(mph_batch* b) {
     cudaError_t e = cudaMemcpyAsync(save, b->fa, bytes, cudaMemcpyDeviceToDevice, b->stream);
     float best = 1e30f;
     int besti = shifted(b->prec) ? 1 : 0;
-    for (int wi = shifted(b->prec) ? 1 : 0; wi < 3 && e == cudaSuccess; ++wi) {
-        int rc = ensure_chunks(b, wi);
+    for (int wi = 0; wi < kCands && e == cudaSuccess; ++wi) {
+        if (shifted(b->prec) && wi % 3 == 0) continue;
+        int rc = ensure_chunks(b, wi % 3);
         if (rc) { cudaFree(save); return rc; }
         rc = step_once(b, wi);
         if (!rc) rc = step_once(b, wi);
@@ -358,9 +390,6 @@ int mph_batch_init_fields(mph_batch* b, int domain, double* rho, double* u) {
     const mph_desc& ds = b->descs[domain];
     const KParams& kp = b->params_h[domain];
     const long long N = kp.ncell;
-    if (!b->d_rho || N > b->max_cells) {
-        // sized for the largest domain
-    }
     if (!b->d_rho) MPH_CK(cudaMalloc(&b->d_rho, sizeof(double) * b->max_cells), "batch rho");
     if (!b->d_u) MPH_CK(cudaMalloc(&b->d_u, sizeof(double) * 3 * b->max_cells), "batch u");
     MPH_CK(cudaMemcpyAsync(b->d_rho, rho, sizeof(double) * N, cudaMemcpyHostToDevice, b->stream), "batch init rho");
@@ -373,6 +402,7 @@ int mph_batch_init_fields(mph_batch* b, int domain, double* rho, double* u) {
     }
     MPH_CK(cudaStreamSynchronize(b->stream), "batch init");
     b->time = 0.0;
+    b->has_uprev = false;
     return MPH_OK;
 }
 
@@ -462,11 +492,44 @@ int mph_batch_moments(mph_batch* b, int domain, double* rho, double* u) {
     return MPH_OK;
 }
 
-int mph_batch_info(const mph_batch* b, long long* total_cells, int* cells_per_thread, int* nchunks) {
+int mph_batch_residual(mph_batch* b, double* out) {
+    if (!b || !out) return fail(MPH_ERR_ARG, "mph_batch_residual: NULL argument");
+    int rc = ensure_chunks(b, 0);  // K = 1 chunk list, independent of the tuned K
+    if (rc) return rc;
+    if (!b->d_uprev) {
+        std::vector<long long> coffs(b->ndom);
+        long long c = 0;
+        for (int d = 0; d < b->ndom; ++d) { coffs[d] = c; c += b->params_h[d].ncell; }
+        MPH_CK(cudaMalloc(&b->d_uprev, sizeof(double) * b->dim * b->total_cells), "batch residual field");
+        MPH_CK(cudaMalloc(&b->d_coffs, sizeof(long long) * b->ndom), "batch residual offsets");
+        MPH_CK(cudaMemcpy(b->d_coffs, coffs.data(), sizeof(long long) * b->ndom, cudaMemcpyHostToDevice),
+               "batch residual offsets");
+        MPH_CK(cudaMalloc(&b->d_rpart, sizeof(double) * 2 * b->nchunks[0]), "batch residual partials");
+        MPH_CK(cudaMalloc(&b->d_rout, sizeof(double) * 2 * b->ndom), "batch residual sums");
+    }
+    MPH_CK(launch_batch_residual(b->prec, b->q, b->fa, b->d_chunks[0], b->nchunks[0], kCells[0], b->d_params,
+                                 b->d_offs, b->d_coffs, b->d_uprev, !b->has_uprev, b->d_rpart, b->d_chunk_first[0],
+                                 b->ndom, b->d_rout, b->stream),
+           "batch residual");
+    std::vector<double> sums(2 * b->ndom);
+    MPH_CK(cudaMemcpyAsync(sums.data(), b->d_rout, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost, b->stream),
+           "batch residual download");
+    MPH_CK(cudaStreamSynchronize(b->stream), "batch residual");
+    for (int d = 0; d < b->ndom; ++d) {
+        const double s0 = sums[2 * d], s1 = sums[2 * d + 1];
+        out[2 * d + 1] = std::sqrt(s1);
+        out[2 * d] = b->has_uprev ? (s1 > 0.0 ? std::sqrt(s0 / s1) : (s0 > 0.0 ? HUGE_VAL : 0.0)) : HUGE_VAL;
+    }
+    b->has_uprev = true;
+    return MPH_OK;
+}
+
+int mph_batch_info(const mph_batch* b, long long* total_cells, int* cells_per_thread, int* nchunks, int* persistent) {
     if (!b) return fail(MPH_ERR_ARG, "mph_batch_info: NULL batch");
     if (total_cells) *total_cells = b->total_cells;
-    if (cells_per_thread) *cells_per_thread = b->k_idx >= 0 ? kCells[b->k_idx] : 0;
-    if (nchunks) *nchunks = b->k_idx >= 0 ? b->nchunks[b->k_idx] : 0;
+    if (cells_per_thread) *cells_per_thread = b->k_idx >= 0 ? kCells[b->k_idx % 3] : 0;
+    if (nchunks) *nchunks = b->k_idx >= 0 ? b->nchunks[b->k_idx % 3] : 0;
+    if (persistent) *persistent = b->k_idx >= 3 ? 1 : 0;
     return MPH_OK;
 }
 

@@ -50,10 +50,13 @@ __device__ __forceinline__ void chunk_cell(const KParams& p, const Chunk& ch, in
 template <int Q, class St, int ARITH, bool FORCED, int K>
 __global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __restrict__ fin_base,
                                                     typename St::T* __restrict__ fout_base,
-                                                    const Chunk* __restrict__ chunks, const KParams* __restrict__ dp,
+                                                    const Chunk* __restrict__ chunks, int nchunks,
+                                                    const KParams* __restrict__ dp,
                                                     const long long* __restrict__ offs) {
     using R = typename St::R;
-    const Chunk ch = chunks[blockIdx.x];
+    // One chunk per block, or a persistent grid walking the list.
+    for (int ci = blockIdx.x; ci < nchunks; ci += gridDim.x) {
+    const Chunk ch = chunks[ci];
     const KParams& p = dp[ch.dom];
     const long long off = offs[ch.dom];
     const typename St::T* fin = fin_base + off;
@@ -123,6 +126,7 @@ __global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __rest
             for (int n = 0; n < Q; ++n) St::template ste<Q>(fout, n, (unsigned)n * N + (unsigned)cc[k], f[k][n]);
         }
     }
+    }
 }
 
 // Cells next to a non-periodic face: {domain, linear cell index}, one per
@@ -154,18 +158,38 @@ cudaError_t batch_with_q(int q, F&& f) {
     return cudaErrorInvalidValue;
 }
 
+// Grid of a persistent launch: resident blocks of kernel k times the SMs.
+template <class Kern>
+int persistent_grid(Kern k) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, 0) != cudaSuccess) return 0;
+    return per_sm * sms;
+}
+
 // Cells per thread offered to the autotuner: K in {1, 2, 4} (pairs only for
-// the shifted policies).  Launches the chunk kernel, then the wall cells.
+// the shifted policies), one chunk per block or a persistent grid.  Launches
+// the chunk kernel, then the wall cells.
 template <class St, int ARITH>
-cudaError_t launch_batch_t(int q, bool forced, int K, const void* fin, void* fout, const Chunk* chunks, int nchunks,
-                           const int2* walls, int nwalls, const KParams* dp, const long long* offs, cudaStream_t s) {
+cudaError_t launch_batch_t(int q, bool forced, int K, bool persistent, const void* fin, void* fout,
+                           const Chunk* chunks, int nchunks, const int2* walls, int nwalls, const KParams* dp,
+                           const long long* offs, cudaStream_t s) {
     return batch_with_q(q, [&](auto qc) {
         constexpr int Q = decltype(qc)::value;
         auto in = static_cast<const typename St::T*>(fin);
         auto out = static_cast<typename St::T*>(fout);
-#define MPH_BK(KK)                                                                                          \
-    if (forced) k_batch_step<Q, St, ARITH, true, KK><<<nchunks, 256, 0, s>>>(in, out, chunks, dp, offs);    \
-    else k_batch_step<Q, St, ARITH, false, KK><<<nchunks, 256, 0, s>>>(in, out, chunks, dp, offs);
+#define MPH_BK(KK)                                                                                             \
+    {                                                                                                          \
+        auto kern = forced ? k_batch_step<Q, St, ARITH, true, KK> : k_batch_step<Q, St, ARITH, false, KK>;     \
+        int grid = nchunks;                                                                                    \
+        if (persistent) {                                                                                      \
+            const int g = persistent_grid(kern);                                                               \
+            if (g <= 0) return cudaErrorInvalidConfiguration;                                                  \
+            grid = g < nchunks ? g : nchunks;                                                                  \
+        }                                                                                                      \
+        kern<<<grid, 256, 0, s>>>(in, out, chunks, nchunks, dp, offs);                                         \
+    }
         if (K == 4) { MPH_BK(4) }
         else if (K == 2) { MPH_BK(2) }
         else {
@@ -187,14 +211,21 @@ cudaError_t launch_batch_t(int q, bool forced, int K, const void* fin, void* fou
 // Instantiations, one per storage precision, each defined in the kernel
 // translation unit of that precision (k_f64_exact.cu, k_fast_*.cu) so the
 // builds run in parallel.
-#define MPH_DECL_BATCH(NAME)                                                                                    \
-    cudaError_t NAME(int q, bool forced, int K, const void* fin, void* fout, const Chunk* chunks, int nchunks,  \
-                     const int2* walls, int nwalls, const KParams* dp, const long long* offs, cudaStream_t s);
+#define MPH_DECL_BATCH(NAME)                                                                                  \
+    cudaError_t NAME(int q, bool forced, int K, bool persistent, const void* fin, void* fout, const Chunk* chunks, \
+                     int nchunks, const int2* walls, int nwalls, const KParams* dp, const long long* offs,        \
+                     cudaStream_t s);
 MPH_DECL_BATCH(launch_batch_exact)
 MPH_DECL_BATCH(launch_batch_fast_f64)
 MPH_DECL_BATCH(launch_batch_f32)
 MPH_DECL_BATCH(launch_batch_f16s)
 MPH_DECL_BATCH(launch_batch_bf16s)
 #undef MPH_DECL_BATCH
+
+// Per-domain residual sums of a batch (monitor.cu): out[2 d + {0, 1}].
+cudaError_t launch_batch_residual(int prec, int q, const void* f_base, const Chunk* chunks, int nchunks, int K,
+                                  const KParams* dp, const long long* offs, const long long* coffs, double* uprev,
+                                  bool first, double* part, const int* chunk_first, int ndom, double* out,
+                                  cudaStream_t s);
 
 }  // namespace mph

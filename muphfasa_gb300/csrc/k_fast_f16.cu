@@ -8,8 +8,8 @@ cudaError_t launch_step_fast_f16s(int q, bool forced, const void* fin, void* fou
                                   const KParams* pg, cudaStream_t s) {
     return launch_step_fast<StF16S>(q, forced, fin, fout, p, pg, s);
 }
-cudaError_t launch_batch_f16s(int q, bool forced, int K, const void* fin, void* fout, const Chunk* chunks, int nchunks,
+cudaError_t launch_batch_f16s(int q, bool forced, int K, bool persistent, const void* fin, void* fout, const Chunk* chunks, int nchunks,
                        const int2* walls, int nwalls, const KParams* dp, const long long* offs, cudaStream_t s) {
-    return launch_batch_t<StF16S, kFast>(q, forced, K, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
+    return launch_batch_t<StF16S, kFast>(q, forced, K, persistent, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
 }
 }  // namespace mph

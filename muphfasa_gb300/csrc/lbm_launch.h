@@ -73,4 +73,10 @@ cudaError_t launch_step_f64x_pipe(int q, bool forced, const long long* fin, long
                                   const KParamsX& px, const KParams* pg, const long long* kbb, int* flag,
                                   int ctas, cudaStream_t s);
 
+// ---- monitor.cu (steady-state residual, FP64) ---------------------------
+// out2 = {sum |u - u_prev|^2, sum |u|^2} of the stored-population velocity;
+// u_prev (dim x ncell doubles) is overwritten with u.
+cudaError_t launch_residual(int prec, int q, const void* f, long long ncell, double* uprev, bool first, double* part,
+                            int nblocks, double* out2, cudaStream_t s);
+
 }  // namespace mph

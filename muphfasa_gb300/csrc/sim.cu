@@ -31,6 +31,8 @@ struct mph_sim {
     double* d_stage = nullptr;  // FP64 staging of one population (conversions)
     double* d_part = nullptr;   // reduction partials
     double* d_red = nullptr;    // reduction result
+    double* d_uprev = nullptr;  // velocity field saved by the last mph_residual (dim x N)
+    bool has_uprev = false;
     int red_blocks = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -149,6 +151,19 @@ void fixed_params(const mph_sim* s, KParamsX& px, long long* kbb) {
 
 }  // namespace
 
+namespace {
+// Velocity set of lattice Q into plain arrays (mph_lattice).
+template <int Q>
+void lattice_tables(int* c, double* w, int* opp) {
+    using L = Lat<Q>;
+    for (int n = 0; n < Q; ++n) {
+        if (c) { c[3 * n] = L::cx(n); c[3 * n + 1] = L::cy(n); c[3 * n + 2] = L::cz(n); }
+        if (w) w[n] = L::w(n);
+        if (opp) opp[n] = L::opp(n);
+    }
+}
+}  // namespace
+
 namespace mph {
 // KParams of one domain, shared with the batch (batch.cu).
 void build_params_public(const mph_desc& d, const mph_resolved_bc* tab, KParams& kp) { build_params(d, tab, kp); }
@@ -168,6 +183,7 @@ void free_all(mph_sim* s) {
     cudaFree(s->d_stage);
     cudaFree(s->d_part);
     cudaFree(s->d_red);
+    cudaFree(s->d_uprev);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -365,6 +381,7 @@ int mph_set_f(mph_sim* s, const double* f) {
     int rc = upload(s, f);
     if (rc) return rc;
     s->has_state = true;
+    s->has_uprev = false;
     return sync(s, "mph_set_f");
 }
 
@@ -389,6 +406,7 @@ int mph_init_fields(mph_sim* s, double* rho, double* u) {
         MPH_CK(cudaMemcpyAsync(u, s->d_u, sizeof(double) * s->d.dim * N, cudaMemcpyDeviceToHost, s->stream), "init download u");
     }
     s->has_state = true;
+    s->has_uprev = false;
     s->time = 0.0;
     return sync(s, "mph_init_fields");
 }
@@ -435,6 +453,34 @@ int mph_reduce(mph_sim* s, double* out) {
            "reduce kernel");
     MPH_CK(cudaMemcpyAsync(out, s->d_red, sizeof(double) * 4, cudaMemcpyDeviceToHost, s->stream), "download sums");
     return sync(s, "mph_reduce");
+}
+
+int mph_residual(mph_sim* s, double* out) {
+    if (!s || !out) return fail(MPH_ERR_ARG, "mph_residual: NULL argument");
+    if (!s->has_state) return fail(MPH_ERR_STATE, "mph_residual: no populations yet");
+    if (!s->d_uprev)
+        MPH_CK(cudaMalloc(&s->d_uprev, sizeof(double) * s->d.dim * s->kp.ncell), "cudaMalloc(residual field)");
+    MPH_CK(launch_residual(s->d.precision, s->d.q, s->fa, s->kp.ncell, s->d_uprev, !s->has_uprev, s->d_part,
+                           s->red_blocks, s->d_red, s->stream),
+           "residual kernel");
+    double sums[2];
+    MPH_CK(cudaMemcpyAsync(sums, s->d_red, sizeof(sums), cudaMemcpyDeviceToHost, s->stream), "download residual");
+    int rc = sync(s, "mph_residual");
+    if (rc) return rc;
+    out[1] = std::sqrt(sums[1]);
+    out[0] = s->has_uprev ? (sums[1] > 0.0 ? std::sqrt(sums[0] / sums[1]) : (sums[0] > 0.0 ? HUGE_VAL : 0.0)) : HUGE_VAL;
+    s->has_uprev = true;
+    return MPH_OK;
+}
+
+int mph_lattice(int q, int* c, double* w, int* opp) {
+    switch (q) {
+        case 9: lattice_tables<9>(c, w, opp); return MPH_OK;
+        case 15: lattice_tables<15>(c, w, opp); return MPH_OK;
+        case 19: lattice_tables<19>(c, w, opp); return MPH_OK;
+        case 27: lattice_tables<27>(c, w, opp); return MPH_OK;
+    }
+    return fail(MPH_ERR_ARG, "mph_lattice: q must be 9, 15, 19 or 27");
 }
 
 int mph_time(const mph_sim* s, double* t) {

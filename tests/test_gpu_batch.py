@@ -38,7 +38,7 @@ def test_batch_domains_equal_single_handles(precision, mph):
         rb, ub = batch.moments(i)
         rs, us = s.update_macroscopic()
         assert np.array_equal(rb, rs) and np.array_equal(ub, us)
-    total, kcells, nchunks = batch.info()
+    total, kcells, nchunks, _ = batch.info()
     assert total == sum(batch.ncells) and kcells in (1, 2, 4) and nchunks > 0
 
 
@@ -81,6 +81,28 @@ def test_looped_launches_equal_batched(precision, mph):
     b.advance_looped_timed(10)
     for i in range(len(descs)):
         assert np.array_equal(a.f(i), b.f(i))
+
+
+@pytest.mark.parametrize("cand", range(6))
+@pytest.mark.parametrize("precision", ["f32", "f16s"])
+def test_every_launch_candidate_equals_single_handles(cand, precision, mph, monkeypatch):
+    """Each autotuner candidate (K = 1, 2, 4 cells per thread; one block per
+    chunk or a persistent grid) gives the single-domain bits."""
+    if precision == "f16s" and cand % 3 == 0:
+        pytest.skip("16-bit storage takes cells in pairs")
+    monkeypatch.setenv("MPH_BATCH_CANDIDATE", str(cand))
+    descs = mph.cavity_batch_descs(9, seed=4, side=(16, 70), precision=precision)
+    b = mph.Batch(descs)
+    singles = [mph.Simulation(d) for d in descs]
+    for i, s in enumerate(singles):
+        b.initialize(i)
+        s.initialize()
+    b.advance(13)
+    total, kcells, nchunks, persistent = b.info()
+    assert kcells == (1, 2, 4)[cand % 3] and persistent == (cand >= 3)
+    for i, s in enumerate(singles):
+        s.advance(13)
+        assert np.array_equal(b.f(i), s.f()), i
 
 
 def test_cavity_ensemble_draw(mph):
