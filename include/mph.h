@@ -152,6 +152,14 @@ int mph_update_macroscopic(mph_sim* sim, double* rho, double* u);
 /* FP64 sums of the stored populations: out[0] = sum f (mass),
  * out[1..3] = sum c f (momentum). */
 int mph_reduce(mph_sim* sim, double* out);
+/* Interior obstacles (no counterpart in the reference; the reference's
+ * embedded-boundary geometry is an unimplemented stub).  mask[cell] != 0
+ * marks a solid cell (valid cells, x fastest); NULL removes all obstacles.
+ * Rule: a population whose upstream cell x - c_n is solid takes the cell's
+ * own opposite population (the BounceBack rule of BounceBack.H:36-63 with
+ * U = 0 at the obstacle face); solid cells hold the rest state f = w.  Adds
+ * one byte per cell of traffic.  Not available with MPH_F64X_KERNEL=pipe. */
+int mph_set_obstacles(mph_sim* sim, const unsigned char* mask);
 /* Steady-state residual (no counterpart in the reference), FP64 on the GPU:
  * with u = (sum c f) / (sum f) of the stored populations,
  *   out[0] = ||u - u_prev||_2 / ||u||_2, out[1] = ||u||_2,
@@ -224,6 +232,8 @@ int mph_batch_advance_timed(mph_batch* b, int nsteps, float* ms);
 int mph_batch_advance_looped_timed(mph_batch* b, int nsteps, float* ms);
 int mph_batch_get_f(mph_batch* b, int domain, double* f);
 int mph_batch_moments(mph_batch* b, int domain, double* rho, double* u);
+/* Obstacles of one batch domain, as mph_set_obstacles. */
+int mph_batch_set_obstacles(mph_batch* b, int domain, const unsigned char* mask);
 /* Per-domain steady-state residual (as mph_residual): out[2 d] = relative
  * change of domain d's stored-population velocity since the previous call
  * (+inf on the first call after an init), out[2 d + 1] = ||u_d||_2. */

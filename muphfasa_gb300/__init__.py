@@ -41,7 +41,7 @@ EXPORTS = [
     "mph_periodic_fill_arr", "mph_bc_fill_arr", "mph_reduce_f64_noalloc", "mph_batch_create",
     "mph_batch_destroy", "mph_batch_init_fields", "mph_batch_advance", "mph_batch_advance_timed",
     "mph_batch_advance_looped_timed", "mph_batch_get_f", "mph_batch_moments", "mph_batch_info",
-    "mph_residual", "mph_batch_residual", "mph_lattice",
+    "mph_residual", "mph_batch_residual", "mph_lattice", "mph_set_obstacles", "mph_batch_set_obstacles",
 ]
 
 
@@ -106,6 +106,8 @@ def lib():
     L.mph_update_macroscopic.argtypes = [P, dp, dp]
     L.mph_reduce.argtypes = [P, dp]
     L.mph_residual.argtypes = [P, dp]
+    L.mph_set_obstacles.argtypes = [P, C.c_void_p]
+    L.mph_batch_set_obstacles.argtypes = [P, C.c_int, C.c_void_p]
     L.mph_lattice.argtypes = [C.c_int, C.POINTER(C.c_int), dp, C.POINTER(C.c_int)]
     L.mph_batch_residual.argtypes = [P, dp]
     L.mph_time.argtypes = [P, dp]
@@ -299,6 +301,17 @@ class Simulation:
         check(lib().mph_reduce(self._h, _dp(out)))
         return out
 
+    def set_obstacles(self, mask):
+        """Interior obstacles: mask of N cells (x fastest), nonzero = solid;
+        None removes them."""
+        if mask is None:
+            check(lib().mph_set_obstacles(self._h, None))
+            return
+        m = np.ascontiguousarray(np.asarray(mask, dtype=np.uint8).ravel())
+        if m.size != self.ncell:
+            raise ValueError(f"mask has {m.size} cells, the domain {self.ncell}")
+        check(lib().mph_set_obstacles(self._h, m.ctypes.data))
+
     def residual(self):
         """(||u - u_prev|| / ||u||, ||u||) of the stored-population velocity
         against the previous call (inf on the first call after an init)."""
@@ -372,6 +385,16 @@ class Batch:
         rho, u = np.empty(N), np.empty(dim * N)
         check(lib().mph_batch_moments(self._h, int(domain), _dp(rho), _dp(u)))
         return rho, u
+
+    def set_obstacles(self, domain, mask):
+        """Obstacles of one domain, as Simulation.set_obstacles."""
+        if mask is None:
+            check(lib().mph_batch_set_obstacles(self._h, int(domain), None))
+            return
+        m = np.ascontiguousarray(np.asarray(mask, dtype=np.uint8).ravel())
+        if m.size != self.ncells[domain]:
+            raise ValueError(f"mask has {m.size} cells, domain {domain} {self.ncells[domain]}")
+        check(lib().mph_batch_set_obstacles(self._h, int(domain), m.ctypes.data))
 
     def residual(self):
         """Per-domain (relative change, norm) arrays, as Simulation.residual."""

@@ -79,6 +79,7 @@ std::map<std::tuple<int, int, int, int>, int> g_tune;
 // Defined in sim.cu (shared with single domains).
 namespace mph {
 void build_params_public(const mph_desc& d, const mph_resolved_bc* tab, KParams& kp);
+void build_cls(const KParams& p, int q, const unsigned char* mask, unsigned char* cls);
 }
 
 struct mph_batch {
@@ -96,9 +97,13 @@ struct mph_batch {
     double* d_u = nullptr;
     long long max_cells = 0;
     std::vector<KParams> params_h;
-    // cells next to non-periodic faces {domain, cell}
+    // cells needing the boundary rules {domain, cell}
     int2* d_walls = nullptr;
     int nwalls = 0;
+    // obstacle classes per domain (host copies; empty = none) and on the device
+    std::vector<std::vector<unsigned char>> cls_h;
+    unsigned char* d_cls = nullptr;
+    std::vector<long long> coffs_h;  // cell offset of each domain
     // chunk lists per candidate K, and the index of each domain's first chunk
     Chunk* d_chunks[3] = {nullptr, nullptr, nullptr};
     int nchunks[3] = {0, 0, 0};
@@ -144,6 +149,7 @@ void free_batch(mph_batch* b) {
     cudaFree(b->d_rpart);
     cudaFree(b->d_rout);
     cudaFree(b->d_walls);
+    cudaFree(b->d_cls);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
@@ -177,26 +183,29 @@ int ensure_chunks(mph_batch* b, int ki) {
     return MPH_OK;
 }
 
-// The list of cells next to a non-periodic face (the boundary rules apply
-// to their pulls): whole rows on y / z faces, the row ends on x faces.
+// The list of cells whose pulls need the boundary rules: cells next to a
+// non-periodic face (whole rows on y / z faces, the row ends on x faces) and
+// obstacle cells with their fluid neighbours.
 int build_walls(mph_batch* b) {
     std::vector<int2> walls;
     for (int d = 0; d < b->ndom; ++d) {
         const KParams& p = b->params_h[d];
+        const unsigned char* cls = b->cls_h[d].empty() ? nullptr : b->cls_h[d].data();
         for (int z = 0; z < p.nz; ++z)
             for (int y = 0; y < p.ny; ++y) {
                 const int row = (z * p.ny + y) * p.nx;
                 const bool face = (!p.periodic[1] && (y == 0 || y == p.ny - 1)) ||
                                   (b->dim == 3 && !p.periodic[2] && (z == 0 || z == p.nz - 1));
-                if (face) {
-                    for (int x = 0; x < p.nx; ++x) walls.push_back(make_int2(d, row + x));
-                } else if (!p.periodic[0]) {
-                    walls.push_back(make_int2(d, row));
-                    if (p.nx > 1) walls.push_back(make_int2(d, row + p.nx - 1));
+                for (int x = 0; x < p.nx; ++x) {
+                    const bool edge = face || (!p.periodic[0] && (x == 0 || x == p.nx - 1)) ||
+                                      (cls && cls[row + x] != kFluid);
+                    if (edge) walls.push_back(make_int2(d, row + x));
                 }
             }
     }
     if (walls.size() > 0x7fffffffu) return fail(MPH_ERR_ARG, "batch: too many wall cells");
+    cudaFree(b->d_walls);
+    b->d_walls = nullptr;
     b->nwalls = (int)walls.size();
     if (walls.empty()) return MPH_OK;
     MPH_CK(cudaMalloc(&b->d_walls, sizeof(int2) * walls.size()), "batch wall list");
@@ -317,6 +326,7 @@ int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out) {
     if (elem_of(b->prec) == 0) { delete b; return fail(MPH_ERR_UNSUPPORTED, "mph_batch_create: precision not supported in a batch"); }
     b->descs.assign(descs, descs + ndomains);
     b->params_h.resize(ndomains);
+    b->cls_h.resize(ndomains);
     long long off = 0;
     for (int d = 0; d < ndomains; ++d) {
         mph_desc& ds = b->descs[d];
@@ -343,6 +353,7 @@ int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out) {
         build_params_public(ds, tab, b->params_h[d]);
         const long long cells = (long long)ds.n[0] * ds.n[1] * ds.n[2];
         b->offs_h.push_back(off);
+        b->coffs_h.push_back(b->total_cells);
         // Each domain starts on a 128-element boundary (>= 256 B): aligned
         // rows for every precision and the 32-bit pair accesses of the
         // 16-bit kernels in the per-domain (looped) launches.
@@ -492,17 +503,41 @@ int mph_batch_moments(mph_batch* b, int domain, double* rho, double* u) {
     return MPH_OK;
 }
 
+int mph_batch_set_obstacles(mph_batch* b, int domain, const unsigned char* mask) {
+    if (!b || domain < 0 || domain >= b->ndom) return fail(MPH_ERR_ARG, "mph_batch_set_obstacles: bad argument");
+    MPH_CK(cudaStreamSynchronize(b->stream), "mph_batch_set_obstacles");
+    KParams& p = b->params_h[domain];
+    if (!mask) {
+        b->cls_h[domain].clear();
+        p.cls = nullptr;
+    } else {
+        if (!b->d_cls) MPH_CK(cudaMalloc(&b->d_cls, b->total_cells), "batch obstacle classes");
+        auto& cls = b->cls_h[domain];
+        cls.assign(p.ncell, 0);
+        build_cls(p, b->q, mask, cls.data());
+        unsigned char* dst = b->d_cls + b->coffs_h[domain];
+        MPH_CK(cudaMemcpy(dst, cls.data(), p.ncell, cudaMemcpyHostToDevice), "batch obstacle classes");
+        p.cls = dst;
+    }
+    MPH_CK(cudaMemcpy(b->d_params + domain, &p, sizeof(KParams), cudaMemcpyHostToDevice), "batch parameters");
+    int rc = build_walls(b);
+    if (rc) return rc;
+    if (b->graph) {  // the captured steps name the old wall list
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+        b->graph_k = -1;
+    }
+    return MPH_OK;
+}
+
 int mph_batch_residual(mph_batch* b, double* out) {
     if (!b || !out) return fail(MPH_ERR_ARG, "mph_batch_residual: NULL argument");
     int rc = ensure_chunks(b, 0);  // K = 1 chunk list, independent of the tuned K
     if (rc) return rc;
     if (!b->d_uprev) {
-        std::vector<long long> coffs(b->ndom);
-        long long c = 0;
-        for (int d = 0; d < b->ndom; ++d) { coffs[d] = c; c += b->params_h[d].ncell; }
         MPH_CK(cudaMalloc(&b->d_uprev, sizeof(double) * b->dim * b->total_cells), "batch residual field");
         MPH_CK(cudaMalloc(&b->d_coffs, sizeof(long long) * b->ndom), "batch residual offsets");
-        MPH_CK(cudaMemcpy(b->d_coffs, coffs.data(), sizeof(long long) * b->ndom, cudaMemcpyHostToDevice),
+        MPH_CK(cudaMemcpy(b->d_coffs, b->coffs_h.data(), sizeof(long long) * b->ndom, cudaMemcpyHostToDevice),
                "batch residual offsets");
         MPH_CK(cudaMalloc(&b->d_rpart, sizeof(double) * 2 * b->nchunks[0]), "batch residual partials");
         MPH_CK(cudaMalloc(&b->d_rout, sizeof(double) * 2 * b->ndom), "batch residual sums");

@@ -71,7 +71,7 @@ __device__ __forceinline__ void pull_x(const KParams& p, const KParams* __restri
                                        const i64* __restrict__ fin, int x, int y, int z, long long c, i64* h) {
     using L = Lat<Q>;
     const Nbr o = neighbours<L::D>(p, x, y, z);
-    if (!o.wall) {
+    if (!o.wall && !(p.cls && p.cls[c] != kFluid)) {
         const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
 #pragma unroll
         for (int n = 0; n < Q; ++n) h[n] = __ldg(fin + ((unsigned)n * N + (unsigned)((int)ci + upstream<Q>(o, n))));
@@ -90,7 +90,11 @@ __device__ __forceinline__ void pull_x(const KParams& p, const KParams* __restri
             else if (gz >= p.nz) { if (p.periodic[2]) gz -= p.nz; else k2 = 1; }
         }
         if ((k0 | k1 | k2) == 0) {
-            h[n] = __ldg(fin + n * p.ncell + ((long long)gz * p.ny + gy) * p.nx + gx);
+            const long long g = ((long long)gz * p.ny + gy) * p.nx + gx;
+            // Obstacle link: bounce-back with U = 0; w_opp = w_n, so in h = f / w
+            // it is the cell's own opposite value.
+            if (p.cls && p.cls[g] == kSolid) h[n] = __ldg(fin + L::opp(n) * p.ncell + c);
+            else h[n] = __ldg(fin + n * p.ncell + g);
         } else {
             const int cls = (k0 + 1) + 3 * (k1 + 1) + (L::D == 3 ? 9 * (k2 + 1) : 0);
             h[n] = boundary_value_x<Q>(pg, kbb, n, cls, fin, c);
@@ -297,12 +301,17 @@ __global__ void __launch_bounds__(256) k_step_x(const i64* __restrict__ fin, i64
     const int z = blockIdx.z;
     if (x >= p.nx || y >= p.ny) return;
     const long long c = ((long long)z * p.ny + y) * p.nx + x;
+    const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
+    if (p.cls && p.cls[c] == kSolid) {  // obstacle cell: rest state, h = f / w = 1
+#pragma unroll
+        for (int n = 0; n < Q; ++n) fout[(unsigned)n * N + ci] = 1LL << 56;
+        return;
+    }
     i64 h[Q];
     pull_x<Q>(p, pg, kbb, fin, x, y, z, c, h);
     int bad = 0;
     collide_x<Q, FORCED>(px, h, bad);
     if (bad) atomicOr(flag, 1);
-    const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
 #pragma unroll
     for (int n = 0; n < Q; ++n) fout[(unsigned)n * N + ci] = h[n];
 }

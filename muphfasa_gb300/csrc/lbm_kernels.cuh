@@ -32,6 +32,7 @@ namespace mph {
 
 enum { kBcMoving = 0, kBcNoSlip = 1, kBcInflow = 2, kBcOutflow = 3, kBcPressure = 4, kBcPeriodic = 5 };
 enum { kExact = 0, kFast = 1 };
+enum { kFluid = 0, kNearSolid = 1, kSolid = 2 };
 
 // Per-domain constants passed by value to every kernel.
 struct KParams {
@@ -49,6 +50,10 @@ struct KParams {
     // conversion runs on the FP64 pipe (2 per SM per clock on GB300).
     float omega_f, hF_f[3], F_f[3], gpref_f[27], gcF_f[27];
     float inv_nx_f, inv_ny_f;  // 1/nx, 1/ny (cell coordinates in the batch kernel)
+    // Interior obstacles (no counterpart in the reference): one class byte per
+    // cell, kFluid / kNearSolid (a fluid cell with a solid upstream cell) /
+    // kSolid; nullptr when the domain has none (no extra traffic then).
+    const unsigned char* cls;
 };
 
 // Parameters in the compute type R of a collide.
@@ -284,7 +289,11 @@ __device__ __forceinline__ void pull_edge(const KParams& p, const KParams* __res
             else if (gz >= p.nz) { if (p.periodic[2]) gz -= p.nz; else k2 = 1; }
         }
         if ((k0 | k1 | k2) == 0) {
-            f[n] = St::template ld<Q>(fin, n, ((long long)gz * p.ny + gy) * p.nx + gx, p.ncell);
+            const long long g = ((long long)gz * p.ny + gy) * p.nx + gx;
+            // Obstacle link: bounce-back with U = 0 (BounceBack.H:36-63 at an
+            // interior solid cell): the cell's own opposite population.
+            if (p.cls && p.cls[g] == kSolid) f[n] = St::template ld<Q>(fin, L::opp(n), c, p.ncell);
+            else f[n] = St::template ld<Q>(fin, n, g, p.ncell);
         } else {
             const int cls = (k0 + 1) + 3 * (k1 + 1) + (L::D == 3 ? 9 * (k2 + 1) : 0);
             f[n] = boundary_value<Q, St>(pg, n, cls, fin, c);
@@ -363,7 +372,7 @@ __device__ __forceinline__ void pull(const KParams& p, const KParams* __restrict
                                      typename St::R* f) {
     using L = Lat<Q>;
     const Nbr o = neighbours<L::D>(p, x, y, z);
-    if (!o.wall) {
+    if (!o.wall && !(p.cls && p.cls[c] != kFluid)) {
         const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
 #pragma unroll
         for (int n = 0; n < Q; ++n) {
@@ -677,7 +686,7 @@ __device__ __forceinline__ void pull_shift(const KParams& p, const KParams* __re
                                            float* g) {
     using L = Lat<Q>;
     const Nbr o = neighbours<L::D>(p, x, y, z);
-    if (!o.wall) {
+    if (!o.wall && !(p.cls && p.cls[c] != kFluid)) {
         const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
 #pragma unroll
         for (int n = 0; n < Q; ++n) g[n] = St::ldr1(fin, (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(o, n)));
@@ -696,6 +705,14 @@ __device__ __forceinline__ void step_cell(const KParams& p, const KParams* __res
     using R = typename St::R;
     const long long c = ((long long)z * p.ny + y) * p.nx + x;
     const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
+    if (p.cls && p.cls[c] == kSolid) {  // obstacle cell: rest state f = w
+#pragma unroll
+        for (int n = 0; n < Q; ++n) {
+            if constexpr (St::kShift) St::str1(fout, (unsigned)n * N + ci, 0.0f);
+            else St::template ste<Q>(fout, n, (unsigned)n * N + ci, (typename St::R)Lat<Q>::w(n));
+        }
+        return;
+    }
     if constexpr (St::kShift) {
         float g[Q];
         pull_shift<Q, St>(p, pg, fin, x, y, z, c, g);
@@ -741,6 +758,11 @@ __global__ void __launch_bounds__(256, 3) k_step_pair(const typename St::T* __re
     if (x >= p.nx || y >= p.ny) return;
     const long long c = ((long long)z * p.ny + y) * p.nx + x;
     const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
+    if (p.cls && (p.cls[c] | p.cls[c + 1]) != kFluid) {  // obstacle or its neighbour: one cell at a time
+        step_cell<Q, St, kFast, FORCED>(p, pg, fin, fout, x, y, z);
+        step_cell<Q, St, kFast, FORCED>(p, pg, fin, fout, x + 1, y, z);
+        return;
+    }
     const Nbr oa = neighbours<L::D>(p, x, y, z), ob = neighbours<L::D>(p, x + 1, y, z);
     float2 g[Q];
     if (!oa.wall && !ob.wall) {

@@ -8,6 +8,7 @@
 #include <cstring>
 #include <string>
 #include <utility>
+#include <vector>
 
 #include "lbm_launch.h"
 #include "mph_internal.h"
@@ -32,6 +33,7 @@ struct mph_sim {
     double* d_part = nullptr;   // reduction partials
     double* d_red = nullptr;    // reduction result
     double* d_uprev = nullptr;  // velocity field saved by the last mph_residual (dim x N)
+    unsigned char* d_cls = nullptr;  // obstacle class per cell (kp.cls), or null
     bool has_uprev = false;
     int red_blocks = 0;
     cudaStream_t stream = nullptr;
@@ -164,7 +166,45 @@ void lattice_tables(int* c, double* w, int* opp) {
 }
 }  // namespace
 
+namespace {
+// Class byte per cell from an obstacle mask: kSolid, kNearSolid (fluid with a
+// solid upstream cell x - c_n, periodic images included, cells beyond a
+// non-periodic face excluded) or kFluid.
+template <int Q>
+void classify(const KParams& p, const unsigned char* mask, unsigned char* cls) {
+    using L = Lat<Q>;
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                const long long c = ((long long)z * ny + y) * nx + x;
+                if (mask[c]) { cls[c] = kSolid; continue; }
+                unsigned char k = kFluid;
+                for (int n = 1; n < Q && k == kFluid; ++n) {
+                    int g[3] = {x - L::cx(n), y - L::cy(n), z - L::cz(n)};
+                    const int dims[3] = {nx, ny, nz};
+                    bool inside = true;
+                    for (int a = 0; a < 3; ++a) {
+                        if (g[a] >= 0 && g[a] < dims[a]) continue;
+                        if (!p.periodic[a]) { inside = false; break; }
+                        g[a] = g[a] < 0 ? g[a] + dims[a] : g[a] - dims[a];
+                    }
+                    if (inside && mask[((long long)g[2] * ny + g[1]) * nx + g[0]]) k = kNearSolid;
+                }
+                cls[c] = k;
+            }
+}
+}  // namespace
+
 namespace mph {
+void build_cls(const KParams& p, int q, const unsigned char* mask, unsigned char* cls) {
+    switch (q) {
+        case 9: classify<9>(p, mask, cls); break;
+        case 15: classify<15>(p, mask, cls); break;
+        case 19: classify<19>(p, mask, cls); break;
+        case 27: classify<27>(p, mask, cls); break;
+    }
+}
 // KParams of one domain, shared with the batch (batch.cu).
 void build_params_public(const mph_desc& d, const mph_resolved_bc* tab, KParams& kp) { build_params(d, tab, kp); }
 }  // namespace mph
@@ -184,6 +224,7 @@ void free_all(mph_sim* s) {
     cudaFree(s->d_part);
     cudaFree(s->d_red);
     cudaFree(s->d_uprev);
+    cudaFree(s->d_cls);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -453,6 +494,24 @@ int mph_reduce(mph_sim* s, double* out) {
            "reduce kernel");
     MPH_CK(cudaMemcpyAsync(out, s->d_red, sizeof(double) * 4, cudaMemcpyDeviceToHost, s->stream), "download sums");
     return sync(s, "mph_reduce");
+}
+
+int mph_set_obstacles(mph_sim* s, const unsigned char* mask) {
+    if (!s) return fail(MPH_ERR_ARG, "mph_set_obstacles: NULL handle");
+    if (s->pipe_ctas > 0)
+        return fail(MPH_ERR_UNSUPPORTED, "mph_set_obstacles: the pipelined fixed-point kernel has no obstacle path");
+    MPH_CK(cudaStreamSynchronize(s->stream), "mph_set_obstacles");
+    if (!mask) {
+        s->kp.cls = nullptr;
+    } else {
+        std::vector<unsigned char> cls(s->kp.ncell);
+        build_cls(s->kp, s->d.q, mask, cls.data());
+        if (!s->d_cls) MPH_CK(cudaMalloc(&s->d_cls, s->kp.ncell), "cudaMalloc(obstacle classes)");
+        MPH_CK(cudaMemcpy(s->d_cls, cls.data(), s->kp.ncell, cudaMemcpyHostToDevice), "upload obstacle classes");
+        s->kp.cls = s->d_cls;
+    }
+    MPH_CK(cudaMemcpy(s->d_kp, &s->kp, sizeof(KParams), cudaMemcpyHostToDevice), "upload parameters");
+    return MPH_OK;
 }
 
 int mph_residual(mph_sim* s, double* out) {

@@ -84,6 +84,9 @@ struct State {
     double rrho[27];
     double rU[27][3];
     std::vector<double> fin, fout;
+    // Interior obstacles (no counterpart in the reference): solid[cell] = 1,
+    // valid cells x fastest; empty when the domain has none.
+    std::vector<unsigned char> solid;
 
     long long at(int i, int j, int k) const {
         return ((long long)(k + gk) * gy + (j + 1)) * gx + (i + 1);
@@ -91,7 +94,34 @@ struct State {
     bool inDomain(int i, int j, int k) const {
         return i >= 0 && i < d.n[0] && j >= 0 && j < d.n[1] && k >= 0 && k < d.n[2];
     }
+    // Is the upstream cell (i, j, k) (possibly a periodic image) an obstacle?
+    // Cells beyond a non-periodic face belong to the face's boundary rule.
+    bool solidAt(int i, int j, int k) const {
+        if (solid.empty()) return false;
+        int g[3] = {i, j, k};
+        for (int dd = 0; dd < 3; ++dd) {
+            if (g[dd] >= 0 && g[dd] < d.n[dd]) continue;
+            if (!periodic[dd]) return false;
+            g[dd] = g[dd] < 0 ? g[dd] + d.n[dd] : g[dd] - d.n[dd];
+        }
+        return solid[((long long)g[2] * d.n[1] + g[1]) * d.n[0] + g[0]] != 0;
+    }
 };
+
+// Pull of cell (i, j, k) (streamCell, Streaming.H:20-35) with the interior
+// obstacle rule: a population whose upstream cell is solid takes the cell's
+// own opposite population, the BounceBack rule of BounceBack.H:36-63 with
+// U = 0 applied at an obstacle face.
+template <int D, int Q, class Lt>
+inline void pullCell(const State& s, const double* fin, int i, int j, int k, const long long* off, double* f) {
+    const long long c = s.at(i, j, k);
+    for (int n = 0; n < Q; ++n) {
+        if (s.solidAt(i - Lt::cx[n], j - Lt::cy[n], k - (D == 3 ? Lt::cz[n] : 0)))
+            f[n] = fin[(long long)Lt::opp[n] * s.gcells + c];
+        else
+            f[n] = fin[c + off[n]];
+    }
+}
 
 // ---------------------------------------------------------------------------
 // Per-cell arithmetic: Macroscopic.H:36-45,158-204,241-278, Equilibrium.H:28-57,
@@ -169,7 +199,15 @@ void pullCollide(State& s, int nthreads) {
             for (int i = 0; i < nx; ++i) {
                 const long long c = s.at(i, j, k);
                 double f[Q];
-                for (int n = 0; n < Q; ++n) f[n] = fin[c + off[n]];  // streamCell, Streaming.H:20-35
+                if (!s.solid.empty()) {
+                    if (s.solid[((long long)k * ny + j) * nx + i]) {  // obstacle: rest state
+                        for (int n = 0; n < Q; ++n) fout[(long long)n * G + c] = L::w[n];
+                        continue;
+                    }
+                    pullCell<D, Q, L>(s, fin, i, j, k, off, f);
+                } else {
+                    for (int n = 0; n < Q; ++n) f[n] = fin[c + off[n]];  // streamCell, Streaming.H:20-35
+                }
                 double rho = 0.;
                 for (int n = 0; n < Q; ++n) rho += f[n];
                 double u[3];
@@ -352,13 +390,15 @@ void moments(State& s, double* rho, double* u) {
     const long long N = (long long)s.d.n[0] * s.d.n[1] * s.d.n[2];
     const long long G = s.gcells;
     const double* fin = s.fin.data();
+    long long off[Q];
+    for (int n = 0; n < Q; ++n)
+        off[n] = (long long)n * G - ((long long)(D == 3 ? L::cz[n] : 0) * s.gy + L::cy[n]) * s.gx - L::cx[n];
     long long c = 0;
     for (int k = 0; k < s.d.n[2]; ++k)
         for (int j = 0; j < s.d.n[1]; ++j)
             for (int i = 0; i < s.d.n[0]; ++i, ++c) {
                 double f[Q];
-                for (int n = 0; n < Q; ++n)
-                    f[n] = fin[n * G + s.at(i - L::cx[n], j - L::cy[n], k - (D == 3 ? L::cz[n] : 0))];
+                pullCell<D, Q, L>(s, fin, i, j, k, off, f);
                 double r = 0.;
                 for (int n = 0; n < Q; ++n) r += f[n];
                 double uc[3];
@@ -617,6 +657,15 @@ int orc_init_fields(void* p, double* rho, double* u) {
 #define ORC_CALL(D, Q) initFields<D, Q>(s, rho, u)
     ORC_DISPATCH(s, ORC_CALL);
 #undef ORC_CALL
+    return 0;
+}
+
+int orc_set_obstacles(void* p, const unsigned char* mask) {
+    auto& s = *static_cast<State*>(p);
+    const long long N = (long long)s.d.n[0] * s.d.n[1] * s.d.n[2];
+    if (!mask) { s.solid.clear(); return 0; }
+    s.solid.assign(mask, mask + N);
+    for (auto& v : s.solid) v = v ? 1 : 0;
     return 0;
 }
 

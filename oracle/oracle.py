@@ -98,6 +98,8 @@ def _bind(lib):
     lib.orc_step.argtypes = [P, C.c_int, C.c_int]
     lib.orc_init_fields.argtypes = [P, dp, dp]
     lib.orc_moments.argtypes = [P, dp, dp]
+    if hasattr(lib, "orc_set_obstacles"):  # the restatement only (no reference counterpart)
+        lib.orc_set_obstacles.argtypes = [P, C.c_void_p]
     lib.orc_units.argtypes = [C.POINTER(OrcUnitsIn), C.POINTER(OrcUnitsOut), C.c_int, dp, dp,
                               C.c_int, dp, dp, C.c_int, dp, dp]
     lib.orc_resolve_bc.argtypes = [C.POINTER(OrcDesc), C.POINTER(C.c_int), dp, dp]
@@ -227,6 +229,16 @@ class OracleSim:
         if self.lib.orc_init_fields(self.h, _dptr(rho), _dptr(u)) != 0:
             raise RuntimeError("oracle init failed")
         return rho, u
+
+    def set_obstacles(self, mask):
+        """Interior obstacles (project-defined rule, restatement only): mask
+        is N booleans, x fastest; None removes them."""
+        if mask is None:
+            self.lib.orc_set_obstacles(self.h, None)
+            return
+        m = np.ascontiguousarray(np.asarray(mask, dtype=np.uint8).ravel())
+        assert m.size == self.N
+        self.lib.orc_set_obstacles(self.h, m.ctypes.data)
 
     def moments(self):
         rho = np.empty(self.N, dtype=np.float64)

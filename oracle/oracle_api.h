@@ -84,6 +84,11 @@ int orc_step(void* s, int nsteps, int nthreads);
 int orc_init_fields(void* s, double* rho, double* u);
 /* SimulationImpl::updateMacroscopic(): stream, then moments. */
 int orc_moments(void* s, double* rho, double* u);
+/* Interior obstacles (no counterpart in the reference): mask[cell] != 0 marks
+ * a solid cell (valid cells, x fastest); NULL removes them.  A population
+ * whose upstream cell is solid takes the cell's own opposite population
+ * (bounce-back with U = 0); solid cells hold f = w. */
+int orc_set_obstacles(void* s, const unsigned char* mask);
 
 #ifdef __cplusplus
 }

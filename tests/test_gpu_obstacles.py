@@ -1,0 +1,137 @@
+"""Interior obstacles (project-defined; the reference's embedded-boundary
+geometry is an unimplemented stub, so the oracle restatement carries the rule:
+a link from a solid cell bounces back with U = 0, solid cells hold f = w).
+FP64 bit-exact against the oracle, the fixed point within 1e-12, reduced
+precisions within their velocity tolerances, batches bit-identical to single
+handles."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL_LOWP = {"f32": 3e-4, "f16s": 3e-3, "bf16s": 1.5e-2}
+
+CASES = [
+    ("D2Q9", (40, 30), ["NoSlip", "NoSlip", "NoSlip", "MovingWall", "Periodic", "Periodic"], 1.4, None,
+     {3: [0.08, 0, 0]}, 300),
+    ("D2Q9", (48, 20), ["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic", "Periodic"], 1.6, (2e-5, 0, 0),
+     None, 300),
+    ("D3Q19", (24, 16, 12), ["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic", "Periodic"], 1.5,
+     (1e-5, 0, 0), None, 150),
+    ("D3Q15", (14, 12, 10), ["Inflow", "PressureOutlet", "Periodic", "Periodic", "NoSlip", "NoSlip"], 1.25, None,
+     {0: [0.02, 0, 0]}, 120),
+    ("D3Q27", (12, 10, 10), ["NoSlip", "NoSlip", "NoSlip", "MovingWall", "Periodic", "Periodic"], 1.3, None,
+     {3: [0.05, 0, 0.01]}, 100),
+]
+
+
+def _mask(n, seed):
+    """Seeded rectangular boxes, including one touching a face and, in the
+    periodic cases, one straddling the periodic seam."""
+    rng = np.random.default_rng(seed)
+    m = np.zeros(n[::-1], dtype=np.uint8)
+    for _ in range(3):
+        lo = [int(rng.integers(0, s - 2)) for s in n[::-1]]
+        hi = [min(s, a + int(rng.integers(2, max(3, s // 3)))) for a, s in zip(lo, n[::-1])]
+        m[tuple(slice(a, b) for a, b in zip(lo, hi))] = 1
+    m[(0,) * (len(n) - 1) + (slice(0, 3),)] = 1  # touches the lower faces
+    m[(-1,) * (len(n) - 1) + (slice(-2, None),)] = 1
+    return m.ravel()
+
+
+def _pair(mph, O, case, precision):
+    lat, n, faces, omega, force, U, steps = case
+    face_U = [[0.0] * 3 for _ in range(6)]
+    for k, v in (U or {}).items():
+        face_U[k] = v
+    cfg = O.Config(lat, n, omega=omega, faces=faces, face_U=face_U, force=force)
+    d = mph.make_desc(lat, n, omega, faces=faces, face_U=face_U, force=force, precision=precision)
+    return O.OracleSim(cfg, "port"), mph.Simulation(d), steps
+
+
+def _start(o, s, seed):
+    rng = np.random.default_rng(seed)
+    N, dim = o.N, o.cfg.dim
+    rho, u = 1 + 0.01 * rng.standard_normal(N), 0.02 * rng.standard_normal(dim * N)
+    o.init_fields(rho.copy(), u.copy())
+    s.initialize(rho.copy(), u.copy())
+
+
+@pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}_{c[1][0]}" for c in CASES])
+def test_obstacles_f64_bitwise_vs_oracle(case, mph, oracle_mod):
+    o, s, steps = _pair(mph, oracle_mod, case, "f64")
+    mask = _mask(case[1], 7)
+    _start(o, s, 3)
+    o.set_obstacles(mask)
+    s.set_obstacles(mask)
+    o.step(steps, nthreads=8)
+    s.advance(steps)
+    assert np.array_equal(o.get_f(), s.f())
+    mo, ms = o.moments(), s.update_macroscopic()
+    assert np.array_equal(mo[0], ms[0]) and np.array_equal(mo[1], ms[1])
+
+
+@pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}_{c[1][0]}" for c in CASES])
+def test_obstacles_f64x_within_1e12(case, mph, oracle_mod):
+    o, s, steps = _pair(mph, oracle_mod, case, "f64x")
+    mask = _mask(case[1], 8)
+    _start(o, s, 4)
+    o.set_obstacles(mask)
+    s.set_obstacles(mask)
+    o.step(steps, nthreads=8)
+    s.advance(steps)
+    ref = o.get_f()
+    assert float(np.max(np.abs(s.f() - ref) / np.abs(ref))) < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["f32", "f16s", "bf16s"])
+@pytest.mark.parametrize("case", CASES[:3], ids=[f"{c[0]}_{c[1][0]}" for c in CASES[:3]])
+def test_obstacles_reduced_precision(case, precision, mph, oracle_mod):
+    o, s, steps = _pair(mph, oracle_mod, case, precision)
+    mask = _mask(case[1], 9)
+    _start(o, s, 5)
+    o.set_obstacles(mask)
+    s.set_obstacles(mask)
+    o.step(steps, nthreads=8)
+    s.advance(steps)
+    uo, us = o.moments()[1], s.update_macroscopic()[1]
+    fluid = np.tile(mask == 0, o.cfg.dim)
+    err = np.linalg.norm((us - uo)[fluid]) / np.linalg.norm(uo[fluid])
+    assert err < TOL_LOWP[precision], err
+
+
+def test_removing_obstacles_restores_plain_step(mph):
+    d = mph.make_desc("D2Q9", (30, 22), 1.2, precision="f64")
+    a, b = mph.Simulation(d), mph.Simulation(d)
+    rng = np.random.default_rng(1)
+    rho, u = 1 + 0.01 * rng.standard_normal(660), 0.02 * rng.standard_normal(1320)
+    a.initialize(rho.copy(), u.copy())
+    b.initialize(rho.copy(), u.copy())
+    b.set_obstacles(_mask((30, 22), 2))
+    b.set_obstacles(None)
+    a.advance(20)
+    b.advance(20)
+    assert np.array_equal(a.f(), b.f())
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32", "f16s"])
+def test_batch_obstacles_equal_single_handles(precision, mph):
+    descs = mph.cavity_batch_descs(6, seed=11, side=(20, 60), precision=precision)
+    b = mph.Batch(descs)
+    singles = [mph.Simulation(d) for d in descs]
+    for i, s in enumerate(singles):
+        n = (descs[i].n[0], descs[i].n[1])
+        b.initialize(i)
+        s.initialize()
+        if i % 2 == 0:
+            m = _mask(n, 20 + i)
+            b.set_obstacles(i, m)
+            s.set_obstacles(m)
+    b.advance(7)
+    b.set_obstacles(1, _mask((descs[1].n[0], descs[1].n[1]), 40))  # changes the wall list between advances
+    singles[1].advance(7)
+    singles[1].set_obstacles(_mask((descs[1].n[0], descs[1].n[1]), 40))
+    b.advance(24)
+    for i, s in enumerate(singles):
+        s.advance(24 if i == 1 else 31)
+        assert np.array_equal(b.f(i), s.f()), i

@@ -146,3 +146,74 @@ def test_bc_priority_and_conflicts(oracle_mod):
     assert O.resolve_bc(bad)[0] != 0               # Outflow meets PressureOutlet at a corner
     two_moving = O.Config("D2Q9", (4, 4), omega=1.0, faces=["MovingWall", "NoSlip", "NoSlip", "MovingWall", "Periodic", "Periodic"])
     assert O.resolve_bc(two_moving)[0] != 0
+
+
+# ---------------------------------------------------------------------------
+# Interior obstacles (project-defined rule, no reference counterpart): a link
+# whose upstream cell is solid bounces back (U = 0); solid cells hold f = w.
+# ---------------------------------------------------------------------------
+def _random_state(sim, seed, amp=0.02):
+    rng = np.random.default_rng(seed)
+    N, dim = sim.N, sim.cfg.dim
+    sim.init_fields(1 + 0.01 * rng.standard_normal(N), amp * rng.standard_normal(dim * N))
+
+
+def test_obstacles_all_fluid_mask_is_identity(oracle_mod):
+    O = oracle_mod
+    cfg = O.Config("D2Q9", (20, 14), omega=1.3, faces=["NoSlip", "NoSlip", "NoSlip", "MovingWall", "Periodic", "Periodic"],
+                   face_U=[[0, 0, 0]] * 3 + [[0.05, 0, 0]] + [[0, 0, 0]] * 2)
+    a, b = O.OracleSim(cfg, "port"), O.OracleSim(cfg, "port")
+    _random_state(a, 1)
+    _random_state(b, 1)
+    b.set_obstacles(np.zeros(b.N, dtype=np.uint8))
+    a.step(40)
+    b.step(40)
+    assert np.array_equal(a.get_f(), b.get_f())
+
+
+@pytest.mark.parametrize("lat,n", [("D2Q9", (24, 20)), ("D3Q19", (12, 10, 8)), ("D3Q27", (10, 8, 8))])
+def test_obstacles_conserve_fluid_mass(lat, n, oracle_mod):
+    """Periodic box with a solid block: bounce-back at the block conserves the
+    mass of the fluid cells."""
+    O = oracle_mod
+    sim = O.OracleSim(O.Config(lat, n, omega=1.2), "port")
+    mask = np.zeros(n[::-1], dtype=np.uint8)
+    if len(n) == 2:
+        mask[5:11, 7:13] = 1
+    else:
+        mask[2:5, 3:6, 4:8] = 1
+    _random_state(sim, 2)
+    sim.set_obstacles(mask)
+    fluid = mask.ravel() == 0
+    q = sim.cfg.q
+    m0 = sim.get_f().reshape(q, -1)[:, fluid].sum()
+    sim.step(1)  # solid cells are set to the rest state on the first step
+    m1 = sim.get_f().reshape(q, -1)[:, fluid].sum()
+    s1 = sim.get_f().reshape(q, -1)[:, ~fluid]
+    sim.step(300)
+    m2 = sim.get_f().reshape(q, -1)[:, fluid].sum()
+    assert abs(m2 - m1) < 1e-12 * m1
+    assert abs(m1 - m0) < 1e-12 * m0
+    s2 = sim.get_f().reshape(q, -1)[:, ~fluid]
+    assert np.array_equal(s1, s2) and np.allclose(s2.sum(axis=0), 1.0, rtol=0, atol=1e-15)
+
+
+def test_obstacle_plane_blocks_forced_flow(oracle_mod):
+    """Periodic channel driven by a body force along x: a solid plane across
+    the channel stops the mean flow; without it the flow accelerates."""
+    O = oracle_mod
+    n = (32, 12)
+    cfg = O.Config("D2Q9", n, omega=1.0, force=(1e-5, 0.0, 0.0),
+                   faces=["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic", "Periodic"])
+    free, blocked = O.OracleSim(cfg, "port"), O.OracleSim(cfg, "port")
+    for s in (free, blocked):
+        s.init_fields(np.ones(s.N), np.zeros(2 * s.N))
+    mask = np.zeros(n[::-1], dtype=np.uint8)
+    mask[:, 16] = 1
+    blocked.set_obstacles(mask)
+    free.step(3000)
+    blocked.step(3000)
+    uf = free.moments()[1][: free.N].mean()
+    fluid = mask.ravel() == 0
+    ub = blocked.moments()[1][: blocked.N][fluid].mean()
+    assert uf > 5e-4 and abs(ub) < 1e-3 * uf, (uf, ub)
