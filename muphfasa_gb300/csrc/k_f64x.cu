@@ -66,12 +66,12 @@ __device__ __noinline__ i64 boundary_value_x(const KParams* __restrict__ pg, con
     return fin[o * N + c] + kbb[cls * 27 + n];
 }
 
-template <int Q>
+template <int Q, bool OBST>
 __device__ __forceinline__ void pull_x(const KParams& p, const KParams* __restrict__ pg, const i64* __restrict__ kbb,
                                        const i64* __restrict__ fin, int x, int y, int z, long long c, i64* h) {
     using L = Lat<Q>;
     const Nbr o = neighbours<L::D>(p, x, y, z);
-    if (!o.wall && !(p.cls && p.cls[c] != kFluid)) {
+    if (!o.wall && !(OBST && p.cls[c] != kFluid)) {
         const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
 #pragma unroll
         for (int n = 0; n < Q; ++n) h[n] = __ldg(fin + ((unsigned)n * N + (unsigned)((int)ci + upstream<Q>(o, n))));
@@ -93,7 +93,7 @@ __device__ __forceinline__ void pull_x(const KParams& p, const KParams* __restri
             const long long g = ((long long)gz * p.ny + gy) * p.nx + gx;
             // Obstacle link: bounce-back with U = 0; w_opp = w_n, so in h = f / w
             // it is the cell's own opposite value.
-            if (p.cls && p.cls[g] == kSolid) h[n] = __ldg(fin + L::opp(n) * p.ncell + c);
+            if (OBST && p.cls[g] == kSolid) h[n] = __ldg(fin + L::opp(n) * p.ncell + c);
             else h[n] = __ldg(fin + n * p.ncell + g);
         } else {
             const int cls = (k0 + 1) + 3 * (k1 + 1) + (L::D == 3 ? 9 * (k2 + 1) : 0);
@@ -292,7 +292,9 @@ __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) 
     bad |= dmag >= (1 << 29);
 }
 
-template <int Q, bool FORCED>
+// OBST: the domain has obstacles (p.cls set); the plain instantiation
+// carries no class-byte test.
+template <int Q, bool FORCED, bool OBST>
 __global__ void __launch_bounds__(256) k_step_x(const i64* __restrict__ fin, i64* __restrict__ fout, const KParams p,
                                                 const KParamsX px, const KParams* __restrict__ pg,
                                                 const i64* __restrict__ kbb, int* __restrict__ flag) {
@@ -302,13 +304,13 @@ __global__ void __launch_bounds__(256) k_step_x(const i64* __restrict__ fin, i64
     if (x >= p.nx || y >= p.ny) return;
     const long long c = ((long long)z * p.ny + y) * p.nx + x;
     const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
-    if (p.cls && p.cls[c] == kSolid) {  // obstacle cell: rest state, h = f / w = 1
+    if (OBST && p.cls[c] == kSolid) {  // obstacle cell: rest state, h = f / w = 1
 #pragma unroll
         for (int n = 0; n < Q; ++n) fout[(unsigned)n * N + ci] = 1LL << 56;
         return;
     }
     i64 h[Q];
-    pull_x<Q>(p, pg, kbb, fin, x, y, z, c, h);
+    pull_x<Q, OBST>(p, pg, kbb, fin, x, y, z, c, h);
     int bad = 0;
     collide_x<Q, FORCED>(px, h, bad);
     if (bad) atomicOr(flag, 1);
@@ -389,7 +391,7 @@ __global__ void __launch_bounds__(kPipeThreads) k_step_x_pipe(const i64* __restr
 #pragma unroll
                 for (int n = 0; n < Q; ++n) h[n] = b[n * kPipeThreads];
             } else {
-                pull_x<Q>(p, pg, kbb, fin, x, y, z, c, h);
+                pull_x<Q, false>(p, pg, kbb, fin, x, y, z, c, h);
             }
             collide_x<Q, FORCED>(px, h, bad);
             const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
@@ -466,8 +468,13 @@ cudaError_t launch_step_f64x(int q, bool forced, const long long* fin, long long
     step_shape(p, g, b);
 #define MPH_X_CASE(QQ)                                                                        \
     case QQ:                                                                                  \
-        if (forced) k_step_x<QQ, true><<<g, b, 0, s>>>(fin, fout, p, px, pg, kbb, flag);     \
-        else k_step_x<QQ, false><<<g, b, 0, s>>>(fin, fout, p, px, pg, kbb, flag);           \
+        if (p.cls) {                                                                          \
+            if (forced) k_step_x<QQ, true, true><<<g, b, 0, s>>>(fin, fout, p, px, pg, kbb, flag);  \
+            else k_step_x<QQ, false, true><<<g, b, 0, s>>>(fin, fout, p, px, pg, kbb, flag);        \
+        } else {                                                                              \
+            if (forced) k_step_x<QQ, true, false><<<g, b, 0, s>>>(fin, fout, p, px, pg, kbb, flag); \
+            else k_step_x<QQ, false, false><<<g, b, 0, s>>>(fin, fout, p, px, pg, kbb, flag);       \
+        }                                                                                     \
         return cudaGetLastError();
     switch (q) {
         MPH_X_CASE(9)
