@@ -150,6 +150,86 @@ def cpu_reference(n, steps, warmup, threads):
     return cells * steps / dt / 1e6, dt
 
 
+def tgv3d_fields(n, u0):
+    """3-D Taylor-Green vortex on a periodic n^3 box (project-defined, no
+    reference counterpart): x = 2 pi (i + 1/2) / n,
+    u = u0 (sin x cos y cos z, -cos x sin y cos z, 0),
+    rho = 1 + 3 u0^2 / 16 (cos 2x + cos 2y)(cos 2z + 2) (the incompressible
+    pressure over cs^2)."""
+    t = 2.0 * np.pi * (np.arange(n) + 0.5) / n
+    s, c = np.sin(t), np.cos(t)
+    c2 = np.cos(2 * t)
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij", sparse=True)
+    u = np.empty((3, n, n, n))
+    u[0] = u0 * s[x] * c[y] * c[z]
+    u[1] = -u0 * c[x] * s[y] * c[z]
+    u[2] = 0.0
+    rho = 1.0 + 3.0 * u0 * u0 / 16.0 * (c2[x] + c2[y]) * (c2[z] + 2.0)
+    return rho.reshape(-1), u.reshape(-1)
+
+
+def run_tgv3d(args):
+    """Precision study: D3Q27 TGV at n^3, tau 0.52, u0 0.05; the shifted FP16 and
+    BF16 storage against the FP64-accurate reference path, velocity L2 and
+    kinetic-energy errors and FP64 mass / momentum sums every `every` steps."""
+    import muphfasa_gb300 as m
+    m.set_device(0)
+    n, u0, tau = args.n, 0.05, 0.52
+    every, total = args.every, args.tgv_steps
+    rho, u = tgv3d_fields(n, u0)
+    N = n ** 3
+    names = [args.tgv_ref, "f16s", "bf16s"]
+    sims = {}
+    for p in names:
+        s = m.Simulation(m.make_desc("D3Q27", (n, n, n), 1.0 / tau, precision=p))
+        s.initialize(rho.copy(), u.copy())
+        sims[p] = s
+    del rho, u
+    mass0 = {p: sims[p].reduce()[0] for p in names}
+    ms = {p: 0.0 for p in names}
+    table = []
+    for step in range(every, total + 1, every):
+        vel = {}
+        row = {"step": step}
+        for p in names:
+            ms[p] += sims[p].advance_timed(every)
+            r, v = sims[p].update_macroscopic()
+            vel[p] = v
+            sums = sims[p].reduce()
+            row[p] = {"mass_drift": float((sums[0] - mass0[p]) / mass0[p]),
+                      "momentum": [float(x) for x in sums[1:4]]}
+        ref = vel[names[0]]
+        ke_ref = 0.5 * float(np.dot(ref, ref)) / N
+        nref = float(np.linalg.norm(ref))
+        row[names[0]]["ke"] = ke_ref
+        for p in names[1:]:
+            d = vel[p] - ref
+            ke = 0.5 * float(np.dot(vel[p], vel[p])) / N
+            row[p].update({"u_l2_rel": float(np.linalg.norm(d)) / nref, "ke_rel": abs(ke - ke_ref) / ke_ref})
+        del vel
+        table.append(row)
+        print(json.dumps({"progress": row}), file=sys.stderr, flush=True)
+    mlups = {p: N * total / (ms[p] / 1e3) / 1e6 for p in names}
+    bytes_cell = {"f64x": 432, "f64": 432, "f64_fast": 432, "f32": 216, "f16s": 108, "bf16s": 108}
+    peak, kind = peaks()
+    last = table[-1]
+    line = {"metric": "velocity L2 error vs FP64-accurate reference (and MLUPS)",
+            "value": last["f16s"]["u_l2_rel"], "unit": "relative", "n_gpus": 1, "steps": total, "warmup": 0,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f16/bf16 storage, f32 collide",
+            "data": "synthetic",
+            "config": {"workload": f"tgv3d_d3q27_{n}^3", "lattice": "D3Q27", "grid": [n] * 3, "tau": tau, "u0": u0,
+                       "reference_precision": names[0], "every": every,
+                       "init": "u = u0 (sin x cos y cos z, -cos x sin y cos z, 0), "
+                               "rho = 1 + 3 u0^2/16 (cos 2x + cos 2y)(cos 2z + 2)"},
+            "mlups": {p: round(v, 1) for p, v in mlups.items()},
+            "roofline_frac": {p: round(mlups[p] * 1e6 * bytes_cell[p] / 1e9 / peak, 4) for p in names},
+            "table": table}
+    print(json.dumps(line), flush=True)
+    for s in sims.values():
+        s.close()
+    return 0
+
+
 def run_reference(args):
     from muphfasa_gb300 import replicas
     rank, world, _ = replicas.rank_info()
@@ -224,8 +304,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--domains", type=int, default=512, help="domains of the batch512 workload")
     ap.add_argument("--probes", action="store_true", help="build and run bench_probes.cu (pipe rates, pull-copy)")
-    ap.add_argument("--workload", default="channel", choices=["channel", "batch512"],
-                    help="channel: the D3Q19 channel (headline); batch512: 512 uneven D2Q9 cavities")
+    ap.add_argument("--workload", default="channel", choices=["channel", "batch512", "tgv3d"],
+                    help="channel: the D3Q19 channel (headline); batch512: 512 uneven D2Q9 cavities; "
+                         "tgv3d: the D3Q27 precision study (use --n 384)")
+    ap.add_argument("--tgv-steps", type=int, default=10000, help="tgv3d: total steps")
+    ap.add_argument("--every", type=int, default=1000, help="tgv3d: steps between error samples")
+    ap.add_argument("--tgv-ref", default="f64x", choices=["f64x", "f64", "f64_fast"],
+                    help="tgv3d: reference precision (FP64 or the FP64-accurate fixed point)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -235,6 +320,8 @@ def main():
         subprocess.run(["nvcc", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-o", exe,
                         os.path.join(ROOT, "bench_probes.cu")], check=True)
         return subprocess.run([exe]).returncode
+    if args.workload == "tgv3d":
+        return run_tgv3d(args)
     if args.workload == "batch512":
         return run_batch(args)
 
