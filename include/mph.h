@@ -262,6 +262,50 @@ int mph_batch_info(const mph_batch* b, long long* total_cells, int* cells_per_th
  * slot a call reads is written earlier in the same call. */
 int mph_reduce_f64_noalloc(int dim, int q, const double* f, long long ncell, double* out, void* stream);
 
+/* ---- warm-start surrogate kernels ------------------------------------------
+ * No counterpart in the reference.  Building blocks of the convolutional
+ * neural operator that predicts steady (rho, u) fields (muphfasa_gb300/
+ * surrogate.py drives them).  Activations are NHWC [P][C] (P = batch x H x W),
+ * BF16 unless named float; a 3 x 3 conv's weights are Wt [Cout][9 Cin].  All
+ * work is queued on `stream` (NULL = default stream); every call returns a
+ * status code. */
+int mph_nn_alloc(long long bytes, void** out);
+int mph_nn_free(void* p);
+/* dir: 0 host -> device, 1 device -> host (both synchronous), 2 device -> device. */
+int mph_nn_copy(void* dst, const void* src, long long bytes, int dir, void* stream);
+int mph_nn_sync(void* stream);
+/* C (float, ldc) [+]= A . B on the tensor cores, BF16 operands, FP32
+ * accumulation: A(m, k) = ta ? A[k lda + m] : A[m lda + k],
+ * B(k, n) = tb ? B[k ldb + n] : B[n ldb + k]. */
+int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const void* B, long long ldb, int tb,
+                float* C, long long ldc, int accumulate, void* stream);
+int mph_nn_im2col3(const void* X, int Bn, int H, int W, int C, void* Xcol, void* stream);
+int mph_nn_col2im3(const float* dXcol, int Bn, int H, int W, int C, float* dX, void* stream);
+/* out = act(Y + bias) into columns [c_off, c_off + C) of rows of width ld_out
+ * (BF16 and/or float); act 1 = leaky ReLU (slope 0.1), 0 = identity. */
+int mph_nn_bias_act(const float* Y, const float* bias, long long P, int C, int act, void* out_bf16, float* out_f32,
+                    int ld_out, int c_off, void* stream);
+int mph_nn_act_bwd(const float* dOut, int ld_dout, int c_off, const void* act_out, int ld_act, int act_off,
+                   long long P, int C, int act, float* dPre, void* stream);
+int mph_nn_colsum(const float* X, long long P, int C, float* out, void* stream);
+int mph_nn_pool(const void* X, int Bn, int H, int W, int C, void* Y, void* stream);
+int mph_nn_pool_bwd(const float* dY, int Bn, int H, int W, int C, float* dX, void* stream);
+int mph_nn_up(const void* X, int Bn, int H, int W, int C, void* Y, int ldy, int c_off, void* stream);
+int mph_nn_up_bwd(const float* dY, int ldy, int c_off, int Bn, int H, int W, int C, float* dX, void* stream);
+/* Channel-slice copy; kind 0 BF16 -> BF16, 1 float -> float (optionally
+ * accumulating), 2 float -> BF16. */
+int mph_nn_slice(int kind, const void* src, int ld_src, int s_off, long long P, int C, void* dst, int ld_dst,
+                 int d_off, int accumulate, void* stream);
+/* Masked MSE: dpred = 2 w (pred - target) inv_count, part[b] = block sums of
+ * w (pred - target)^2 (nblocks blocks of 256 threads). */
+int mph_nn_mse(const float* pred, const float* target, const float* wgt, long long P, int C, float inv_count,
+               float* dpred, float* part, int nblocks, void* stream);
+int mph_nn_adam(float* w, float* m, float* v, const float* grad, long long n, float lr, float b1, float b2, float eps,
+                int t, float wd, void* stream);
+/* kind 0 float -> BF16, 1 BF16 -> float. */
+int mph_nn_cast(int kind, const void* x, long long n, void* y, void* stream);
+int mph_nn_fill(float* x, long long n, float v, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,496 @@
+// nn.cu -- kernels of the warm-start surrogate (no counterpart in the
+// reference): a small convolutional U-Net over NHWC activations, trained and
+// evaluated on the GPU with these kernels only.
+//
+//   * gemm_bf16: C (FP32) [+]= A . B with BF16 operands on the tensor cores
+//     (mma.sync m16n8k16, FP32 accumulation), 64 x 64 x 32 block tiles staged
+//     through shared memory; either operand may be stored transposed, so the
+//     forward pass (X_col . W), the data gradient (dY . W^T) and the weight
+//     gradient (X_col^T . dY) of a 3 x 3 convolution are the same kernel.
+//   * im2col / col2im for 3 x 3, pad 1 convolutions (col2im gathers, so the
+//     data gradient is deterministic), bias + leaky ReLU (forward, backward,
+//     bias gradient), 2 x 2 average pooling, nearest 2x upsampling, channel
+//     concatenation, masked MSE loss, Adam on FP32 master weights, casts, and
+//     device buffers for a host driver without its own allocator.
+//
+// Shapes: activations [P][C] with P = batch x H x W pixels (NHWC), weights of
+// a 3 x 3 conv as Wt [Cout][9 Cin] (k = (dy * 3 + dx) * Cin + ci contiguous).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "mph.h"
+#include "mph_internal.h"
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int BM = 64, BN = 64, BK = 32, KPAD = 8;
+
+__device__ __forceinline__ unsigned pack_bf16(bf16 lo, bf16 hi) {
+    return (unsigned)__bfloat16_as_ushort(lo) | ((unsigned)__bfloat16_as_ushort(hi) << 16);
+}
+
+__device__ __forceinline__ void mma_bf16(float* d, const unsigned* a, const unsigned* b) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+        "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// C[m][n] (ldc) = sum_k A(m, k) B(k, n) (+ C if accumulate).
+// A(m, k) = TA ? A[k * lda + m] : A[m * lda + k]
+// B(k, n) = TB ? B[k * ldb + n] : B[n * ldb + k]
+// 128 threads: warp w computes rows (w / 2) * 32 .. +32, cols (w % 2) * 32 .. +32.
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf16* __restrict__ A, long long lda,
+                                                   const bf16* __restrict__ B, long long ldb, float* __restrict__ C,
+                                                   long long ldc, int accumulate) {
+    __shared__ __align__(16) bf16 As[BM][BK + KPAD];
+    __shared__ __align__(16) bf16 Bs[BN][BK + KPAD];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int g = lane >> 2, t = lane & 3;
+    const long long m0 = (long long)blockIdx.y * BM, n0 = (long long)blockIdx.x * BN;
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
+    const bf16 zero = __float2bfloat16(0.f);
+    for (int k0 = 0; k0 < K; k0 += BK) {
+        // Stage A and B tiles (64 x 32 each: 2048 values, 16 per thread).
+#pragma unroll 4
+        for (int e = tid; e < BM * BK; e += 128) {
+            int r, c;
+            if (TA) { c = e / BM; r = e % BM; } else { r = e / BK; c = e % BK; }
+            const long long gm = m0 + r;
+            const int gk = k0 + c;
+            bf16 v = zero;
+            if (gm < M && gk < K) v = TA ? A[(long long)gk * lda + gm] : A[gm * lda + gk];
+            As[r][c] = v;
+        }
+#pragma unroll 4
+        for (int e = tid; e < BN * BK; e += 128) {
+            int r, c;
+            if (TB) { c = e / BN; r = e % BN; } else { r = e / BK; c = e % BK; }
+            const long long gn = n0 + r;
+            const int gk = k0 + c;
+            bf16 v = zero;
+            if (gn < N && gk < K) v = TB ? B[(long long)gk * ldb + gn] : B[gn * ldb + gk];
+            Bs[r][c] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; kk += 16) {
+            unsigned af[2][4], bfr[4][2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const int r = wm + i * 16 + g;
+                af[i][0] = *reinterpret_cast<const unsigned*>(&As[r][kk + 2 * t]);
+                af[i][1] = *reinterpret_cast<const unsigned*>(&As[r + 8][kk + 2 * t]);
+                af[i][2] = *reinterpret_cast<const unsigned*>(&As[r][kk + 2 * t + 8]);
+                af[i][3] = *reinterpret_cast<const unsigned*>(&As[r + 8][kk + 2 * t + 8]);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int cidx = wn + j * 8 + g;
+                bfr[j][0] = *reinterpret_cast<const unsigned*>(&Bs[cidx][kk + 2 * t]);
+                bfr[j][1] = *reinterpret_cast<const unsigned*>(&Bs[cidx][kk + 2 * t + 8]);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bfr[j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const long long row = m0 + wm + i * 16 + g + (r >= 2 ? 8 : 0);
+                const long long col = n0 + wn + j * 8 + 2 * t + (r & 1);
+                if (row < M && col < N) {
+                    float* p = C + row * ldc + col;
+                    *p = accumulate ? *p + acc[i][j][r] : acc[i][j][r];
+                }
+            }
+}
+
+// ---- convolution data movement --------------------------------------------
+// Xcol[p][(dy * 3 + dx) * C + c] = X[b][y + dy - 1][x + dx - 1][c] (0 outside).
+__global__ void k_im2col3(const bf16* __restrict__ X, int Bn, int H, int W, int C, bf16* __restrict__ Xcol) {
+    const long long total = (long long)Bn * H * W * 9 * C;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long r = i / C;
+        const int tap = (int)(r % 9);
+        const long long p = r / 9;
+        const int x = (int)(p % W), y = (int)((p / W) % H);
+        const long long b = p / ((long long)W * H);
+        const int sy = y + tap / 3 - 1, sx = x + tap % 3 - 1;
+        bf16 v = __float2bfloat16(0.f);
+        if (sy >= 0 && sy < H && sx >= 0 && sx < W) v = X[((b * H + sy) * W + sx) * C + c];
+        Xcol[i] = v;
+    }
+}
+
+// dX[b][y][x][c] = sum over taps of dXcol at the pixel that read (y, x).
+__global__ void k_col2im3(const float* __restrict__ dXcol, int Bn, int H, int W, int C, float* __restrict__ dX) {
+    const long long total = (long long)Bn * H * W * C;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        const int x = (int)(p % W), y = (int)((p / W) % H);
+        const long long b = p / ((long long)W * H);
+        float s = 0.f;
+#pragma unroll
+        for (int tap = 0; tap < 9; ++tap) {
+            const int oy = y - (tap / 3 - 1), ox = x - (tap % 3 - 1);  // output pixel whose tap read (y, x)
+            if (oy >= 0 && oy < H && ox >= 0 && ox < W)
+                s += dXcol[(((b * H + oy) * W + ox) * 9 + tap) * (long long)C + c];
+        }
+        dX[i] = s;
+    }
+}
+
+// out[p][c] = leaky(Y[p][c] + bias[c]) as BF16 into a channel slice of width
+// ld_out starting at column c_off; leaky slope 0.1 (act = 1), identity (0).
+__global__ void k_bias_act(const float* __restrict__ Y, const float* __restrict__ bias, long long P, int C, int act,
+                           bf16* __restrict__ out_bf, float* __restrict__ out_f, int ld_out, int c_off) {
+    const long long total = P * C;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        float v = Y[i] + bias[c];
+        if (act && v < 0.f) v *= 0.1f;
+        if (out_bf) out_bf[p * ld_out + c_off + c] = __float2bfloat16(v);
+        if (out_f) out_f[p * ld_out + c_off + c] = v;
+    }
+}
+
+// dPre = dOut * leaky'(pre), reading the sign from the stored activation.
+__global__ void k_act_bwd(const float* __restrict__ dOut, int ld_dout, int c_off, const bf16* __restrict__ act_out,
+                          int ld_act, int act_off, long long P, int C, int act, float* __restrict__ dPre) {
+    const long long total = P * C;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        float d = dOut[p * ld_dout + c_off + c];
+        if (act && __bfloat162float(act_out[p * ld_act + act_off + c]) < 0.f) d *= 0.1f;
+        dPre[i] = d;
+    }
+}
+
+// db[c] = sum_p dPre[p][c]: one block per channel group, fixed order.
+__global__ void k_colsum(const float* __restrict__ X, long long P, int C, float* __restrict__ out) {
+    const int c = blockIdx.x;
+    float s = 0.f;
+    for (long long p = threadIdx.x; p < P; p += blockDim.x) s += X[p * C + c];
+    __shared__ float sh[256];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[c] = sh[0];
+}
+
+__global__ void k_pool_fwd(const bf16* __restrict__ X, int Bn, int H, int W, int C, bf16* __restrict__ Y) {
+    const int Ho = H / 2, Wo = W / 2;
+    const long long total = (long long)Bn * Ho * Wo * C;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho);
+        const long long b = p / ((long long)Wo * Ho);
+        const bf16* s = X + ((b * H + 2 * y) * W + 2 * x) * C + c;
+        const float v = __bfloat162float(s[0]) + __bfloat162float(s[C]) + __bfloat162float(s[(long long)W * C]) +
+                        __bfloat162float(s[(long long)W * C + C]);
+        Y[i] = __float2bfloat16(0.25f * v);
+    }
+}
+
+__global__ void k_pool_bwd(const float* __restrict__ dY, int Bn, int H, int W, int C, float* __restrict__ dX) {
+    const long long total = (long long)Bn * H * W * C;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        const int x = (int)(p % W), y = (int)((p / W) % H);
+        const long long b = p / ((long long)W * H);
+        dX[i] = 0.25f * dY[((b * (H / 2) + y / 2) * (W / 2) + x / 2) * C + c];
+    }
+}
+
+// Nearest 2x upsampling of X [Bn][H][W][C] into a channel slice of Y
+// [Bn][2H][2W][ldy] at c_off.
+__global__ void k_up_fwd(const bf16* __restrict__ X, int Bn, int H, int W, int C, bf16* __restrict__ Y, int ldy,
+                         int c_off) {
+    const long long total = (long long)Bn * 4 * H * W * C;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        const int x = (int)(p % (2 * W)), y = (int)((p / (2 * W)) % (2 * H));
+        const long long b = p / (4LL * W * H);
+        Y[p * ldy + c_off + c] = X[((b * H + y / 2) * W + x / 2) * C + c];
+    }
+}
+
+__global__ void k_up_bwd(const float* __restrict__ dY, int ldy, int c_off, int Bn, int H, int W, int C,
+                         float* __restrict__ dX) {
+    const long long total = (long long)Bn * H * W * C;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        const int x = (int)(p % W), y = (int)((p / W) % H);
+        const long long b = p / ((long long)W * H);
+        float s = 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const long long po = (b * 2 * H + 2 * y + q / 2) * 2 * W + 2 * x + q % 2;
+            s += dY[po * ldy + c_off + c];
+        }
+        dX[i] = s;
+    }
+}
+
+// Copy a channel slice: dst[p][d_off + c] (ld_dst) = src[p][s_off + c] (ld_src), c < C.
+template <class T, class U>
+__global__ void k_slice(const T* __restrict__ src, int ld_src, int s_off, long long P, int C, U* __restrict__ dst,
+                        int ld_dst, int d_off, int accumulate) {
+    const long long total = P * C;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        const float v = (float)src[p * ld_src + s_off + c];
+        U* o = dst + p * ld_dst + d_off + c;
+        *o = (U)(accumulate ? (float)*o + v : v);
+    }
+}
+
+// Masked mean-squared error over C channels: weight[p] in {0, 1}.
+// dPred = 2 w (pred - target) / (sum w * C); partial sums of w (pred - target)^2.
+__global__ void k_mse(const float* __restrict__ pred, const float* __restrict__ target, const float* __restrict__ wgt,
+                      long long P, int C, float inv_count, float* __restrict__ dpred, float* __restrict__ part) {
+    float s = 0.f;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < P * C;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float w = wgt[i / C];
+        const float d = pred[i] - target[i];
+        s += w * d * d;
+        dpred[i] = 2.f * w * d * inv_count;
+    }
+    __shared__ float sh[256];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// Adam (decoupled from the BF16 copies, which mph_nn_cast refreshes) on FP32
+// master weights, with L2 weight decay wd.
+__global__ void k_adam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
+                       const float* __restrict__ grad, long long n, float lr, float b1, float b2, float eps, float c1,
+                       float c2, float wd) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float gi = grad[i] + wd * w[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        w[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+    }
+}
+
+template <class T, class U>
+__global__ void k_cast(const T* __restrict__ x, long long n, U* __restrict__ y) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        y[i] = (U)(float)x[i];
+}
+
+__global__ void k_fill(float* __restrict__ x, long long n, float v) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        x[i] = v;
+}
+
+int grid_for(long long n) {
+    long long b = (n + 255) / 256;
+    if (b > 152 * 32) b = 152 * 32;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+int ck(const char* what) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string("nn ") + what + ": " + cudaGetErrorString(e));
+    return MPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mph_nn_alloc(long long bytes, void** out) {
+    if (!out || bytes <= 0) return mph::fail(MPH_ERR_ARG, "mph_nn_alloc: bad argument");
+    const cudaError_t e = cudaMalloc(out, (size_t)bytes);
+    if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string("mph_nn_alloc: ") + cudaGetErrorString(e));
+    return MPH_OK;
+}
+
+int mph_nn_free(void* p) {
+    cudaFree(p);
+    return MPH_OK;
+}
+
+// dir: 0 = host -> device, 1 = device -> host, 2 = device -> device.
+int mph_nn_copy(void* dst, const void* src, long long bytes, int dir, void* stream) {
+    const cudaMemcpyKind k = dir == 0 ? cudaMemcpyHostToDevice : (dir == 1 ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice);
+    cudaError_t e = cudaMemcpyAsync(dst, src, (size_t)bytes, k, static_cast<cudaStream_t>(stream));
+    if (e == cudaSuccess && dir != 2) e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string("mph_nn_copy: ") + cudaGetErrorString(e));
+    return MPH_OK;
+}
+
+int mph_nn_sync(void* stream) {
+    const cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string("mph_nn_sync: ") + cudaGetErrorString(e));
+    return MPH_OK;
+}
+
+int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const void* B, long long ldb, int tb,
+                float* C, long long ldc, int accumulate, void* stream) {
+    if (M <= 0 || N <= 0 || K <= 0 || !A || !B || !C) return mph::fail(MPH_ERR_ARG, "mph_nn_gemm: bad argument");
+    const dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM));
+    if (grid.y > 65535) return mph::fail(MPH_ERR_ARG, "mph_nn_gemm: M too large for one launch");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    auto a = static_cast<const bf16*>(A);
+    auto b = static_cast<const bf16*>(B);
+    if (!ta && !tb) k_gemm_bf16<false, false><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
+    else if (!ta && tb) k_gemm_bf16<false, true><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
+    else if (ta && !tb) k_gemm_bf16<true, false><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
+    else k_gemm_bf16<true, true><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
+    return ck("gemm");
+}
+
+int mph_nn_im2col3(const void* X, int Bn, int H, int W, int C, void* Xcol, void* stream) {
+    const long long n = (long long)Bn * H * W * 9 * C;
+    k_im2col3<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const bf16*>(X), Bn, H, W, C,
+                                                                           static_cast<bf16*>(Xcol));
+    return ck("im2col");
+}
+
+int mph_nn_col2im3(const float* dXcol, int Bn, int H, int W, int C, float* dX, void* stream) {
+    const long long n = (long long)Bn * H * W * C;
+    k_col2im3<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(dXcol, Bn, H, W, C, dX);
+    return ck("col2im");
+}
+
+int mph_nn_bias_act(const float* Y, const float* bias, long long P, int C, int act, void* out_bf16, float* out_f32,
+                    int ld_out, int c_off, void* stream) {
+    k_bias_act<<<grid_for(P * C), 256, 0, static_cast<cudaStream_t>(stream)>>>(Y, bias, P, C, act,
+                                                                               static_cast<bf16*>(out_bf16), out_f32,
+                                                                               ld_out, c_off);
+    return ck("bias_act");
+}
+
+int mph_nn_act_bwd(const float* dOut, int ld_dout, int c_off, const void* act_out, int ld_act, int act_off,
+                   long long P, int C, int act, float* dPre, void* stream) {
+    k_act_bwd<<<grid_for(P * C), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        dOut, ld_dout, c_off, static_cast<const bf16*>(act_out), ld_act, act_off, P, C, act, dPre);
+    return ck("act_bwd");
+}
+
+int mph_nn_colsum(const float* X, long long P, int C, float* out, void* stream) {
+    k_colsum<<<C, 256, 0, static_cast<cudaStream_t>(stream)>>>(X, P, C, out);
+    return ck("colsum");
+}
+
+int mph_nn_pool(const void* X, int Bn, int H, int W, int C, void* Y, void* stream) {
+    const long long n = (long long)Bn * (H / 2) * (W / 2) * C;
+    k_pool_fwd<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const bf16*>(X), Bn, H, W, C,
+                                                                            static_cast<bf16*>(Y));
+    return ck("pool");
+}
+
+int mph_nn_pool_bwd(const float* dY, int Bn, int H, int W, int C, float* dX, void* stream) {
+    k_pool_bwd<<<grid_for((long long)Bn * H * W * C), 256, 0, static_cast<cudaStream_t>(stream)>>>(dY, Bn, H, W, C, dX);
+    return ck("pool_bwd");
+}
+
+int mph_nn_up(const void* X, int Bn, int H, int W, int C, void* Y, int ldy, int c_off, void* stream) {
+    k_up_fwd<<<grid_for(4LL * Bn * H * W * C), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(X), Bn, H, W, C, static_cast<bf16*>(Y), ldy, c_off);
+    return ck("up");
+}
+
+int mph_nn_up_bwd(const float* dY, int ldy, int c_off, int Bn, int H, int W, int C, float* dX, void* stream) {
+    k_up_bwd<<<grid_for((long long)Bn * H * W * C), 256, 0, static_cast<cudaStream_t>(stream)>>>(dY, ldy, c_off, Bn, H,
+                                                                                                  W, C, dX);
+    return ck("up_bwd");
+}
+
+// kind: 0 = bf16 -> bf16, 1 = f32 -> f32 (accumulate allowed), 2 = f32 -> bf16.
+int mph_nn_slice(int kind, const void* src, int ld_src, int s_off, long long P, int C, void* dst, int ld_dst,
+                 int d_off, int accumulate, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int g = grid_for(P * C);
+    if (kind == 0)
+        k_slice<bf16, bf16><<<g, 256, 0, s>>>(static_cast<const bf16*>(src), ld_src, s_off, P, C,
+                                              static_cast<bf16*>(dst), ld_dst, d_off, 0);
+    else if (kind == 1)
+        k_slice<float, float><<<g, 256, 0, s>>>(static_cast<const float*>(src), ld_src, s_off, P, C,
+                                                static_cast<float*>(dst), ld_dst, d_off, accumulate);
+    else
+        k_slice<float, bf16><<<g, 256, 0, s>>>(static_cast<const float*>(src), ld_src, s_off, P, C,
+                                               static_cast<bf16*>(dst), ld_dst, d_off, 0);
+    return ck("slice");
+}
+
+int mph_nn_mse(const float* pred, const float* target, const float* wgt, long long P, int C, float inv_count,
+               float* dpred, float* part, int nblocks, void* stream) {
+    k_mse<<<nblocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(pred, target, wgt, P, C, inv_count, dpred, part);
+    return ck("mse");
+}
+
+int mph_nn_adam(float* w, float* m, float* v, const float* grad, long long n, float lr, float b1, float b2, float eps,
+                int t, float wd, void* stream) {
+    const float c1 = 1.f / (1.f - powf(b1, (float)t)), c2 = 1.f / (1.f - powf(b2, (float)t));
+    k_adam<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(w, m, v, grad, n, lr, b1, b2, eps, c1, c2, wd);
+    return ck("adam");
+}
+
+// kind: 0 = f32 -> bf16, 1 = bf16 -> f32.
+int mph_nn_cast(int kind, const void* x, long long n, void* y, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (kind == 0) k_cast<float, bf16><<<grid_for(n), 256, 0, s>>>(static_cast<const float*>(x), n, static_cast<bf16*>(y));
+    else k_cast<bf16, float><<<grid_for(n), 256, 0, s>>>(static_cast<const bf16*>(x), n, static_cast<float*>(y));
+    return ck("cast");
+}
+
+int mph_nn_fill(float* x, long long n, float v, void* stream) {
+    k_fill<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, n, v);
+    return ck("fill");
+}
+
+}  // extern "C"

@@ -1,0 +1,125 @@
+"""The surrogate's GPU kernels against the CPU restatement (oracle/nn_oracle):
+the tensor-core GEMM in all four operand layouts, im2col / col2im adjointness,
+and the whole U-Net's prediction and every layer's weight and bias gradient;
+plus a training smoke check."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import nn_oracle as NO
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def S(mph):
+    from muphfasa_gb300 import surrogate
+    return surrogate
+
+
+def _bf16_dev(S, a):
+    a32 = np.ascontiguousarray(a, np.float32)
+    f = S._f32(a32.size)
+    f.upload(a32.reshape(-1))
+    b = S._bf(a32.size)
+    S.check(S._lib().mph_nn_cast(0, f.ptr, a32.size, b.ptr, None))
+    return b
+
+
+@pytest.mark.parametrize("ta,tb", [(0, 0), (0, 1), (1, 0), (1, 1)])
+def test_gemm_layouts(ta, tb, S):
+    rng = np.random.default_rng(ta * 2 + tb)
+    M, N, K = 77, 45, 83
+    A = NO.to_bf16(rng.standard_normal((M, K)).astype(np.float32))
+    B = NO.to_bf16(rng.standard_normal((K, N)).astype(np.float32))
+    a_store = A.T if ta else A          # [K][M] or [M][K]
+    b_store = B if tb else B.T          # [K][N] or [N][K]
+    da, db = _bf16_dev(S, a_store), _bf16_dev(S, b_store)
+    c = S._f32(M * N)
+    S.check(S._lib().mph_nn_gemm(M, N, K, da.ptr, M if ta else K, ta, db.ptr, N if tb else K, tb, c.ptr, N, 0, None))
+    got = c.download(M * N).reshape(M, N)
+    ref = A.astype(np.float64) @ B.astype(np.float64)
+    scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64)
+    assert np.all(np.abs(got - ref) <= 1e-5 * scale + 1e-6)
+    # accumulate mode adds to C
+    S.check(S._lib().mph_nn_gemm(M, N, K, da.ptr, M if ta else K, ta, db.ptr, N if tb else K, tb, c.ptr, N, 1, None))
+    got2 = c.download(M * N).reshape(M, N)
+    assert np.all(np.abs(got2 - 2 * ref) <= 2e-5 * scale + 2e-6)
+
+
+def test_im2col_col2im_adjoint(S):
+    rng = np.random.default_rng(3)
+    Bn, H, W, Cc = 2, 8, 16, 5
+    x = NO.to_bf16(rng.standard_normal((Bn, H, W, Cc)).astype(np.float32))
+    y = rng.standard_normal((Bn * H * W, 9 * Cc)).astype(np.float32)
+    dx_, col = _bf16_dev(S, x), S._bf(y.size)
+    S.check(S._lib().mph_nn_im2col3(dx_.ptr, Bn, H, W, Cc, col.ptr, None))
+    colf = S._f32(y.size)
+    S.check(S._lib().mph_nn_cast(1, col.ptr, y.size, colf.ptr, None))
+    got_col = colf.download(y.size).reshape(y.shape)
+    assert np.array_equal(got_col, NO.Net.im2col(x))
+    dy, dxo = S._f32(y.size), S._f32(x.size)
+    dy.upload(y.reshape(-1))
+    S.check(S._lib().mph_nn_col2im3(dy.ptr, Bn, H, W, Cc, dxo.ptr, None))
+    back = dxo.download(x.size).reshape(x.shape)
+    assert np.allclose(back, NO.Net.col2im(y.astype(np.float64), x.shape), rtol=1e-5, atol=1e-5)
+    assert np.isclose(float((got_col.astype(np.float64) * y).sum()), float((x.astype(np.float64) * back).sum()),
+                      rtol=1e-5)
+
+
+def test_unet_prediction_and_gradients_match_oracle(S):
+    rng = np.random.default_rng(5)
+    Bn, H, W = 2, 16, 16
+    net = S.UNet(seed=7)
+    # give the biases nonzero values so their gradients and the head matter
+    for name, layer in net.layers.items():
+        w, b = layer.get()
+        layer.set(w, 0.05 * rng.standard_normal(b.shape))
+    tr = S.Trainer(net, Bn, H, W)
+    x = rng.standard_normal((Bn, H, W, S.IN_CH)).astype(np.float32)
+    y = rng.standard_normal((Bn, H, W, S.OUT_CH)).astype(np.float32)
+    m = (rng.random((Bn, H, W)) > 0.25).astype(np.float32)
+    tr.load_batch(x, y, m)
+    pred = net.forward(tr.xb, Bn, H, W)
+    count = float(m.sum()) * S.OUT_CH
+    loss = tr.loss_grad(Bn, count)
+    net.backward(tr.dpred)
+    gpu_pred = pred.download(Bn * H * W * S.OUT_CH).reshape(Bn, H, W, S.OUT_CH)
+
+    params = net.state()
+    ref = NO.Net(params, bf16=True)
+    rp = ref.forward(x)
+    rloss, dpred = ref.loss(rp, y, m)
+    grads = ref.backward(dpred)
+    assert np.linalg.norm(gpu_pred - rp) <= 1e-2 * np.linalg.norm(rp)
+    assert abs(loss - rloss) <= 1e-2 * rloss
+    for name, layer in net.layers.items():
+        gw = layer.gw.download(layer.n).reshape(layer.cout, layer.K)
+        gb = layer.gb.download(layer.cout)
+        rw, rb = grads[name]
+        ew = np.linalg.norm(gw - rw) / np.linalg.norm(rw)
+        eb = np.linalg.norm(gb - rb) / max(np.linalg.norm(rb), 1e-30)
+        assert ew < 3e-2 and eb < 3e-2, (name, ew, eb)
+
+
+def test_training_reduces_loss(S):
+    rng = np.random.default_rng(2)
+    Bn, H, W = 4, 32, 32
+    yy, xx = np.meshgrid(np.linspace(0, 1, H), np.linspace(0, 1, W), indexing="ij")
+    xs, ys = [], []
+    for i in range(16):
+        a = rng.uniform(0.5, 1.5)
+        inp = np.zeros((H, W, S.IN_CH), np.float32)
+        inp[..., 0] = a
+        inp[..., 6], inp[..., 7] = xx, yy
+        xs.append(inp)
+        ys.append(np.stack([a * np.sin(np.pi * xx), a * yy, a * xx * yy], -1).astype(np.float32))
+    X, Y, M = np.stack(xs), np.stack(ys), np.ones((16, H, W), np.float32)
+    net = S.UNet(seed=1)
+    tr = S.Trainer(net, Bn, H, W)
+    losses = []
+    for it in range(60):
+        k = (it * Bn) % 16
+        losses.append(tr.train_step(X[k:k + Bn], Y[k:k + Bn], M[k:k + Bn], lr=1e-3))
+    assert np.mean(losses[-8:]) < 0.2 * np.mean(losses[:4])
