@@ -152,6 +152,12 @@ int mph_update_macroscopic(mph_sim* sim, double* rho, double* u);
 /* FP64 sums of the stored populations: out[0] = sum f (mass),
  * out[1..3] = sum c f (momentum). */
 int mph_reduce(mph_sim* sim, double* out);
+/* Warm start (no counterpart in the reference): like mph_init_fields for an
+ * unforced domain, plus the first-order Chapman-Enskog non-equilibrium part
+ * f_neq_n = -(tau w_n rho / cs2)(c_n c_n - cs2 I) : grad u, grad u from
+ * central differences of the given u (one-sided at non-periodic faces and
+ * obstacles).  rho and u are not modified. */
+int mph_init_fields_neq(mph_sim* sim, const double* rho, const double* u);
 /* Interior obstacles (no counterpart in the reference; the reference's
  * embedded-boundary geometry is an unimplemented stub).  mask[cell] != 0
  * marks a solid cell (valid cells, x fastest); NULL removes all obstacles.
@@ -232,6 +238,8 @@ int mph_batch_advance_timed(mph_batch* b, int nsteps, float* ms);
 int mph_batch_advance_looped_timed(mph_batch* b, int nsteps, float* ms);
 int mph_batch_get_f(mph_batch* b, int domain, double* f);
 int mph_batch_moments(mph_batch* b, int domain, double* rho, double* u);
+/* Warm start of one batch domain, as mph_init_fields_neq. */
+int mph_batch_init_fields_neq(mph_batch* b, int domain, const double* rho, const double* u);
 /* Obstacles of one batch domain, as mph_set_obstacles. */
 int mph_batch_set_obstacles(mph_batch* b, int domain, const unsigned char* mask);
 /* Per-domain steady-state residual (as mph_residual): out[2 d] = relative

@@ -42,7 +42,7 @@ EXPORTS = [
     "mph_batch_destroy", "mph_batch_init_fields", "mph_batch_advance", "mph_batch_advance_timed",
     "mph_batch_advance_looped_timed", "mph_batch_get_f", "mph_batch_moments", "mph_batch_info",
     "mph_residual", "mph_batch_residual", "mph_lattice", "mph_set_obstacles", "mph_batch_set_obstacles",
-    "mph_nn_alloc", "mph_nn_free", "mph_nn_copy", "mph_nn_sync", "mph_nn_gemm", "mph_nn_im2col3", "mph_nn_col2im3",
+    "mph_init_fields_neq", "mph_batch_init_fields_neq", "mph_nn_alloc", "mph_nn_free", "mph_nn_copy", "mph_nn_sync", "mph_nn_gemm", "mph_nn_im2col3", "mph_nn_col2im3",
     "mph_nn_bias_act", "mph_nn_act_bwd", "mph_nn_colsum", "mph_nn_pool", "mph_nn_pool_bwd", "mph_nn_up",
     "mph_nn_up_bwd", "mph_nn_slice", "mph_nn_mse", "mph_nn_adam", "mph_nn_cast", "mph_nn_fill",
 ]
@@ -109,6 +109,8 @@ def lib():
     L.mph_update_macroscopic.argtypes = [P, dp, dp]
     L.mph_reduce.argtypes = [P, dp]
     L.mph_residual.argtypes = [P, dp]
+    L.mph_init_fields_neq.argtypes = [P, dp, dp]
+    L.mph_batch_init_fields_neq.argtypes = [P, C.c_int, dp, dp]
     L.mph_set_obstacles.argtypes = [P, C.c_void_p]
     L.mph_batch_set_obstacles.argtypes = [P, C.c_int, C.c_void_p]
     L.mph_lattice.argtypes = [C.c_int, C.POINTER(C.c_int), dp, C.POINTER(C.c_int)]
@@ -262,6 +264,14 @@ class Simulation:
         self._rho, self._vel = rho, u
         return rho, u
 
+    def initialize_neq(self, rho, u):
+        """Warm start: f = feq(rho, u) + the first-order non-equilibrium part
+        from grad u (unforced domains)."""
+        rho = np.ascontiguousarray(rho, dtype=np.float64).reshape(-1)
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+        assert rho.size == self.ncell and u.size == self.dim * self.ncell
+        check(lib().mph_init_fields_neq(self._h, _dp(rho), _dp(u)))
+
     def advance(self, nsteps: int = 1):
         check(lib().mph_advance(self._h, int(nsteps)))
 
@@ -364,6 +374,14 @@ class Batch:
         u = np.zeros(d.dim * N) if u is None else np.ascontiguousarray(u, dtype=np.float64).reshape(-1).copy()
         check(lib().mph_batch_init_fields(self._h, int(domain), _dp(rho), _dp(u)))
         return rho, u
+
+    def initialize_neq(self, domain, rho, u):
+        """Warm start of one domain, as Simulation.initialize_neq."""
+        d, N = self.descs[domain], self.ncells[domain]
+        rho = np.ascontiguousarray(rho, dtype=np.float64).reshape(-1)
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+        assert rho.size == N and u.size == d.dim * N
+        check(lib().mph_batch_init_fields_neq(self._h, int(domain), _dp(rho), _dp(u)))
 
     def advance(self, nsteps=1):
         check(lib().mph_batch_advance(self._h, int(nsteps)))

@@ -417,6 +417,24 @@ int mph_batch_init_fields(mph_batch* b, int domain, double* rho, double* u) {
     return MPH_OK;
 }
 
+int mph_batch_init_fields_neq(mph_batch* b, int domain, const double* rho, const double* u) {
+    if (!b || !rho || !u || domain < 0 || domain >= b->ndom) return fail(MPH_ERR_ARG, "mph_batch_init_fields_neq: bad argument");
+    if (b->forced) return fail(MPH_ERR_UNSUPPORTED, "mph_batch_init_fields_neq: forced domains are not supported");
+    const mph_desc& ds = b->descs[domain];
+    const KParams& kp = b->params_h[domain];
+    const long long N = kp.ncell;
+    if (!b->d_rho) MPH_CK(cudaMalloc(&b->d_rho, sizeof(double) * b->max_cells), "batch rho");
+    if (!b->d_u) MPH_CK(cudaMalloc(&b->d_u, sizeof(double) * 3 * b->max_cells), "batch u");
+    MPH_CK(cudaMemcpyAsync(b->d_rho, rho, sizeof(double) * N, cudaMemcpyHostToDevice, b->stream), "batch init rho");
+    MPH_CK(cudaMemcpyAsync(b->d_u, u, sizeof(double) * ds.dim * N, cudaMemcpyHostToDevice, b->stream), "batch init u");
+    void* base = static_cast<char*>(b->fa) + elem_of(b->prec) * b->offs_h[domain];
+    MPH_CK(launch_init_neq(b->prec, b->q, base, b->d_rho, b->d_u, kp, b->stream), "batch init");
+    MPH_CK(cudaStreamSynchronize(b->stream), "batch init");
+    b->time = 0.0;
+    b->has_uprev = false;
+    return MPH_OK;
+}
+
 int mph_batch_advance(mph_batch* b, int nsteps) {
     if (!b || nsteps < 0) return fail(MPH_ERR_ARG, "mph_batch_advance: bad argument");
     int rc = advance_batch(b, nsteps);

@@ -227,6 +227,20 @@ cudaError_t launch_init(int prec, int q, bool forced, void* f, double* rho, doub
     });
 }
 
+cudaError_t launch_init_neq(int prec, int q, void* f, const double* rho, const double* u, const KParams& p,
+                            cudaStream_t s) {
+    dim3 g, b;
+    flat_shape(p.ncell, g, b);
+    return with_store(prec, [&](auto st) {
+        using St = decltype(st);
+        return with_q(q, [&](auto qc) {
+            constexpr int Q = decltype(qc)::value;
+            k_init_neq<Q, St><<<g, b, 0, s>>>(static_cast<typename St::T*>(f), rho, u, p);
+            return cudaGetLastError();
+        });
+    });
+}
+
 cudaError_t launch_reduce(int prec, int q, const void* f, long long ncell, double* part, int nblocks, double* out4,
                           cudaStream_t s) {
     cudaError_t e = with_store(prec, [&](auto st) {

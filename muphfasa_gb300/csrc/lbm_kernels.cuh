@@ -848,6 +848,66 @@ __global__ void __launch_bounds__(256) k_init(typename St::T* __restrict__ fout,
     }
 }
 
+// Warm start (no counterpart in the reference): f = feq(rho, u) + f_neq with
+// the first-order Chapman-Enskog non-equilibrium part of BGK,
+//   f_neq_n = -(tau w_n rho / cs2) (c_n c_n - cs2 I) : grad u,  cs2 = 1/3,
+// grad u by central differences, one-sided where a neighbour lies beyond a
+// non-periodic face or in an obstacle, zero with no fluid neighbour along an
+// axis.  Obstacle cells get the rest state.  Unforced domains.
+template <int Q, class St>
+__global__ void __launch_bounds__(256) k_init_neq(typename St::T* __restrict__ fout, const double* __restrict__ rho_in,
+                                                  const double* __restrict__ u_in, const KParams p) {
+    using L = Lat<Q>;
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= p.ncell) return;
+    const long long N = p.ncell;
+    if (p.cls && p.cls[c] == kSolid) {
+#pragma unroll
+        for (int n = 0; n < Q; ++n) St::template st<Q>(fout, n, c, N, (typename St::R)L::w(n));
+        return;
+    }
+    const int x = (int)(c % p.nx), y = (int)((c / p.nx) % p.ny), z = (int)(c / ((long long)p.nx * p.ny));
+    const double rho = rho_in[c];
+    double u[3] = {u_in[c], u_in[N + c], L::D == 3 ? u_in[2 * N + c] : 0.0};
+    double G[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // G[a][b] = d_a u_b
+    const int pos[3] = {x, y, z}, dims[3] = {p.nx, p.ny, p.nz};
+    const long long stride[3] = {1, p.nx, (long long)p.nx * p.ny};
+    for (int a = 0; a < L::D; ++a) {
+        long long nb[2];
+        bool ok[2];
+        for (int s = 0; s < 2; ++s) {
+            int q = pos[a] + (s ? 1 : -1);
+            ok[s] = true;
+            if (q < 0 || q >= dims[a]) {
+                if (p.periodic[a]) q = q < 0 ? q + dims[a] : q - dims[a];
+                else ok[s] = false;
+            }
+            nb[s] = c + (long long)(q - pos[a]) * stride[a];
+            if (ok[s] && p.cls && p.cls[nb[s]] == kSolid) ok[s] = false;
+        }
+        for (int b = 0; b < L::D; ++b) {
+            const double um = ok[0] ? u_in[b * N + nb[0]] : 0.0, up = ok[1] ? u_in[b * N + nb[1]] : 0.0;
+            if (ok[0] && ok[1]) G[a][b] = 0.5 * (up - um);
+            else if (ok[1]) G[a][b] = up - u[b];
+            else if (ok[0]) G[a][b] = u[b] - um;
+        }
+    }
+    const double tau = 1.0 / p.omega;
+    const double usq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+    const double divu = G[0][0] + G[1][1] + G[2][2];
+#pragma unroll
+    for (int n = 0; n < Q; ++n) {
+        const double cu = cdot<Q, double>(n, u);
+        const double feq = L::w(n) * rho * (1 + 3.0 * cu + 4.5 * cu * cu - 1.5 * usq);
+        const int cv[3] = {L::cx(n), L::cy(n), L::cz(n)};
+        double cc = 0.0;
+        for (int a = 0; a < L::D; ++a)
+            for (int b = 0; b < L::D; ++b) cc += cv[a] * cv[b] * G[a][b];
+        const double neq = -3.0 * tau * L::w(n) * rho * (cc - divu / 3.0);
+        St::template st<Q>(fout, n, c, N, (typename St::R)(feq + neq));
+    }
+}
+
 // FP64 sums of the stored populations: block partials (mass, jx, jy, jz)
 // into part[4*block]; k_reduce_final adds them in block order.
 template <int Q, class St>

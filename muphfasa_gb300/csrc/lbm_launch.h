@@ -36,6 +36,10 @@ cudaError_t launch_init(int prec, int q, bool forced, void* f, double* rho, doub
                         cudaStream_t s);
 cudaError_t launch_reduce(int prec, int q, const void* f, long long ncell, double* part, int nblocks, double* out4,
                           cudaStream_t s);
+// f = feq + first-order non-equilibrium part from central differences of u
+// (warm start, unforced domains).
+cudaError_t launch_init_neq(int prec, int q, void* f, const double* rho, const double* u, const KParams& p,
+                            cudaStream_t s);
 cudaError_t launch_convert(int prec, int q, bool to_store, void* store, double* f64, int n, long long ncell,
                            cudaStream_t s);
 

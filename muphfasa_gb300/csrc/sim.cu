@@ -452,6 +452,21 @@ int mph_init_fields(mph_sim* s, double* rho, double* u) {
     return sync(s, "mph_init_fields");
 }
 
+int mph_init_fields_neq(mph_sim* s, const double* rho, const double* u) {
+    if (!s || !rho || !u) return fail(MPH_ERR_ARG, "mph_init_fields_neq: NULL argument");
+    if (s->d.forced) return fail(MPH_ERR_UNSUPPORTED, "mph_init_fields_neq: forced domains are not supported");
+    int rc = ensure_macro(s);
+    if (rc) return rc;
+    const long long N = s->kp.ncell;
+    MPH_CK(cudaMemcpyAsync(s->d_rho, rho, sizeof(double) * N, cudaMemcpyHostToDevice, s->stream), "init upload rho");
+    MPH_CK(cudaMemcpyAsync(s->d_u, u, sizeof(double) * s->d.dim * N, cudaMemcpyHostToDevice, s->stream), "init upload u");
+    MPH_CK(launch_init_neq(s->d.precision, s->d.q, s->fa, s->d_rho, s->d_u, s->kp, s->stream), "init kernel");
+    s->has_state = true;
+    s->has_uprev = false;
+    s->time = 0.0;
+    return sync(s, "mph_init_fields_neq");
+}
+
 int mph_advance(mph_sim* s, int nsteps) {
     if (!s || nsteps < 0) return fail(MPH_ERR_ARG, "mph_advance: bad argument");
     if (!s->has_state) return fail(MPH_ERR_STATE, "mph_advance: no populations yet");

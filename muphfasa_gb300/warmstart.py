@@ -1,0 +1,157 @@
+"""Learned warm start of steady 2-D D2Q9 cases (no counterpart in the
+reference).
+
+Cases: lid-driven cavities (MovingWall lid at y = hi, NoSlip elsewhere) and
+channels (Inflow at x = lo, PressureOutlet at x = hi, NoSlip at y = lo, hi),
+n x n cells, Re uniform in [100, 2000] (Re = U n / nu), lid / inflow velocity
+U uniform in [0.02, 0.1], tau = 0.5 + 3 U n / Re, and 0-3 seeded solid boxes
+covering 5-20 % of the domain in total.  FP32 storage.
+
+The plain solver (a batch of all cases, one kernel per step) produces the
+steady fields: a case is steady when the relative change of its
+stored-population velocity over 100 steps drops below `tol`.  The surrogate
+(surrogate.UNet) learns (rho, u) from the geometry and parameters; a warm
+start initialises f = feq + f_neq(grad u) from its prediction
+(mph_init_fields_neq), and the same solver iterates to the same residual.
+"""
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+
+from . import Batch, make_desc, set_device
+
+RE = (100.0, 2000.0)
+U = (0.02, 0.1)
+
+
+def draw_cases(n_cases, seed, sizes=(128,), kinds=("cavity", "channel")):
+    rng = np.random.default_rng(seed)
+    cases = []
+    while len(cases) < n_cases:
+        n = int(sizes[len(cases) % len(sizes)])
+        kind = kinds[int(rng.integers(len(kinds)))]
+        re = float(rng.uniform(*RE))
+        u = float(rng.uniform(*U))
+        tau = 0.5 + 3.0 * u * n / re
+        nbox = int(rng.integers(0, 4))
+        frac = float(rng.uniform(0.05, 0.20)) if nbox else 0.0
+        boxes = []
+        if nbox:
+            area = frac * n * n / nbox
+            for _ in range(nbox):
+                aspect = math.exp(rng.uniform(math.log(0.4), math.log(2.5)))
+                w = int(max(2, min(n // 2, round(math.sqrt(area * aspect)))))
+                h = int(max(2, min(n // 2, round(area / w))))
+                # keep a fluid margin of 3 cells to the faces
+                x0 = int(rng.integers(3, max(4, n - w - 3)))
+                y0 = int(rng.integers(3, max(4, n - h - 3)))
+                boxes.append((x0, y0, w, h))
+        cases.append({"kind": kind, "n": n, "Re": re, "U": u, "tau": tau, "boxes": boxes})
+    return cases
+
+
+def case_mask(c):
+    n = c["n"]
+    m = np.zeros((n, n), np.uint8)  # [y][x]
+    for x0, y0, w, h in c["boxes"]:
+        m[y0:y0 + h, x0:x0 + w] = 1
+    return m
+
+
+def case_desc(c):
+    n, u = c["n"], c["U"]
+    U6 = [[0.0] * 3 for _ in range(6)]
+    if c["kind"] == "cavity":
+        faces = ["NoSlip", "NoSlip", "NoSlip", "MovingWall", "Periodic", "Periodic"]
+        U6[3] = [u, 0.0, 0.0]
+    else:
+        faces = ["Inflow", "PressureOutlet", "NoSlip", "NoSlip", "Periodic", "Periodic"]
+        U6[0] = [u, 0.0, 0.0]
+    return make_desc("D2Q9", (n, n), 1.0 / c["tau"], faces=faces, face_U=U6, precision="f32")
+
+
+def features(c):
+    """Network input [n][n][8]: solid, driving face, no-slip face, outlet
+    face, normalised log Re, U / 0.1, x, y."""
+    n = c["n"]
+    f = np.zeros((n, n, 8), np.float32)
+    f[..., 0] = case_mask(c)
+    if c["kind"] == "cavity":
+        f[-1, :, 1] = 1.0
+        f[0, :, 2] = f[:, 0, 2] = f[:, -1, 2] = 1.0
+    else:
+        f[:, 0, 1] = 1.0
+        f[0, :, 2] = f[-1, :, 2] = 1.0
+        f[:, -1, 3] = 1.0
+    f[..., 4] = (math.log(c["Re"]) - math.log(RE[0])) / (math.log(RE[1]) - math.log(RE[0]))
+    f[..., 5] = c["U"] / U[1]
+    t = (np.arange(n, dtype=np.float32) + 0.5) / n
+    f[..., 6] = t[None, :]
+    f[..., 7] = t[:, None]
+    return f
+
+
+def rho_scale(c):
+    """Scale of rho - 1: inertial (3 U^2) plus viscous (36 nu U / n)."""
+    nu = (c["tau"] - 0.5) / 3.0
+    return 3.0 * c["U"] ** 2 + 36.0 * nu * c["U"] / c["n"]
+
+
+def targets(c, rho, u):
+    n = c["n"]
+    t = np.empty((n, n, 3), np.float32)
+    t[..., 0] = ((rho.reshape(n, n) - 1.0) / rho_scale(c))
+    t[..., 1] = u[: n * n].reshape(n, n) / c["U"]
+    t[..., 2] = u[n * n:].reshape(n, n) / c["U"]
+    return t
+
+
+def fields_from_prediction(c, pred):
+    """(rho, u) in the solver's layout from a [n][n][3] prediction."""
+    n = c["n"]
+    solid = case_mask(c).reshape(-1).astype(bool)
+    rho = 1.0 + rho_scale(c) * pred[..., 0].astype(np.float64).reshape(-1)
+    u = np.concatenate([pred[..., 1].reshape(-1), pred[..., 2].reshape(-1)]).astype(np.float64) * c["U"]
+    rho[solid] = 1.0
+    u[: n * n][solid] = 0.0
+    u[n * n:][solid] = 0.0
+    return rho, u
+
+
+def solve(cases, init=None, max_steps=400_000, tol=1e-8, check_every=1000, k=100, log=None):
+    """Advance all cases together from rest (init None) or from
+    init[i] = (rho, u) (warm start), until each reaches the residual tol over
+    k steps.  Returns (steps per case or -1, final (rho, u) per case, seconds,
+    residual per case)."""
+    set_device(0)
+    b = Batch([case_desc(c) for c in cases])
+    for i, c in enumerate(cases):
+        b.set_obstacles(i, case_mask(c))
+        if init is None:
+            b.initialize(i)
+        else:
+            b.initialize_neq(i, *init[i])
+    steps = np.full(len(cases), -1, np.int64)
+    last = np.full(len(cases), np.inf)
+    t0 = time.perf_counter()
+    done = 0
+    while done < max_steps and np.any(steps == -1):
+        b.advance(check_every - k)
+        b.residual()
+        b.advance(k)
+        r, _ = b.residual()
+        done += check_every
+        bad = ~np.isfinite(r) & (done > check_every)
+        last = r
+        newly = (steps < 0) & (r < tol)
+        steps[newly] = done
+        steps[(steps < 0) & bad] = -2  # diverged
+        if log:
+            log(done, int(np.sum(steps > 0)), float(np.nanmedian(r)))
+    secs = time.perf_counter() - t0
+    out = [b.moments(i) for i in range(len(cases))]
+    b.close()
+    return steps, out, secs, last
