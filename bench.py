@@ -230,6 +230,85 @@ def run_tgv3d(args):
     return 0
 
 
+def run_warmstart(args):
+    """Learned warm start: the plain FP32 batch solver generates steady fields
+    of seeded cavity / channel cases, the U-Net is trained on them with the
+    library's BF16 tensor-core kernels, and held-out cases are solved to the
+    residual 1e-8 (FP64 storage: FP32 stalls near 1e-6) from rest and from
+    the surrogate's prediction (feq + f_neq)."""
+    import muphfasa_gb300 as m
+    from muphfasa_gb300 import warmstart as ws
+    m.set_device(0)
+    n = args.ws_n
+    log = lambda *a: print(json.dumps({"progress": a}), file=sys.stderr, flush=True)
+    train_cases = ws.draw_cases(args.ws_train, seed=101, sizes=(n,))
+    test_cases = ws.draw_cases(args.ws_test, seed=202, sizes=(n,))
+    t0 = time.perf_counter()
+    _, fields, gen_secs, last = ws.solve(train_cases, max_steps=args.ws_gen_steps, tol=0.0, precision="f32",
+                                         check_every=5000)
+    keep = [i for i, r in enumerate(last) if np.isfinite(r) and r < args.ws_keep]
+    X, Y, M = ws.dataset([train_cases[i] for i in keep], [fields[i] for i in keep])
+    log("generated", len(keep), len(train_cases), round(gen_secs, 1))
+    t1 = time.perf_counter()
+    net, hist = ws.train(X, Y, M, epochs=args.ws_epochs, batch=8, lr=args.ws_lr, log=lambda e, l: log("epoch", e, l))
+    train_secs = time.perf_counter() - t1
+    del X, Y, M
+    preds, pred_secs = ws.predict(net, test_cases)
+    sp, ref, secs_plain, rp = ws.solve(test_cases, None, max_steps=args.ws_max_steps, precision="f64_fast")
+    log("plain", int(np.sum(sp > 0)), round(secs_plain, 1))
+    sw, _, secs_warm, rw = ws.solve(test_cases, preds, max_steps=args.ws_max_steps, precision="f64_fast")
+    log("warm", int(np.sum(sw > 0)), round(secs_warm, 1))
+    both = (sp > 0) & (sw > 0)
+    errs = [ws.field_error(c, p, r) for c, p, r, ok in zip(test_cases, preds, ref, sp > 0) if ok]
+    # single-case wall time (one handle per case, FP64): rest vs predict + warm start
+    single = []
+    for c in [c for c, ok in zip(test_cases, both) if ok][: args.ws_single]:
+        row = {}
+        for mode in ("plain", "warm"):
+            tt = time.perf_counter()
+            s = m.Simulation(ws.case_desc(c, "f64_fast"))
+            s.set_obstacles(ws.case_mask(c))
+            if mode == "plain":
+                s.initialize()
+            else:
+                (pr,), _ = ws.predict(net, [c], batch=1)
+                s.initialize_neq(*pr)
+            steps, r = 0, np.inf
+            while steps < args.ws_max_steps and not r < 1e-8:
+                s.advance(900)
+                s.residual()
+                s.advance(100)
+                r, _ = s.residual()
+                steps += 1000
+            row[mode] = {"steps": steps, "seconds": round(time.perf_counter() - tt, 3)}
+            s.close()
+        single.append(row)
+    ratio = sp[both] / sw[both]
+    wall_single = [r["plain"]["seconds"] / r["warm"]["seconds"] for r in single]
+    line = {"metric": "steps and wall time to residual 1e-8, warm start vs start from rest",
+            "value": round(float(np.median(ratio)), 3) if ratio.size else None, "unit": "x (median over cases)",
+            "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "surrogate bf16 / f32 accumulate; solver f32 (data), f64 (judge)", "data": "synthetic",
+            "config": {"workload": f"warmstart_d2q9_{n}^2", "train_cases": len(train_cases), "kept": len(keep),
+                       "test_cases": len(test_cases), "epochs": args.ws_epochs, "gen_steps": args.ws_gen_steps,
+                       "params": net.n_params(), "Re": list(ws.RE), "U": list(ws.U)},
+            "steps_plain_median": float(np.median(sp[sp > 0])) if np.any(sp > 0) else None,
+            "steps_warm_median": float(np.median(sw[sw > 0])) if np.any(sw > 0) else None,
+            "steps_ratio_total": float(sp[both].sum() / sw[both].sum()) if np.any(both) else None,
+            "converged": {"plain": int(np.sum(sp > 0)), "warm": int(np.sum(sw > 0)), "both": int(np.sum(both)),
+                          "diverged_plain": int(np.sum(sp == -2))},
+            "surrogate_u_error": {"median": float(np.median(errs)) if errs else None,
+                                  "p90": float(np.percentile(errs, 90)) if errs else None},
+            "seconds": {"generate": round(gen_secs, 1), "train": round(train_secs, 1),
+                        "predict_all": round(pred_secs, 3), "batch_plain": round(secs_plain, 1),
+                        "batch_warm": round(secs_warm, 1)},
+            "single_case_wall": {"cases": single,
+                                 "median_ratio": float(np.median(wall_single)) if wall_single else None},
+            "train_loss": [round(h, 6) for h in hist]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_reference(args):
     from muphfasa_gb300 import replicas
     rank, world, _ = replicas.rank_info()
@@ -304,11 +383,20 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--domains", type=int, default=512, help="domains of the batch512 workload")
     ap.add_argument("--probes", action="store_true", help="build and run bench_probes.cu (pipe rates, pull-copy)")
-    ap.add_argument("--workload", default="channel", choices=["channel", "batch512", "tgv3d"],
+    ap.add_argument("--workload", default="channel", choices=["channel", "batch512", "tgv3d", "warmstart"],
                     help="channel: the D3Q19 channel (headline); batch512: 512 uneven D2Q9 cavities; "
                          "tgv3d: the D3Q27 precision study (use --n 384)")
     ap.add_argument("--tgv-steps", type=int, default=10000, help="tgv3d: total steps")
     ap.add_argument("--every", type=int, default=1000, help="tgv3d: steps between error samples")
+    ap.add_argument("--ws-n", type=int, default=128, help="warmstart: cells per side")
+    ap.add_argument("--ws-train", type=int, default=2000, help="warmstart: training cases")
+    ap.add_argument("--ws-test", type=int, default=200, help="warmstart: held-out cases")
+    ap.add_argument("--ws-epochs", type=int, default=30)
+    ap.add_argument("--ws-lr", type=float, default=2e-3)
+    ap.add_argument("--ws-gen-steps", type=int, default=150000, help="warmstart: FP32 steps per training field")
+    ap.add_argument("--ws-keep", type=float, default=1e-4, help="warmstart: keep fields with FP32 residual below")
+    ap.add_argument("--ws-max-steps", type=int, default=400000)
+    ap.add_argument("--ws-single", type=int, default=6, help="warmstart: cases timed on single handles")
     ap.add_argument("--tgv-ref", default="f64x", choices=["f64x", "f64", "f64_fast"],
                     help="tgv3d: reference precision (FP64 or the FP64-accurate fixed point)")
     args = ap.parse_args()
@@ -322,6 +410,8 @@ def main():
         return subprocess.run([exe]).returncode
     if args.workload == "tgv3d":
         return run_tgv3d(args)
+    if args.workload == "warmstart":
+        return run_warmstart(args)
     if args.workload == "batch512":
         return run_batch(args)
 

@@ -81,6 +81,9 @@ namespace mph {
 void build_params_public(const mph_desc& d, const mph_resolved_bc* tab, KParams& kp);
 void build_cls(const KParams& p, int q, const unsigned char* mask, unsigned char* cls);
 }
+namespace mph {
+double relative_change(double s0, double s1, bool has_prev);
+}
 
 struct mph_batch {
     int ndom = 0, q = 0, dim = 0, prec = 0;
@@ -571,7 +574,7 @@ int mph_batch_residual(mph_batch* b, double* out) {
     for (int d = 0; d < b->ndom; ++d) {
         const double s0 = sums[2 * d], s1 = sums[2 * d + 1];
         out[2 * d + 1] = std::sqrt(s1);
-        out[2 * d] = b->has_uprev ? (s1 > 0.0 ? std::sqrt(s0 / s1) : (s0 > 0.0 ? HUGE_VAL : 0.0)) : HUGE_VAL;
+        out[2 * d] = relative_change(s0, s1, b->has_uprev);
     }
     b->has_uprev = true;
     return MPH_OK;

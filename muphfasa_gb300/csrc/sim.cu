@@ -197,6 +197,16 @@ void classify(const KParams& p, const unsigned char* mask, unsigned char* cls) {
 }  // namespace
 
 namespace mph {
+// ||u - u_prev|| / ||u|| from the two FP64 sums; NaN when the field is not
+// finite (a diverged state never reads as converged), +inf before a previous
+// field exists, 0 for a field that is zero and unchanged.
+double relative_change(double s0, double s1, bool has_prev) {
+    if (!std::isfinite(s0) || !std::isfinite(s1)) return std::nan("");
+    if (!has_prev) return HUGE_VAL;
+    if (s1 > 0.0) return std::sqrt(s0 / s1);
+    return s0 > 0.0 ? HUGE_VAL : 0.0;
+}
+
 void build_cls(const KParams& p, int q, const unsigned char* mask, unsigned char* cls) {
     switch (q) {
         case 9: classify<9>(p, mask, cls); break;
@@ -542,7 +552,7 @@ int mph_residual(mph_sim* s, double* out) {
     int rc = sync(s, "mph_residual");
     if (rc) return rc;
     out[1] = std::sqrt(sums[1]);
-    out[0] = s->has_uprev ? (sums[1] > 0.0 ? std::sqrt(sums[0] / sums[1]) : (sums[0] > 0.0 ? HUGE_VAL : 0.0)) : HUGE_VAL;
+    out[0] = relative_change(sums[0], sums[1], s->has_uprev);
     s->has_uprev = true;
     return MPH_OK;
 }

@@ -61,7 +61,7 @@ def case_mask(c):
     return m
 
 
-def case_desc(c):
+def case_desc(c, precision="f32"):
     n, u = c["n"], c["U"]
     U6 = [[0.0] * 3 for _ in range(6)]
     if c["kind"] == "cavity":
@@ -70,7 +70,7 @@ def case_desc(c):
     else:
         faces = ["Inflow", "PressureOutlet", "NoSlip", "NoSlip", "Periodic", "Periodic"]
         U6[0] = [u, 0.0, 0.0]
-    return make_desc("D2Q9", (n, n), 1.0 / c["tau"], faces=faces, face_U=U6, precision="f32")
+    return make_desc("D2Q9", (n, n), 1.0 / c["tau"], faces=faces, face_U=U6, precision=precision)
 
 
 def features(c):
@@ -121,13 +121,13 @@ def fields_from_prediction(c, pred):
     return rho, u
 
 
-def solve(cases, init=None, max_steps=400_000, tol=1e-8, check_every=1000, k=100, log=None):
+def solve(cases, init=None, max_steps=400_000, tol=1e-8, check_every=1000, k=100, log=None, precision="f32"):
     """Advance all cases together from rest (init None) or from
     init[i] = (rho, u) (warm start), until each reaches the residual tol over
-    k steps.  Returns (steps per case or -1, final (rho, u) per case, seconds,
-    residual per case)."""
+    k steps.  Returns (steps per case: -1 not reached, -2 diverged; final
+    (rho, u) per case; seconds; last residual per case)."""
     set_device(0)
-    b = Batch([case_desc(c) for c in cases])
+    b = Batch([case_desc(c, precision) for c in cases])
     for i, c in enumerate(cases):
         b.set_obstacles(i, case_mask(c))
         if init is None:
@@ -144,7 +144,7 @@ def solve(cases, init=None, max_steps=400_000, tol=1e-8, check_every=1000, k=100
         b.advance(k)
         r, _ = b.residual()
         done += check_every
-        bad = ~np.isfinite(r) & (done > check_every)
+        bad = np.isnan(r)
         last = r
         newly = (steps < 0) & (r < tol)
         steps[newly] = done
@@ -155,3 +155,59 @@ def solve(cases, init=None, max_steps=400_000, tol=1e-8, check_every=1000, k=100
     out = [b.moments(i) for i in range(len(cases))]
     b.close()
     return steps, out, secs, last
+
+
+def dataset(cases, fields):
+    """Network arrays of the cases with finite fields: X [S][n][n][8],
+    Y [S][n][n][3], fluid mask M [S][n][n]."""
+    X, Y, M = [], [], []
+    for c, (rho, u) in zip(cases, fields):
+        X.append(features(c))
+        Y.append(targets(c, rho, u))
+        M.append(1.0 - case_mask(c).astype(np.float32))
+    return np.stack(X), np.stack(Y), np.stack(M)
+
+
+def train(X, Y, M, epochs=30, batch=8, lr=2e-3, seed=0, log=None, net=None):
+    """Adam with a cosine learning-rate schedule over shuffled mini-batches;
+    returns (net, per-epoch mean loss)."""
+    from .surrogate import Trainer, UNet
+    S, n = X.shape[0], X.shape[1]
+    net = net or UNet(seed=seed)
+    tr = Trainer(net, batch, n, n)
+    rng = np.random.default_rng(seed)
+    total = epochs * (S // batch)
+    it, hist = 0, []
+    for ep in range(epochs):
+        order = rng.permutation(S)
+        losses = []
+        for j in range(S // batch):
+            idx = order[j * batch:(j + 1) * batch]
+            lr_t = 0.5 * lr * (1.0 + math.cos(math.pi * it / total))
+            losses.append(tr.train_step(X[idx], Y[idx], M[idx], lr_t))
+            it += 1
+        hist.append(float(np.mean(losses)))
+        if log:
+            log(ep, hist[-1])
+    return net, hist
+
+
+def predict(net, cases, batch=8):
+    """(rho, u) predictions in the solver's layout, and the seconds taken."""
+    from .surrogate import Trainer
+    n = cases[0]["n"]
+    tr = Trainer(net, batch, n, n)
+    out = []
+    t0 = time.perf_counter()
+    for j in range(0, len(cases), batch):
+        cs = cases[j:j + batch]
+        pred = tr.predict(np.stack([features(c) for c in cs]))
+        out.extend(fields_from_prediction(c, p) for c, p in zip(cs, pred))
+    return out, time.perf_counter() - t0
+
+
+def field_error(c, pred, ref):
+    """Relative L2 error of the predicted velocity over the fluid cells."""
+    fluid = np.tile(case_mask(c).reshape(-1) == 0, 2)
+    du = (pred[1] - ref[1])[fluid]
+    return float(np.linalg.norm(du) / max(np.linalg.norm(ref[1][fluid]), 1e-30))
