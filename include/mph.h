@@ -176,6 +176,8 @@ int mph_residual(mph_sim* sim, double* out);
 /* Velocity set of a lattice (LatticeDescriptor.H:23-263): c[3 n + d],
  * w[n], opp[n] for n < q; any pointer may be NULL. */
 int mph_lattice(int q, int* c, double* w, int* opp);
+/* Sets the lattice time (a restart from a checkpoint, SimulationSetup.cpp:115). */
+int mph_set_time(mph_sim* sim, double t);
 /* Lattice time (number of completed advance() calls since init). */
 int mph_time(const mph_sim* sim, double* t);
 /* Number of step-kernel launches one advance() issues. */

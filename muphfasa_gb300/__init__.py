@@ -42,7 +42,7 @@ EXPORTS = [
     "mph_batch_destroy", "mph_batch_init_fields", "mph_batch_advance", "mph_batch_advance_timed",
     "mph_batch_advance_looped_timed", "mph_batch_get_f", "mph_batch_moments", "mph_batch_info",
     "mph_residual", "mph_batch_residual", "mph_lattice", "mph_set_obstacles", "mph_batch_set_obstacles",
-    "mph_init_fields_neq", "mph_batch_init_fields_neq", "mph_nn_alloc", "mph_nn_free", "mph_nn_copy", "mph_nn_sync", "mph_nn_gemm", "mph_nn_im2col3", "mph_nn_col2im3",
+    "mph_init_fields_neq", "mph_batch_init_fields_neq", "mph_set_time", "mph_nn_alloc", "mph_nn_free", "mph_nn_copy", "mph_nn_sync", "mph_nn_gemm", "mph_nn_im2col3", "mph_nn_col2im3",
     "mph_nn_bias_act", "mph_nn_act_bwd", "mph_nn_colsum", "mph_nn_pool", "mph_nn_pool_bwd", "mph_nn_up",
     "mph_nn_up_bwd", "mph_nn_slice", "mph_nn_mse", "mph_nn_adam", "mph_nn_cast", "mph_nn_fill",
 ]
@@ -109,6 +109,7 @@ def lib():
     L.mph_update_macroscopic.argtypes = [P, dp, dp]
     L.mph_reduce.argtypes = [P, dp]
     L.mph_residual.argtypes = [P, dp]
+    L.mph_set_time.argtypes = [P, C.c_double]
     L.mph_init_fields_neq.argtypes = [P, dp, dp]
     L.mph_batch_init_fields_neq.argtypes = [P, C.c_int, dp, dp]
     L.mph_set_obstacles.argtypes = [P, C.c_void_p]

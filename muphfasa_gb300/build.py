@@ -19,6 +19,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libmph.so")
+DRIVER = os.path.join(BUILD, "mph_run")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler",
@@ -73,15 +74,32 @@ def build(verbose: bool = False) -> str:
     tus = DEVICE_TUS + HOST_TUS
     with cf.ThreadPoolExecutor(max_workers=min(12, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), tus))
-    if os.path.exists(LIB) and all(os.path.getmtime(o) <= os.path.getmtime(LIB) for o in objs):
-        return LIB
+    if not (os.path.exists(LIB) and all(os.path.getmtime(o) <= os.path.getmtime(LIB) for o in objs)):
+        _link(objs)
+    _driver()
+    return LIB
+
+
+def _driver():
+    """The host driver executable (csrc/mph_run.cpp) over libmph.so."""
+    src = os.path.join(CSRC, "mph_run.cpp")
+    if os.path.exists(DRIVER) and os.path.getmtime(DRIVER) >= max(os.path.getmtime(src), os.path.getmtime(LIB)):
+        return
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I", INCLUDE, src, "-o", DRIVER + ".tmp", "-L", BUILD, "-lmph",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(DRIVER + ".tmp", DRIVER)
+
+
+def _link(objs):
     tmp = LIB + f".tmp{os.getpid()}"
     cmd = [_nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcudart_static", "-lrt", "-ldl", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
-    return LIB
 
 
 if __name__ == "__main__":

@@ -567,6 +567,12 @@ int mph_lattice(int q, int* c, double* w, int* opp) {
     return fail(MPH_ERR_ARG, "mph_lattice: q must be 9, 15, 19 or 27");
 }
 
+int mph_set_time(mph_sim* s, double t) {
+    if (!s) return fail(MPH_ERR_ARG, "mph_set_time: NULL handle");
+    s->time = t;
+    return MPH_OK;
+}
+
 int mph_time(const mph_sim* s, double* t) {
     if (!s || !t) return fail(MPH_ERR_ARG, "mph_time: NULL argument");
     *t = s->time;
