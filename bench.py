@@ -309,6 +309,20 @@ def run_warmstart(args):
     return 0
 
 
+def cpu_model():
+    """Host CPU name and core count (for the baseline record)."""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                name = ln.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    return {"model": name, "nproc": os.cpu_count()}
+
+
 def run_reference(args):
     from muphfasa_gb300 import replicas
     rank, world, _ = replicas.rank_info()
@@ -325,7 +339,8 @@ def run_reference(args):
                    "force": 1e-6, "sample_grid": list(n), "parallelism": "replicas"},
         "cpu_baseline": {"value": round(value, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
                          "sample": f"{n[0]}^3 domain of the workload, {args.steps} steps after {args.warmup} warm-up, "
-                                   f"OpenMP over cells, {threads} threads"},
+                                   f"OpenMP over cells, {threads} threads",
+                         "host": cpu_model()},
         "e2e": {"value": round(value, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -478,9 +493,12 @@ def main():
         threads = os.cpu_count() or 1
         sn = (256, 256, 256)
         v, dt = cpu_reference(sn, 20, 1, threads)
+        v1, dt1 = cpu_reference((128, 128, 128), 10, 1, 1)
         cpu = {"value": round(v, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
                "sample": f"{sn[0]}^3 domain of the workload, 20 steps after 1 warm-up, FP64, OpenMP {threads} threads "
-                         f"({dt:.2f} s)"}
+                         f"({dt:.2f} s)",
+               "single_thread": {"value": round(v1, 3), "sample": f"128^3, 10 steps, 1 thread ({dt1:.2f} s)"},
+               "host": cpu_model()}
 
     if rank == 0:
         line = {

@@ -11,10 +11,10 @@ namespace mph {
 
 // Block of 256 threads with lanes along x (rows of one (y, z)), grid over
 // (x-blocks, y-blocks, z).
-inline void step_shape(const KParams& p, dim3& grid, dim3& block) {
+inline void step_shape(const KParams& p, dim3& grid, dim3& block, int threads = 256) {
     int bx = ((p.nx + 31) / 32) * 32;
-    if (bx > 256) bx = 256;
-    const int by = 256 / bx;
+    if (bx > threads) bx = threads;
+    const int by = threads / bx;
     block = dim3(bx, by, 1);
     grid = dim3((p.nx + bx - 1) / bx, (p.ny + by - 1) / by, p.nz);
 }

@@ -360,7 +360,7 @@ int mph_create(const mph_desc* desc, mph_sim** out) {
     if (ncell >= (1LL << 31)) return fail(MPH_ERR_ARG, "mph_create: more than 2^31-1 cells");
     if ((long long)d.q * ncell >= (1LL << 32))
         return fail(MPH_ERR_ARG, "mph_create: q * cells must stay below 2^32 (32-bit element indices)");
-    if ((d.dim == 3 ? d.n[2] : 1) > 65535 || (d.n[1] + 7) / 8 > 65535)
+    if ((d.dim == 3 ? d.n[2] : 1) > 65535 || d.n[1] > 65535)
         return fail(MPH_ERR_ARG, "mph_create: ny or nz exceeds the launch grid limit (65535)");
     if (!(d.omega > 0.0 && d.omega < 2.0)) return fail(MPH_ERR_CONFIG, "mph_create: omega must lie in (0, 2)");
     if (d.precision == MPH_PREC_F64X && d.forced)
