@@ -289,6 +289,13 @@ int mph_nn_sync(void* stream);
  * B(k, n) = tb ? B[k ldb + n] : B[n ldb + k]. */
 int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const void* B, long long ldb, int tb,
                 float* C, long long ldc, int accumulate, void* stream);
+/* GEMM kernel choice for later calls: 1 = mma.sync (m16n8k16) tiles, 2 =
+ * tcgen05.mma with the accumulator in tensor memory (128 x 64 tiles), 0 =
+ * tcgen05 for M >= 128 and N >= 16, else mma.sync. */
+int mph_nn_gemm_mode(int mode);
+/* Reads (and with reset != 0 clears) the flag the tcgen05 GEMM sets when a
+ * bounded wait for its tensor-core work runs out. */
+int mph_nn_status(int* timeout, int reset);
 int mph_nn_im2col3(const void* X, int Bn, int H, int W, int C, void* Xcol, void* stream);
 int mph_nn_col2im3(const float* dXcol, int Bn, int H, int W, int C, float* dX, void* stream);
 /* out = act(Y + bias) into columns [c_off, c_off + C) of rows of width ld_out

@@ -29,9 +29,6 @@ typedef __nv_bfloat16 bf16;
 
 constexpr int BM = 64, BN = 64, BK = 32, KPAD = 8;
 
-__device__ __forceinline__ unsigned pack_bf16(bf16 lo, bf16 hi) {
-    return (unsigned)__bfloat16_as_ushort(lo) | ((unsigned)__bfloat16_as_ushort(hi) << 16);
-}
 
 __device__ __forceinline__ void mma_bf16(float* d, const unsigned* a, const unsigned* b) {
     asm volatile(
@@ -123,6 +120,172 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf
                     *p = accumulate ? *p + acc[i][j][r] : acc[i][j][r];
                 }
             }
+}
+
+// ---- tcgen05 GEMM (5th-generation tensor cores, accumulator in TMEM) ------
+// Same contract as k_gemm_bf16.  One CTA of 128 threads computes a 128 x 64
+// tile of C: per 64-wide K step all threads stage A (128 x 64) and B (64 x 64)
+// into shared memory in the no-swizzle K-major core-matrix layout (8 rows x
+// 16 bytes per 128-byte core matrix, core matrices contiguous along K, 1 KiB
+// apart along M / N), one thread issues four tcgen05.mma (M 128, N 64, K 16,
+// BF16 in, FP32 accumulate in TMEM) and commits them to an mbarrier that every
+// thread waits on before the buffer is refilled.  Each warp then reads its 32
+// TMEM lanes (rows) with tcgen05.ld.  Every wait is bounded: on timeout the
+// kernel records an error flag and skips its tile.
+constexpr int TC_BM = 128, TC_BN = 64, TC_BK = 64;
+constexpr unsigned long long kSpinLimit = 1ull << 26;
+
+__device__ int g_nn_timeout = 0;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// Core-matrix layout offset (bytes) of element (row, k) in a rows x TC_BK tile.
+__device__ __forceinline__ unsigned cm_off(int row, int k) {
+    return (unsigned)((((row >> 3) * (TC_BK / 8) + (k >> 3)) << 7) + ((row & 7) << 4) + ((k & 7) << 1));
+}
+
+__device__ __forceinline__ unsigned long long smem_desc(unsigned addr) {
+    const unsigned long long lbo = 128 >> 4, sbo = ((TC_BK / 8) * 128) >> 4;
+    return (unsigned long long)((addr >> 4) & 0x3FFF) | (lbo << 16) | (sbo << 32) | (1ull << 46);
+}
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(128) k_gemm_tc05(int M, int N, int K, const bf16* __restrict__ A, long long lda,
+                                                   const bf16* __restrict__ B, long long ldb, float* __restrict__ C,
+                                                   long long ldc, int accumulate) {
+    __shared__ __align__(1024) unsigned char As[TC_BM * TC_BK * 2];
+    __shared__ __align__(1024) unsigned char Bs[TC_BN * TC_BK * 2];
+    __shared__ __align__(8) unsigned long long mbar;
+    __shared__ unsigned tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long long m0 = (long long)blockIdx.y * TC_BM, n0 = (long long)blockIdx.x * TC_BN;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
+                     "r"(TC_BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    const unsigned tmem = tmem_base;
+    const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(TC_BN >> 3) << 17) |
+                           ((unsigned)(TC_BM >> 4) << 24);
+    const bf16 zero = __float2bfloat16(0.f);
+    unsigned phase = 0;
+    bool ok = true;
+    for (int k0 = 0; k0 < K && ok; k0 += TC_BK) {
+        // A: 128 rows x 8 chunks of 8 k-values; thread handles chunks tid + 128 i.
+#pragma unroll 2
+        for (int ch = tid; ch < TC_BM * (TC_BK / 8); ch += 128) {
+            const int row = ch % TC_BM, kc = ch / TC_BM;
+            const long long gm = m0 + row;
+            unsigned short v[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int gk = k0 + kc * 8 + j;
+                bf16 x = zero;
+                if (gm < M && gk < K) x = TA ? A[(long long)gk * lda + gm] : A[gm * lda + gk];
+                v[j] = __bfloat16_as_ushort(x);
+            }
+            uint4 w;
+            w.x = v[0] | ((unsigned)v[1] << 16);
+            w.y = v[2] | ((unsigned)v[3] << 16);
+            w.z = v[4] | ((unsigned)v[5] << 16);
+            w.w = v[6] | ((unsigned)v[7] << 16);
+            *reinterpret_cast<uint4*>(As + cm_off(row, kc * 8)) = w;
+        }
+#pragma unroll 2
+        for (int ch = tid; ch < TC_BN * (TC_BK / 8); ch += 128) {
+            const int row = ch % TC_BN, kc = ch / TC_BN;
+            const long long gn = n0 + row;
+            unsigned short v[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int gk = k0 + kc * 8 + j;
+                bf16 x = zero;
+                if (gn < N && gk < K) x = TB ? B[(long long)gk * ldb + gn] : B[gn * ldb + gk];
+                v[j] = __bfloat16_as_ushort(x);
+            }
+            uint4 w;
+            w.x = v[0] | ((unsigned)v[1] << 16);
+            w.y = v[2] | ((unsigned)v[3] << 16);
+            w.z = v[4] | ((unsigned)v[5] << 16);
+            w.w = v[6] | ((unsigned)v[7] << 16);
+            *reinterpret_cast<uint4*>(Bs + cm_off(row, kc * 8)) = w;
+        }
+        // Generic-proxy stores must be visible to the tensor core's async proxy.
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+        if (tid == 0) {
+#pragma unroll
+            for (int kk = 0; kk < TC_BK / 16; ++kk) {
+                // K step of 16 = two core matrices = 256 bytes
+                const unsigned long long ad = smem_desc(smem_u32(As) + kk * 256);
+                const unsigned long long bd = smem_desc(smem_u32(Bs) + kk * 256);
+                const unsigned acc = (k0 > 0 || kk > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                smem_u32(&mbar)));
+        }
+        // Every thread waits for the MMAs (they read the staged tiles).
+        unsigned done = 0;
+        for (unsigned long long it = 0; it < kSpinLimit && !done; ++it) {
+            asm volatile(
+                "{\n.reg .pred q;\nmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\nselp.u32 %0, 1, 0, q;\n}\n"
+                : "=r"(done)
+                : "r"(smem_u32(&mbar)), "r"(phase));
+        }
+        if (!done) {
+            ok = false;
+            atomicExch(&g_nn_timeout, 1);
+        }
+        phase ^= 1;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+        __syncthreads();
+    }
+    if (ok) {
+        // Warp w reads TMEM lanes 32 w .. 32 w + 31 (rows), 64 columns.
+        float acc[TC_BN];
+        unsigned r[TC_BN];
+        const unsigned taddr = tmem + ((unsigned)(32 * warp) << 16);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x64.b32 "
+            "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,"
+            "%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,"
+            "%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];\n"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+              "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
+              "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
+              "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
+              "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
+              "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < TC_BN; ++j) acc[j] = __uint_as_float(r[j]);
+        const long long row = m0 + 32 * warp + lane;
+        if (row < M) {
+            float* crow = C + row * ldc + n0;
+#pragma unroll
+            for (int j = 0; j < TC_BN; ++j)
+                if (n0 + j < N) crow[j] = accumulate ? crow[j] + acc[j] : acc[j];
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_BN));
 }
 
 // ---- convolution data movement --------------------------------------------
@@ -378,14 +541,44 @@ int mph_nn_sync(void* stream) {
     return MPH_OK;
 }
 
+static int g_gemm_mode = 0;  // 0 auto, 1 mma.sync, 2 tcgen05
+
+int mph_nn_gemm_mode(int mode) {
+    if (mode < 0 || mode > 2) return mph::fail(MPH_ERR_ARG, "mph_nn_gemm_mode: 0 auto, 1 mma.sync, 2 tcgen05");
+    g_gemm_mode = mode;
+    return MPH_OK;
+}
+
+int mph_nn_status(int* timeout, int reset) {
+    int v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_nn_timeout, sizeof(int));
+    if (e == cudaSuccess && reset) {
+        const int z = 0;
+        e = cudaMemcpyToSymbol(g_nn_timeout, &z, sizeof(int));
+    }
+    if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string("mph_nn_status: ") + cudaGetErrorString(e));
+    if (timeout) *timeout = v;
+    return MPH_OK;
+}
+
 int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const void* B, long long ldb, int tb,
                 float* C, long long ldc, int accumulate, void* stream) {
     if (M <= 0 || N <= 0 || K <= 0 || !A || !B || !C) return mph::fail(MPH_ERR_ARG, "mph_nn_gemm: bad argument");
-    const dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM));
-    if (grid.y > 65535) return mph::fail(MPH_ERR_ARG, "mph_nn_gemm: M too large for one launch");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     auto a = static_cast<const bf16*>(A);
     auto b = static_cast<const bf16*>(B);
+    const bool tc = g_gemm_mode == 2 || (g_gemm_mode == 0 && M >= TC_BM && N >= 16);
+    if (tc) {
+        const dim3 g((unsigned)((N + TC_BN - 1) / TC_BN), (unsigned)((M + TC_BM - 1) / TC_BM));
+        if (g.y > 65535) return mph::fail(MPH_ERR_ARG, "mph_nn_gemm: M too large for one launch");
+        if (!ta && !tb) k_gemm_tc05<false, false><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
+        else if (!ta && tb) k_gemm_tc05<false, true><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
+        else if (ta && !tb) k_gemm_tc05<true, false><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
+        else k_gemm_tc05<true, true><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
+        return ck("gemm (tcgen05)");
+    }
+    const dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM));
+    if (grid.y > 65535) return mph::fail(MPH_ERR_ARG, "mph_nn_gemm: M too large for one launch");
     if (!ta && !tb) k_gemm_bf16<false, false><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
     else if (!ta && tb) k_gemm_bf16<false, true><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
     else if (ta && !tb) k_gemm_bf16<true, false><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);

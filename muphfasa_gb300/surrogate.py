@@ -97,6 +97,8 @@ def _lib():
         L.mph_nn_cast.argtypes = [I, P, LL, P, P]
         L.mph_nn_fill.argtypes = [fp, LL, F, P]
         L.mph_nn_sync.argtypes = [P]
+        L.mph_nn_gemm_mode.argtypes = [I]
+        L.mph_nn_status.argtypes = [C.POINTER(C.c_int), I]
         _L = L
     return _L
 
