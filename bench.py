@@ -248,8 +248,9 @@ def run_warmstart(args):
                                          check_every=5000)
     keep = [i for i, r in enumerate(last) if np.isfinite(r) and r < args.ws_keep]
     X, Y, M = ws.dataset([train_cases[i] for i in keep], [fields[i] for i in keep])
-    log("generated", len(keep), len(train_cases), round(gen_secs, 1))
+    log("generated", len(keep), X.shape[0], len(train_cases), round(gen_secs, 1))
     t1 = time.perf_counter()
+    ntrain = X.shape[0]
     net, hist = ws.train(X, Y, M, epochs=args.ws_epochs, batch=8, lr=args.ws_lr, log=lambda e, l: log("epoch", e, l))
     train_secs = time.perf_counter() - t1
     del X, Y, M
@@ -290,6 +291,7 @@ def run_warmstart(args):
             "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "surrogate bf16 / f32 accumulate; solver f32 (data), f64 (judge)", "data": "synthetic",
             "config": {"workload": f"warmstart_d2q9_{n}^2", "train_cases": len(train_cases), "kept": len(keep),
+                       "trained_on": int(ntrain),
                        "test_cases": len(test_cases), "epochs": args.ws_epochs, "gen_steps": args.ws_gen_steps,
                        "params": net.n_params(), "Re": list(ws.RE), "U": list(ws.U)},
             "steps_plain_median": float(np.median(sp[sp > 0])) if np.any(sp > 0) else None,
@@ -407,7 +409,7 @@ def main():
     ap.add_argument("--ws-train", type=int, default=2000, help="warmstart: training cases")
     ap.add_argument("--ws-test", type=int, default=200, help="warmstart: held-out cases")
     ap.add_argument("--ws-epochs", type=int, default=30)
-    ap.add_argument("--ws-lr", type=float, default=2e-3)
+    ap.add_argument("--ws-lr", type=float, default=1e-3)
     ap.add_argument("--ws-gen-steps", type=int, default=150000, help="warmstart: FP32 steps per training field")
     ap.add_argument("--ws-keep", type=float, default=1e-4, help="warmstart: keep fields with FP32 residual below")
     ap.add_argument("--ws-max-steps", type=int, default=400000)

@@ -317,8 +317,11 @@ int mph_nn_slice(int kind, const void* src, int ld_src, int s_off, long long P, 
  * w (pred - target)^2 (nblocks blocks of 256 threads). */
 int mph_nn_mse(const float* pred, const float* target, const float* wgt, long long P, int C, float inv_count,
                float* dpred, float* part, int nblocks, void* stream);
+/* Adam step t on FP32 masters with gradient grad * gscale and L2 decay wd. */
 int mph_nn_adam(float* w, float* m, float* v, const float* grad, long long n, float lr, float b1, float b2, float eps,
-                int t, float wd, void* stream);
+                int t, float wd, float gscale, void* stream);
+/* part[b] = block sums of x^2 (nblocks blocks of 256 threads). */
+int mph_nn_sumsq(const float* x, long long n, float* part, int nblocks, void* stream);
 /* kind 0 float -> BF16, 1 BF16 -> float. */
 int mph_nn_cast(int kind, const void* x, long long n, void* y, void* stream);
 int mph_nn_fill(float* x, long long n, float v, void* stream);

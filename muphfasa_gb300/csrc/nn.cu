@@ -18,6 +18,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
 
 #include "mph.h"
@@ -42,10 +43,13 @@ __device__ __forceinline__ void mma_bf16(float* d, const unsigned* a, const unsi
 // A(m, k) = TA ? A[k * lda + m] : A[m * lda + k]
 // B(k, n) = TB ? B[k * ldb + n] : B[n * ldb + k]
 // 128 threads: warp w computes rows (w / 2) * 32 .. +32, cols (w % 2) * 32 .. +32.
+// Split K: blockIdx.z covers k in [z kchunk, (z + 1) kchunk) and, with more
+// than one split, writes its partial product to C + z M ldc (a workspace that
+// k_splitk_reduce adds up in split order).
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf16* __restrict__ A, long long lda,
                                                    const bf16* __restrict__ B, long long ldb, float* __restrict__ C,
-                                                   long long ldc, int accumulate) {
+                                                   long long ldc, int accumulate, int kchunk) {
     __shared__ __align__(16) bf16 As[BM][BK + KPAD];
     __shared__ __align__(16) bf16 Bs[BN][BK + KPAD];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -60,7 +64,9 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf
 #pragma unroll
             for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
     const bf16 zero = __float2bfloat16(0.f);
-    for (int k0 = 0; k0 < K; k0 += BK) {
+    const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+    C += (long long)blockIdx.z * M * ldc;
+    for (int k0 = kb; k0 < ke; k0 += BK) {
         // Stage A and B tiles (64 x 32 each: 2048 values, 16 per thread).
 #pragma unroll 4
         for (int e = tid; e < BM * BK; e += 128) {
@@ -69,7 +75,7 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf
             const long long gm = m0 + r;
             const int gk = k0 + c;
             bf16 v = zero;
-            if (gm < M && gk < K) v = TA ? A[(long long)gk * lda + gm] : A[gm * lda + gk];
+            if (gm < M && gk < ke) v = TA ? A[(long long)gk * lda + gm] : A[gm * lda + gk];
             As[r][c] = v;
         }
 #pragma unroll 4
@@ -79,7 +85,7 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf
             const long long gn = n0 + r;
             const int gk = k0 + c;
             bf16 v = zero;
-            if (gn < N && gk < K) v = TB ? B[(long long)gk * ldb + gn] : B[gn * ldb + gk];
+            if (gn < N && gk < ke) v = TB ? B[(long long)gk * ldb + gn] : B[gn * ldb + gk];
             Bs[r][c] = v;
         }
         __syncthreads();
@@ -152,7 +158,7 @@ __device__ __forceinline__ unsigned long long smem_desc(unsigned addr) {
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(128) k_gemm_tc05(int M, int N, int K, const bf16* __restrict__ A, long long lda,
                                                    const bf16* __restrict__ B, long long ldb, float* __restrict__ C,
-                                                   long long ldc, int accumulate) {
+                                                   long long ldc, int accumulate, int kchunk) {
     __shared__ __align__(1024) unsigned char As[TC_BM * TC_BK * 2];
     __shared__ __align__(1024) unsigned char Bs[TC_BN * TC_BK * 2];
     __shared__ __align__(8) unsigned long long mbar;
@@ -177,7 +183,9 @@ __global__ void __launch_bounds__(128) k_gemm_tc05(int M, int N, int K, const bf
     const bf16 zero = __float2bfloat16(0.f);
     unsigned phase = 0;
     bool ok = true;
-    for (int k0 = 0; k0 < K && ok; k0 += TC_BK) {
+    const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+    C += (long long)blockIdx.z * M * ldc;
+    for (int k0 = kb; k0 < ke && ok; k0 += TC_BK) {
         // A: 128 rows x 8 chunks of 8 k-values; thread handles chunks tid + 128 i.
 #pragma unroll 2
         for (int ch = tid; ch < TC_BM * (TC_BK / 8); ch += 128) {
@@ -188,7 +196,7 @@ __global__ void __launch_bounds__(128) k_gemm_tc05(int M, int N, int K, const bf
             for (int j = 0; j < 8; ++j) {
                 const int gk = k0 + kc * 8 + j;
                 bf16 x = zero;
-                if (gm < M && gk < K) x = TA ? A[(long long)gk * lda + gm] : A[gm * lda + gk];
+                if (gm < M && gk < ke) x = TA ? A[(long long)gk * lda + gm] : A[gm * lda + gk];
                 v[j] = __bfloat16_as_ushort(x);
             }
             uint4 w;
@@ -207,7 +215,7 @@ __global__ void __launch_bounds__(128) k_gemm_tc05(int M, int N, int K, const bf
             for (int j = 0; j < 8; ++j) {
                 const int gk = k0 + kc * 8 + j;
                 bf16 x = zero;
-                if (gn < N && gk < K) x = TB ? B[(long long)gk * ldb + gn] : B[gn * ldb + gk];
+                if (gn < N && gk < ke) x = TB ? B[(long long)gk * ldb + gn] : B[gn * ldb + gk];
                 v[j] = __bfloat16_as_ushort(x);
             }
             uint4 w;
@@ -228,7 +236,7 @@ __global__ void __launch_bounds__(128) k_gemm_tc05(int M, int N, int K, const bf
                 // K step of 16 = two core matrices = 256 bytes
                 const unsigned long long ad = smem_desc(smem_u32(As) + kk * 256);
                 const unsigned long long bd = smem_desc(smem_u32(Bs) + kk * 256);
-                const unsigned acc = (k0 > 0 || kk > 0) ? 1u : 0u;
+                const unsigned acc = (k0 > kb || kk > 0) ? 1u : 0u;
                 asm volatile(
                     "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
@@ -286,6 +294,20 @@ __global__ void __launch_bounds__(128) k_gemm_tc05(int M, int N, int K, const bf
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_BN));
+}
+
+// C[m][n] (+)= sum over splits z of W[z][m][n] (W rows of width N), in split order.
+__global__ void k_splitk_reduce(const float* __restrict__ W, int S, int M, int N, float* __restrict__ C, long long ldc,
+                                int accumulate) {
+    const long long total = (long long)M * N;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int z = 0; z < S; ++z) s += W[(long long)z * total + i];
+        const long long m = i / N, n = i % N;
+        float* p = C + m * ldc + n;
+        *p = accumulate ? *p + s : s;
+    }
 }
 
 // ---- convolution data movement --------------------------------------------
@@ -475,9 +497,9 @@ __global__ void k_mse(const float* __restrict__ pred, const float* __restrict__ 
 // master weights, with L2 weight decay wd.
 __global__ void k_adam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
                        const float* __restrict__ grad, long long n, float lr, float b1, float b2, float eps, float c1,
-                       float c2, float wd) {
+                       float c2, float wd, float gscale) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const float gi = grad[i] + wd * w[i];
+        const float gi = gscale * grad[i] + wd * w[i];
         const float mi = b1 * m[i] + (1.f - b1) * gi;
         const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
         m[i] = mi;
@@ -490,6 +512,21 @@ template <class T, class U>
 __global__ void k_cast(const T* __restrict__ x, long long n, U* __restrict__ y) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         y[i] = (U)(float)x[i];
+}
+
+// Block sums of x^2 into part[blockIdx.x].
+__global__ void k_sumsq(const float* __restrict__ x, long long n, float* __restrict__ part) {
+    float s = 0.f;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        s += x[i] * x[i];
+    __shared__ float sh[256];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
 __global__ void k_fill(float* __restrict__ x, long long n, float v) {
@@ -561,6 +598,11 @@ int mph_nn_status(int* timeout, int reset) {
     return MPH_OK;
 }
 
+// Split-K workspace, grown on demand (the weight gradients have a small
+// output and K = the pixel count).
+static float* g_ws = nullptr;
+static size_t g_ws_bytes = 0;
+
 int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const void* B, long long ldb, int tb,
                 float* C, long long ldc, int accumulate, void* stream) {
     if (M <= 0 || N <= 0 || K <= 0 || !A || !B || !C) return mph::fail(MPH_ERR_ARG, "mph_nn_gemm: bad argument");
@@ -568,22 +610,50 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
     auto a = static_cast<const bf16*>(A);
     auto b = static_cast<const bf16*>(B);
     const bool tc = g_gemm_mode == 2 || (g_gemm_mode == 0 && M >= TC_BM && N >= 16);
-    if (tc) {
-        const dim3 g((unsigned)((N + TC_BN - 1) / TC_BN), (unsigned)((M + TC_BM - 1) / TC_BM));
-        if (g.y > 65535) return mph::fail(MPH_ERR_ARG, "mph_nn_gemm: M too large for one launch");
-        if (!ta && !tb) k_gemm_tc05<false, false><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
-        else if (!ta && tb) k_gemm_tc05<false, true><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
-        else if (ta && !tb) k_gemm_tc05<true, false><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
-        else k_gemm_tc05<true, true><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
-        return ck("gemm (tcgen05)");
+    const int tm = tc ? TC_BM : BM, tn = tc ? TC_BN : BN;
+    const long long gx = (N + tn - 1) / tn, gy = (M + tm - 1) / tm;
+    if (gy > 65535) return mph::fail(MPH_ERR_ARG, "mph_nn_gemm: M too large for one launch");
+    // Enough blocks for the 152 SMs: split K when the output tiles are few.
+    int S = 1, kchunk = K;
+    const long long blocks = gx * gy;
+    if (blocks < 2 * 152 && K >= 8 * 64) {
+        S = (int)std::min<long long>((2 * 152 + blocks - 1) / blocks, K / (4 * 64));
+        S = std::max(1, std::min(S, 64));
+        kchunk = (K + S - 1) / S;
+        kchunk = (kchunk + 63) / 64 * 64;
+        S = (K + kchunk - 1) / kchunk;
     }
-    const dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM));
-    if (grid.y > 65535) return mph::fail(MPH_ERR_ARG, "mph_nn_gemm: M too large for one launch");
-    if (!ta && !tb) k_gemm_bf16<false, false><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
-    else if (!ta && tb) k_gemm_bf16<false, true><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
-    else if (ta && !tb) k_gemm_bf16<true, false><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
-    else k_gemm_bf16<true, true><<<grid, 128, 0, s>>>(M, N, K, a, lda, b, ldb, C, ldc, accumulate);
-    return ck("gemm");
+    float* out = C;
+    long long ldo = ldc;
+    int acc = accumulate;
+    if (S > 1) {
+        const size_t need = (size_t)S * M * N * sizeof(float);
+        if (need > g_ws_bytes) {
+            cudaFree(g_ws);
+            g_ws = nullptr;
+            g_ws_bytes = 0;
+            const cudaError_t e = cudaMalloc(&g_ws, need);
+            if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string("mph_nn_gemm workspace: ") + cudaGetErrorString(e));
+            g_ws_bytes = need;
+        }
+        out = g_ws;
+        ldo = N;
+        acc = 0;
+    }
+    const dim3 g((unsigned)gx, (unsigned)gy, (unsigned)S);
+#define MPH_GEMM_LAUNCH(KERN)                                                                                  \
+    if (!ta && !tb) KERN<false, false><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, out, ldo, acc, kchunk);      \
+    else if (!ta && tb) KERN<false, true><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, out, ldo, acc, kchunk);   \
+    else if (ta && !tb) KERN<true, false><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, out, ldo, acc, kchunk);   \
+    else KERN<true, true><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, out, ldo, acc, kchunk);
+    if (tc) {
+        MPH_GEMM_LAUNCH(k_gemm_tc05)
+    } else {
+        MPH_GEMM_LAUNCH(k_gemm_bf16)
+    }
+#undef MPH_GEMM_LAUNCH
+    if (S > 1) k_splitk_reduce<<<grid_for((long long)M * N), 256, 0, s>>>(g_ws, S, M, N, C, ldc, accumulate);
+    return ck(tc ? "gemm (tcgen05)" : "gemm (mma.sync)");
 }
 
 int mph_nn_im2col3(const void* X, int Bn, int H, int W, int C, void* Xcol, void* stream) {
@@ -667,10 +737,16 @@ int mph_nn_mse(const float* pred, const float* target, const float* wgt, long lo
 }
 
 int mph_nn_adam(float* w, float* m, float* v, const float* grad, long long n, float lr, float b1, float b2, float eps,
-                int t, float wd, void* stream) {
+                int t, float wd, float gscale, void* stream) {
     const float c1 = 1.f / (1.f - powf(b1, (float)t)), c2 = 1.f / (1.f - powf(b2, (float)t));
-    k_adam<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(w, m, v, grad, n, lr, b1, b2, eps, c1, c2, wd);
+    k_adam<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(w, m, v, grad, n, lr, b1, b2, eps, c1, c2, wd,
+                                                                         gscale);
     return ck("adam");
+}
+
+int mph_nn_sumsq(const float* x, long long n, float* part, int nblocks, void* stream) {
+    k_sumsq<<<nblocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(x, n, part);
+    return ck("sumsq");
 }
 
 // kind: 0 = f32 -> bf16, 1 = bf16 -> f32.

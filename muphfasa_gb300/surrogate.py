@@ -93,7 +93,8 @@ def _lib():
         L.mph_nn_up_bwd.argtypes = [fp, I, I, I, I, I, I, fp, P]
         L.mph_nn_slice.argtypes = [I, P, I, I, LL, I, P, I, I, I, P]
         L.mph_nn_mse.argtypes = [fp, fp, fp, LL, I, F, fp, fp, I, P]
-        L.mph_nn_adam.argtypes = [fp, fp, fp, fp, LL, F, F, F, F, I, F, P]
+        L.mph_nn_adam.argtypes = [fp, fp, fp, fp, LL, F, F, F, F, I, F, F, P]
+        L.mph_nn_sumsq.argtypes = [fp, LL, fp, I, P]
         L.mph_nn_cast.argtypes = [I, P, LL, P, P]
         L.mph_nn_fill.argtypes = [fp, LL, F, P]
         L.mph_nn_sync.argtypes = [P]
@@ -176,12 +177,20 @@ class Conv:
                                 self.dx.ptr, self.K, 0, None))
         return self.dx
 
-    def adam(self, lr, t, wd=0.0, b1=0.9, b2=0.999, eps=1e-8):
+    def adam(self, lr, t, wd=0.0, gscale=1.0, b1=0.9, b2=0.999, eps=1e-8):
         L = _lib()
-        check(L.mph_nn_adam(self.wt.ptr, self.mw.ptr, self.vw.ptr, self.gw.ptr, self.n, lr, b1, b2, eps, t, wd, None))
-        check(L.mph_nn_adam(self.b.ptr, self.mb.ptr, self.vb.ptr, self.gb.ptr, self.cout, lr, b1, b2, eps, t, 0.0,
+        check(L.mph_nn_adam(self.wt.ptr, self.mw.ptr, self.vw.ptr, self.gw.ptr, self.n, lr, b1, b2, eps, t, wd, gscale,
                             None))
+        check(L.mph_nn_adam(self.b.ptr, self.mb.ptr, self.vb.ptr, self.gb.ptr, self.cout, lr, b1, b2, eps, t, 0.0,
+                            gscale, None))
         self.refresh()
+
+    def grad_sumsq(self, part: Dev, nblk: int) -> float:
+        L = _lib()
+        check(L.mph_nn_sumsq(self.gw.ptr, self.n, part.ptr, nblk, None))
+        s = float(part.download(nblk).astype(np.float64).sum())
+        check(L.mph_nn_sumsq(self.gb.ptr, self.cout, part.ptr, nblk, None))
+        return s + float(part.download(nblk).astype(np.float64).sum())
 
     def get(self):
         return self.wt.download(self.n).reshape(self.cout, self.K), self.b.download(self.cout)
@@ -291,10 +300,24 @@ class UNet:
         d = l["e1b"].backward(self.ds1)
         l["e1a"].backward(d, need_dx=False)
 
-    def step(self, lr, wd=0.0):
+    def grad_norm(self) -> float:
+        if not hasattr(self, "_part"):
+            self._part = _f32(64)
+        return float(np.sqrt(sum(l.grad_sumsq(self._part, 64) for l in self.layers.values())))
+
+    def step(self, lr, wd=0.0, clip=None):
+        """Adam step; with clip, gradients are scaled so their global L2 norm
+        is at most clip (returns the norm before scaling)."""
         self.t += 1
+        norm, gscale = None, 1.0
+        if clip is not None:
+            norm = self.grad_norm()
+            if not np.isfinite(norm):
+                return norm  # skip a non-finite step
+            gscale = min(1.0, clip / max(norm, 1e-30))
         for layer in self.layers.values():
-            layer.adam(lr, self.t, wd)
+            layer.adam(lr, self.t, wd, gscale)
+        return norm
 
     def state(self):
         return {n: l.get() for n, l in self.layers.items()}
@@ -333,13 +356,13 @@ class Trainer:
                                 self.dpred.ptr, self.part.ptr, self.nblk, None))
         return float(self.part.download(self.nblk).sum()) / count
 
-    def train_step(self, x, y, m, lr, wd=0.0):
+    def train_step(self, x, y, m, lr, wd=0.0, clip=1.0):
         Bn = self.load_batch(x, y, m)
         self.net.forward(self.xb, Bn, self.H, self.W)
         count = float(m.sum()) * OUT_CH
         loss = self.loss_grad(Bn, count)
         self.net.backward(self.dpred)
-        self.net.step(lr, wd)
+        self.net.step(lr, wd, clip)
         return loss
 
     def predict(self, x):

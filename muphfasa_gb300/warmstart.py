@@ -157,20 +157,24 @@ def solve(cases, init=None, max_steps=400_000, tol=1e-8, check_every=1000, k=100
     return steps, out, secs, last
 
 
-def dataset(cases, fields):
-    """Network arrays of the cases with finite fields: X [S][n][n][8],
-    Y [S][n][n][3], fluid mask M [S][n][n]."""
+def dataset(cases, fields, limit=20.0):
+    """Network arrays of the cases with finite, bounded targets (|t| <= limit;
+    larger values mean a field far from a steady state at this scale):
+    X [S][n][n][8], Y [S][n][n][3], fluid mask M [S][n][n]."""
     X, Y, M = [], [], []
     for c, (rho, u) in zip(cases, fields):
+        t = targets(c, rho, u)
+        if not np.all(np.isfinite(t)) or np.max(np.abs(t)) > limit:
+            continue
         X.append(features(c))
-        Y.append(targets(c, rho, u))
+        Y.append(t)
         M.append(1.0 - case_mask(c).astype(np.float32))
     return np.stack(X), np.stack(Y), np.stack(M)
 
 
-def train(X, Y, M, epochs=30, batch=8, lr=2e-3, seed=0, log=None, net=None):
-    """Adam with a cosine learning-rate schedule over shuffled mini-batches;
-    returns (net, per-epoch mean loss)."""
+def train(X, Y, M, epochs=30, batch=8, lr=1e-3, seed=0, log=None, net=None, clip=1.0):
+    """Adam with a cosine learning-rate schedule and global gradient-norm
+    clipping over shuffled mini-batches; returns (net, per-epoch mean loss)."""
     from .surrogate import Trainer, UNet
     S, n = X.shape[0], X.shape[1]
     net = net or UNet(seed=seed)
@@ -184,7 +188,7 @@ def train(X, Y, M, epochs=30, batch=8, lr=2e-3, seed=0, log=None, net=None):
         for j in range(S // batch):
             idx = order[j * batch:(j + 1) * batch]
             lr_t = 0.5 * lr * (1.0 + math.cos(math.pi * it / total))
-            losses.append(tr.train_step(X[idx], Y[idx], M[idx], lr_t))
+            losses.append(tr.train_step(X[idx], Y[idx], M[idx], lr_t, clip=clip))
             it += 1
         hist.append(float(np.mean(losses)))
         if log:
