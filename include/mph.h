@@ -176,6 +176,13 @@ int mph_residual(mph_sim* sim, double* out);
 /* Velocity set of a lattice (LatticeDescriptor.H:23-263): c[3 n + d],
  * w[n], opp[n] for n < q; any pointer may be NULL. */
 int mph_lattice(int q, int* c, double* w, int* opp);
+/* The populations in the handle's own storage format (FP64, FP32, shifted
+ * 16-bit, or fixed-point int64; SoA, population slowest), for checkpoints
+ * that resume bit for bit in every precision (the FP64 view of mph_get_f
+ * rounds the 64-bit fixed point).  bytes must equal mph_state_bytes. */
+int mph_state_bytes(const mph_sim* sim, long long* bytes);
+int mph_get_state(mph_sim* sim, void* buf, long long bytes);
+int mph_set_state(mph_sim* sim, const void* buf, long long bytes);
 /* Sets the lattice time (a restart from a checkpoint, SimulationSetup.cpp:115). */
 int mph_set_time(mph_sim* sim, double t);
 /* Lattice time (number of completed advance() calls since init). */

@@ -42,7 +42,8 @@ EXPORTS = [
     "mph_batch_destroy", "mph_batch_init_fields", "mph_batch_advance", "mph_batch_advance_timed",
     "mph_batch_advance_looped_timed", "mph_batch_get_f", "mph_batch_moments", "mph_batch_info",
     "mph_residual", "mph_batch_residual", "mph_lattice", "mph_set_obstacles", "mph_batch_set_obstacles",
-    "mph_init_fields_neq", "mph_batch_init_fields_neq", "mph_set_time", "mph_nn_alloc", "mph_nn_free", "mph_nn_copy", "mph_nn_sync", "mph_nn_gemm", "mph_nn_im2col3", "mph_nn_col2im3",
+    "mph_init_fields_neq", "mph_batch_init_fields_neq", "mph_set_time", "mph_state_bytes", "mph_get_state",
+    "mph_set_state", "mph_nn_alloc", "mph_nn_free", "mph_nn_copy", "mph_nn_sync", "mph_nn_gemm", "mph_nn_im2col3", "mph_nn_col2im3",
     "mph_nn_bias_act", "mph_nn_act_bwd", "mph_nn_colsum", "mph_nn_pool", "mph_nn_pool_bwd", "mph_nn_up",
     "mph_nn_up_bwd", "mph_nn_slice", "mph_nn_mse", "mph_nn_adam", "mph_nn_cast", "mph_nn_fill",
     "mph_nn_gemm_mode", "mph_nn_status", "mph_nn_sumsq",

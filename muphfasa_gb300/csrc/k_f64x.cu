@@ -293,10 +293,10 @@ __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) 
 }
 
 // OBST: the domain has obstacles (p.cls set); the plain instantiation
-// carries no class-byte test.  128-thread blocks capped at 96 registers give
-// 20 resident warps per SM (two 256-thread blocks at 104 registers gave 16).
+// carries no class-byte test.  (128-thread blocks capped at 96 registers, 20
+// warps per SM, measured slower: 17.7 against 18.0 GLUPS at 512^3.)
 template <int Q, bool FORCED, bool OBST>
-__global__ void __launch_bounds__(128, 5) k_step_x(const i64* __restrict__ fin, i64* __restrict__ fout, const KParams p,
+__global__ void __launch_bounds__(256) k_step_x(const i64* __restrict__ fin, i64* __restrict__ fout, const KParams p,
                                                 const KParamsX px, const KParams* __restrict__ pg,
                                                 const i64* __restrict__ kbb, int* __restrict__ flag) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -466,7 +466,7 @@ cudaError_t launch_step_f64x(int q, bool forced, const long long* fin, long long
                              const KParamsX& px, const KParams* pg, const long long* kbb, int* flag,
                              cudaStream_t s) {
     dim3 g, b;
-    step_shape(p, g, b, 128);  // 128-thread blocks, 5 per SM at <= 96 registers
+    step_shape(p, g, b);
 #define MPH_X_CASE(QQ)                                                                        \
     case QQ:                                                                                  \
         if (p.cls) {                                                                          \

@@ -17,8 +17,10 @@
 //   * every amr.chk_int steps a checkpoint <amr.check_file><step:07d>: the
 //     reference's Header lines (Checkpoint.cpp:36-44: version, step, time,
 //     domain box, component count, ghost vector; version string of this
-//     build) and the populations as raw little-endian FP64 in valid-cell SoA
-//     order (x fastest, population slowest) in place of VisMF;
+//     build) plus a line naming the storage precision, the populations as
+//     raw little-endian FP64 in valid-cell SoA order (x fastest, population
+//     slowest, f.f64) in place of VisMF, and the handle's own storage
+//     (state.raw) so that every precision resumes bit for bit;
 //   * amr.restart = <checkpoint directory> resumes from such a checkpoint
 //     with step + 1 (SimulationSetup.cpp:107-117), bit for bit.
 #include <sys/stat.h>
@@ -132,7 +134,7 @@ int main(int argc, char** argv) {
     } else {
         std::ifstream hdr(restart + "/Header");
         if (!hdr) die("no Header file found in " + restart);
-        std::string version, domain, ngrow;
+        std::string version, domain, ngrow, stored;
         int step = 0, ncomp = 0;
         double time = 0.0;
         hdr >> version >> step >> time >> std::ws;
@@ -140,11 +142,22 @@ int main(int argc, char** argv) {
         hdr >> ncomp >> ngrow;
         if (version != kCheckpointVersion) die("unrecognized checkpoint version \"" + version + "\" in " + restart);
         if (!hdr || domain != domain_box(d) || ncomp != d.q) die("checkpoint " + restart + " does not match the domain");
-        std::vector<double> f((size_t)d.q * N);
-        std::ifstream fb(restart + "/f.f64", std::ios::binary);
-        fb.read(reinterpret_cast<char*>(f.data()), (std::streamsize)(f.size() * sizeof(double)));
-        if (!fb) die("short checkpoint payload in " + restart);
-        ck(mph_set_f(sim, f.data()), "restart");
+        hdr >> stored;  // "mph.precision=<name>" (optional)
+        long long nbytes = 0;
+        ck(mph_state_bytes(sim, &nbytes), "restart");
+        std::ifstream raw(restart + "/state.raw", std::ios::binary);
+        if (stored == "mph.precision=" + prec_name && raw) {
+            std::vector<unsigned char> st((size_t)nbytes);
+            raw.read(reinterpret_cast<char*>(st.data()), (std::streamsize)nbytes);
+            if (!raw) die("short state payload in " + restart);
+            ck(mph_set_state(sim, st.data(), nbytes), "restart");
+        } else {
+            std::vector<double> f((size_t)d.q * N);
+            std::ifstream fb(restart + "/f.f64", std::ios::binary);
+            fb.read(reinterpret_cast<char*>(f.data()), (std::streamsize)(f.size() * sizeof(double)));
+            if (!fb) die("short checkpoint payload in " + restart);
+            ck(mph_set_f(sim, f.data()), "restart");
+        }
         ck(mph_set_time(sim, time), "restart");
         start = step + 1;
     }
@@ -179,10 +192,16 @@ int main(int argc, char** argv) {
             ck(mph_get_f(sim, f.data()), "checkpoint");
             std::ofstream h(dir + "/Header");
             h << kCheckpointVersion << "\n" << step << "\n" << std::setprecision(17) << t << "\n" << domain_box(d)
-              << "\n" << d.q << "\n" << (d.dim == 2 ? "(0,0)" : "(0,0,0)") << "\n";
+              << "\n" << d.q << "\n" << (d.dim == 2 ? "(0,0)" : "(0,0,0)") << "\nmph.precision=" << prec_name << "\n";
             std::ofstream fb(dir + "/f.f64", std::ios::binary);
             fb.write(reinterpret_cast<const char*>(f.data()), (std::streamsize)(f.size() * sizeof(double)));
-            if (!fb || !h) die("cannot write checkpoint " + dir);
+            long long nbytes = 0;
+            ck(mph_state_bytes(sim, &nbytes), "checkpoint");
+            std::vector<unsigned char> st((size_t)nbytes);
+            ck(mph_get_state(sim, st.data(), nbytes), "checkpoint");
+            std::ofstream rb(dir + "/state.raw", std::ios::binary);
+            rb.write(reinterpret_cast<const char*>(st.data()), (std::streamsize)nbytes);
+            if (!fb || !h || !rb) die("cannot write checkpoint " + dir);
             std::cout << "Checkpoint: wrote " << dir << "  step=" << step << "  time=" << t << "\n";
         }
     }

@@ -567,6 +567,31 @@ int mph_lattice(int q, int* c, double* w, int* opp) {
     return fail(MPH_ERR_ARG, "mph_lattice: q must be 9, 15, 19 or 27");
 }
 
+int mph_state_bytes(const mph_sim* s, long long* bytes) {
+    if (!s || !bytes) return fail(MPH_ERR_ARG, "mph_state_bytes: NULL argument");
+    *bytes = (long long)(s->elem * (size_t)s->d.q * (size_t)s->kp.ncell);
+    return MPH_OK;
+}
+
+int mph_get_state(mph_sim* s, void* buf, long long bytes) {
+    if (!s || !buf) return fail(MPH_ERR_ARG, "mph_get_state: NULL argument");
+    if (!s->has_state) return fail(MPH_ERR_STATE, "mph_get_state: no populations yet");
+    const long long n = (long long)(s->elem * (size_t)s->d.q * (size_t)s->kp.ncell);
+    if (bytes != n) return fail(MPH_ERR_ARG, "mph_get_state: size differs from mph_state_bytes");
+    MPH_CK(cudaMemcpyAsync(buf, s->fa, (size_t)n, cudaMemcpyDeviceToHost, s->stream), "download state");
+    return sync(s, "mph_get_state");
+}
+
+int mph_set_state(mph_sim* s, const void* buf, long long bytes) {
+    if (!s || !buf) return fail(MPH_ERR_ARG, "mph_set_state: NULL argument");
+    const long long n = (long long)(s->elem * (size_t)s->d.q * (size_t)s->kp.ncell);
+    if (bytes != n) return fail(MPH_ERR_ARG, "mph_set_state: size differs from mph_state_bytes");
+    MPH_CK(cudaMemcpyAsync(s->fa, buf, (size_t)n, cudaMemcpyHostToDevice, s->stream), "upload state");
+    s->has_state = true;
+    s->has_uprev = false;
+    return sync(s, "mph_set_state");
+}
+
 int mph_set_time(mph_sim* s, double t) {
     if (!s) return fail(MPH_ERR_ARG, "mph_set_time: NULL handle");
     s->time = t;

@@ -39,7 +39,7 @@ def test_plotfile_matches_library_moments(mph, tmp_path):
     vx = _load_npy(tmp_path / "plt0000020" / "vx.npy").reshape(-1)
     assert np.array_equal(vx, u[:1024] * (info.dx / info.dt))
     hdr = (tmp_path / "plt0000020" / "Header").read_text().split("\n")
-    assert hdr[0] == "muphfasa_gb300_plotfile_v1" and int(hdr[6]) == 20
+    assert hdr[0] == "muphfasa_gb300_plotfile_v1" and hdr[1] == "3" and int(hdr[7]) == 20
 
 
 @pytest.mark.parametrize("precision", ["f64", "f64x"])
@@ -57,6 +57,9 @@ def test_restart_is_bit_exact(mph, tmp_path, precision):
     ha = (a / "chk0000040" / "Header").read_text().split("\n")
     hb = (b / "chk0000040" / "Header").read_text().split("\n")
     assert ha == hb and ha[0] == "muphfasa_gb300_checkpoint_v1" and float(ha[2]) == 41.0
+    assert ha[6] == f"mph.precision={precision}"
+    ra = (a / "chk0000040" / "state.raw").read_bytes()
+    assert ra == (b / "chk0000040" / "state.raw").read_bytes()
 
 
 def test_errors_are_reported(mph, tmp_path):
