@@ -261,6 +261,9 @@ def run_warmstart(args):
     log("warm", int(np.sum(sw > 0)), round(secs_warm, 1))
     both = (sp > 0) & (sw > 0)
     errs = [ws.field_error(c, p, r) for c, p, r, ok in zip(test_cases, preds, ref, sp > 0) if ok]
+    err_all = np.array([ws.field_error(c, p, r) if ok else np.nan for c, p, r, ok in zip(test_cases, preds, ref, sp > 0)])
+    by_kind = {k: float(np.nanmedian(err_all[[c["kind"] == k for c in test_cases]])) for k in ("cavity", "channel")}
+    good = both & (err_all < 0.2)
     # single-case wall time (one handle per case, FP64): rest vs predict + warm start
     single = []
     for c in [c for c, ok in zip(test_cases, both) if ok][: args.ws_single]:
@@ -300,7 +303,9 @@ def run_warmstart(args):
             "converged": {"plain": int(np.sum(sp > 0)), "warm": int(np.sum(sw > 0)), "both": int(np.sum(both)),
                           "diverged_plain": int(np.sum(sp == -2))},
             "surrogate_u_error": {"median": float(np.median(errs)) if errs else None,
-                                  "p90": float(np.percentile(errs, 90)) if errs else None},
+                                  "p90": float(np.percentile(errs, 90)) if errs else None, "by_kind": by_kind},
+            "steps_ratio_when_error_below_0.2": {"cases": int(good.sum()),
+                                                 "median": float(np.median(sp[good] / sw[good])) if good.any() else None},
             "seconds": {"generate": round(gen_secs, 1), "train": round(train_secs, 1),
                         "predict_all": round(pred_secs, 3), "batch_plain": round(secs_plain, 1),
                         "batch_warm": round(secs_warm, 1)},
