@@ -250,6 +250,7 @@ def run_warmstart(args):
     X, Y, M = ws.dataset([train_cases[i] for i in keep], [fields[i] for i in keep])
     log("generated", len(keep), X.shape[0], len(train_cases), round(gen_secs, 1))
     t1 = time.perf_counter()
+    X, Y, M = ws.mirror_channels(X, Y, M)
     ntrain = X.shape[0]
     net, hist = ws.train(X, Y, M, epochs=args.ws_epochs, batch=8, lr=args.ws_lr, log=lambda e, l: log("epoch", e, l))
     train_secs = time.perf_counter() - t1
@@ -413,10 +414,10 @@ def main():
     ap.add_argument("--ws-n", type=int, default=128, help="warmstart: cells per side")
     ap.add_argument("--ws-train", type=int, default=2000, help="warmstart: training cases")
     ap.add_argument("--ws-test", type=int, default=200, help="warmstart: held-out cases")
-    ap.add_argument("--ws-epochs", type=int, default=30)
-    ap.add_argument("--ws-lr", type=float, default=1e-3)
-    ap.add_argument("--ws-gen-steps", type=int, default=150000, help="warmstart: FP32 steps per training field")
-    ap.add_argument("--ws-keep", type=float, default=1e-4, help="warmstart: keep fields with FP32 residual below")
+    ap.add_argument("--ws-epochs", type=int, default=200)
+    ap.add_argument("--ws-lr", type=float, default=2e-3)
+    ap.add_argument("--ws-gen-steps", type=int, default=300000, help="warmstart: FP32 steps per training field")
+    ap.add_argument("--ws-keep", type=float, default=5e-5, help="warmstart: keep fields with FP32 residual below")
     ap.add_argument("--ws-max-steps", type=int, default=400000)
     ap.add_argument("--ws-single", type=int, default=6, help="warmstart: cases timed on single handles")
     ap.add_argument("--tgv-ref", default="f64x", choices=["f64x", "f64", "f64_fast"],

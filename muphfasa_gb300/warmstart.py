@@ -172,6 +172,21 @@ def dataset(cases, fields, limit=20.0):
     return np.stack(X), np.stack(Y), np.stack(M)
 
 
+def mirror_channels(X, Y, M):
+    """Channels are symmetric under y -> n - 1 - y (uniform inflow, walls at
+    both y faces): append the mirrored copy of every channel sample (obstacles
+    mirrored, u_y negated) to the training arrays."""
+    ch = X[..., 3].max(axis=(1, 2)) > 0  # the outlet column marks a channel
+    if not ch.any():
+        return X, Y, M
+    Xm = X[ch][:, ::-1].copy()
+    Xm[..., 7] = X[ch][..., 7]  # the y coordinate channel keeps its orientation
+    Ym = Y[ch][:, ::-1].copy()
+    Ym[..., 2] = -Ym[..., 2]
+    Mm = M[ch][:, ::-1].copy()
+    return np.concatenate([X, Xm]), np.concatenate([Y, Ym]), np.concatenate([M, Mm])
+
+
 def train(X, Y, M, epochs=30, batch=8, lr=1e-3, seed=0, log=None, net=None, clip=1.0):
     """Adam with a cosine learning-rate schedule and global gradient-norm
     clipping over shuffled mini-batches; returns (net, per-epoch mean loss)."""
