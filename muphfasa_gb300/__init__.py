@@ -112,6 +112,9 @@ def lib():
     L.mph_reduce.argtypes = [P, dp]
     L.mph_residual.argtypes = [P, dp]
     L.mph_set_time.argtypes = [P, C.c_double]
+    L.mph_state_bytes.argtypes = [P, C.POINTER(C.c_longlong)]
+    L.mph_get_state.argtypes = [P, C.c_void_p, C.c_longlong]
+    L.mph_set_state.argtypes = [P, C.c_void_p, C.c_longlong]
     L.mph_init_fields_neq.argtypes = [P, dp, dp]
     L.mph_batch_init_fields_neq.argtypes = [P, C.c_int, dp, dp]
     L.mph_set_obstacles.argtypes = [P, C.c_void_p]
