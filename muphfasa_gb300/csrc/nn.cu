@@ -181,6 +181,9 @@ __global__ void __launch_bounds__(128) k_gemm_tc05(int M, int N, int K, const bf
     const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(TC_BN >> 3) << 17) |
                            ((unsigned)(TC_BM >> 4) << 24);
     const bf16 zero = __float2bfloat16(0.f);
+    // 16-byte loads need 16-byte aligned bases (element offsets are checked per chunk)
+    const bool a_vec = (reinterpret_cast<unsigned long long>(A) & 15) == 0;
+    const bool b_vec = (reinterpret_cast<unsigned long long>(B) & 15) == 0;
     unsigned phase = 0;
     bool ok = true;
     const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
@@ -191,10 +194,16 @@ __global__ void __launch_bounds__(128) k_gemm_tc05(int M, int N, int K, const bf
         for (int ch = tid; ch < TC_BM * (TC_BK / 8); ch += 128) {
             const int row = ch % TC_BM, kc = ch / TC_BM;
             const long long gm = m0 + row;
+            const int gk0 = k0 + kc * 8;
+            if (!TA && a_vec && gm < M && gk0 + 8 <= ke && ((gm * lda + gk0) & 7) == 0) {
+                // eight K-contiguous values: one 16-byte load
+                *reinterpret_cast<uint4*>(As + cm_off(row, kc * 8)) = __ldg(reinterpret_cast<const uint4*>(A + gm * lda + gk0));
+                continue;
+            }
             unsigned short v[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                const int gk = k0 + kc * 8 + j;
+                const int gk = gk0 + j;
                 bf16 x = zero;
                 if (gm < M && gk < ke) x = TA ? A[(long long)gk * lda + gm] : A[gm * lda + gk];
                 v[j] = __bfloat16_as_ushort(x);
@@ -210,10 +219,15 @@ __global__ void __launch_bounds__(128) k_gemm_tc05(int M, int N, int K, const bf
         for (int ch = tid; ch < TC_BN * (TC_BK / 8); ch += 128) {
             const int row = ch % TC_BN, kc = ch / TC_BN;
             const long long gn = n0 + row;
+            const int gk0 = k0 + kc * 8;
+            if (!TB && b_vec && gn < N && gk0 + 8 <= ke && ((gn * ldb + gk0) & 7) == 0) {
+                *reinterpret_cast<uint4*>(Bs + cm_off(row, kc * 8)) = __ldg(reinterpret_cast<const uint4*>(B + gn * ldb + gk0));
+                continue;
+            }
             unsigned short v[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                const int gk = k0 + kc * 8 + j;
+                const int gk = gk0 + j;
                 bf16 x = zero;
                 if (gn < N && gk < ke) x = TB ? B[(long long)gk * ldb + gn] : B[gn * ldb + gk];
                 v[j] = __bfloat16_as_ushort(x);
