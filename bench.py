@@ -478,7 +478,8 @@ def main():
     try:
         if args.e2e_steps <= 0:
             raise StopIteration
-        f_host = torch.empty(q * cells, dtype=torch.float64, pin_memory=True).numpy()
+        pinned = m.PinnedArray(q * cells)  # cudaHostAlloc'ed, not a pageable buffer
+        f_host = pinned.array
         sim.f(out=f_host)
         sim.step_host(f_host, f_host, 1)  # warm-up of the path
         replicas.barrier(dist, dev)
@@ -489,8 +490,9 @@ def main():
         dt = replicas.max_over_ranks(dist, dt, dev)
         e2e = {"value": round(total_cells * args.e2e_steps / dt / 1e6, 3), "unit": "MLUPS",
                "h2d_bytes_per_step": q * cells * 8, "d2h_bytes_per_step": q * cells * 8,
-               "steps": args.e2e_steps, "host_buffers": "pinned", "api": "mph_step_host"}
+               "steps": args.e2e_steps, "host_buffers": "pinned (cudaHostAlloc)", "api": "mph_step_host"}
         del f_host
+        pinned.close()
     except StopIteration:
         pass
     except Exception as ex:  # report, do not hide

@@ -103,6 +103,11 @@ typedef struct {
 
 const char* mph_last_error(void);
 int mph_abi_version(void);
+/* Page-locked host memory for the host-buffer calls (mph_step_host,
+ * mph_set_f, mph_get_f): copies from it run at the full host link rate. */
+int mph_host_alloc(long long bytes, void** out);
+int mph_host_free(void* p);
+
 /* Selects the CUDA device used by handles created afterwards on the calling
  * thread (the reference binds one device per MPI rank when AMReX initialises
  * its GPU backend; here one process drives one device). */

@@ -43,7 +43,7 @@ EXPORTS = [
     "mph_batch_advance_looped_timed", "mph_batch_get_f", "mph_batch_moments", "mph_batch_info",
     "mph_residual", "mph_batch_residual", "mph_lattice", "mph_set_obstacles", "mph_batch_set_obstacles",
     "mph_init_fields_neq", "mph_batch_init_fields_neq", "mph_set_time", "mph_state_bytes", "mph_get_state",
-    "mph_set_state", "mph_nn_alloc", "mph_nn_free", "mph_nn_copy", "mph_nn_sync", "mph_nn_gemm", "mph_nn_im2col3", "mph_nn_col2im3",
+    "mph_set_state", "mph_host_alloc", "mph_host_free", "mph_nn_alloc", "mph_nn_free", "mph_nn_copy", "mph_nn_sync", "mph_nn_gemm", "mph_nn_im2col3", "mph_nn_col2im3",
     "mph_nn_bias_act", "mph_nn_act_bwd", "mph_nn_colsum", "mph_nn_pool", "mph_nn_pool_bwd", "mph_nn_up",
     "mph_nn_up_bwd", "mph_nn_slice", "mph_nn_mse", "mph_nn_adam", "mph_nn_cast", "mph_nn_fill",
     "mph_nn_gemm_mode", "mph_nn_status", "mph_nn_sumsq",
@@ -112,6 +112,8 @@ def lib():
     L.mph_reduce.argtypes = [P, dp]
     L.mph_residual.argtypes = [P, dp]
     L.mph_set_time.argtypes = [P, C.c_double]
+    L.mph_host_alloc.argtypes = [C.c_longlong, C.POINTER(C.c_void_p)]
+    L.mph_host_free.argtypes = [C.c_void_p]
     L.mph_state_bytes.argtypes = [P, C.POINTER(C.c_longlong)]
     L.mph_get_state.argtypes = [P, C.c_void_p, C.c_longlong]
     L.mph_set_state.argtypes = [P, C.c_void_p, C.c_longlong]
@@ -162,6 +164,27 @@ def lattice_tables(lattice: str):
     opp = (C.c_int * q)()
     check(lib().mph_lattice(q, c, _dp(w), opp))
     return np.array(list(c), dtype=np.int64).reshape(q, 3), w, np.array(list(opp), dtype=np.int64)
+
+
+class PinnedArray:
+    """A float64 NumPy array in page-locked host memory (mph_host_alloc)."""
+
+    def __init__(self, n: int):
+        self._p = C.c_void_p()
+        check(lib().mph_host_alloc(C.c_longlong(8 * int(n)), C.byref(self._p)))
+        self.array = np.ctypeslib.as_array((C.c_double * int(n)).from_address(self._p.value))
+
+    def close(self):
+        if getattr(self, "_p", None) is not None and self._p.value:
+            self.array = None
+            lib().mph_host_free(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def make_desc(lattice: str, n, omega: float, faces=None, face_rho=None, face_U=None, force=None,

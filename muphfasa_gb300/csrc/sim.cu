@@ -339,6 +339,18 @@ int sync(mph_sim* s, const char* what) {
 
 extern "C" {
 
+int mph_host_alloc(long long bytes, void** out) {
+    if (!out || bytes <= 0) return fail(MPH_ERR_ARG, "mph_host_alloc: bad argument");
+    *out = nullptr;
+    MPH_CK(cudaHostAlloc(out, (size_t)bytes, cudaHostAllocDefault), "cudaHostAlloc");
+    return MPH_OK;
+}
+
+int mph_host_free(void* p) {
+    if (p) MPH_CK(cudaFreeHost(p), "cudaFreeHost");
+    return MPH_OK;
+}
+
 int mph_set_device(int device) {
     int n = 0;
     MPH_CK(cudaGetDeviceCount(&n), "cudaGetDeviceCount");

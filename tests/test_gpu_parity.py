@@ -229,6 +229,13 @@ def test_step_host_equals_resident_steps(mph):
     out = np.empty_like(f0)
     b.step_host(f0, out, 7)
     assert np.array_equal(out, a.f())
+    # the same through page-locked buffers from mph_host_alloc
+    pin_in, pin_out = mph.PinnedArray(f0.size), mph.PinnedArray(f0.size)
+    pin_in.array[:] = f0
+    b.step_host(pin_in.array, pin_out.array, 7)
+    assert np.array_equal(pin_out.array, out)
+    pin_in.close()
+    pin_out.close()
 
 
 def _dev_a4(mph, torch, arr_ghost, q, ext):
