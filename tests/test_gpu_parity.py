@@ -306,3 +306,23 @@ def test_plugin_rejects_too_small_array(mph):
     lo = (C.c_int * 3)(0, 0, 0)
     hi = (C.c_int * 3)(3, 3, 0)
     assert L.mph_pull_collide_fused_arr(2, 9, lo, hi, C.byref(a), C.byref(a), 1.0, None, None) == 1
+
+
+@pytest.mark.parametrize("precision", ["f64", "f64x", "f32", "f16s"])
+@pytest.mark.parametrize("lat,n", [("D2Q9", (20, 16)), ("D3Q19", (12, 10, 8)), ("D3Q27", (10, 8, 6))])
+def test_zero_force_is_bit_identical_to_unforced(lat, n, precision, mph):
+    """The forced kernels with F = 0 reproduce the unforced ones bit for bit
+    (the reference's F = 0 identity of the Guo path, test_forcing.cpp)."""
+    faces = ["Periodic", "Periodic", "NoSlip", "MovingWall", "Periodic", "Periodic"]
+    U = [[0.0] * 3 for _ in range(6)]
+    U[3] = [0.05, 0.0, 0.0]
+    kw = dict(faces=faces, face_U=U, precision=precision)
+    a = mph.Simulation(mph.make_desc(lat, n, 1.3, **kw))
+    b = mph.Simulation(mph.make_desc(lat, n, 1.3, force=(0.0, 0.0, 0.0), **kw))
+    rng = np.random.default_rng(3)
+    rho, u = _fields(rng, a.ncell, len(n))
+    a.initialize(rho.copy(), u.copy())
+    b.initialize(rho.copy(), u.copy())
+    a.advance(23)
+    b.advance(23)
+    assert np.array_equal(a.f(), b.f())
