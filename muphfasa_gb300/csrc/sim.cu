@@ -29,7 +29,9 @@ struct mph_sim {
     void* fb = nullptr;       // next populations (m_fout)
     double* d_rho = nullptr;  // macroscopic scratch (init / moments)
     double* d_u = nullptr;
-    double* d_stage = nullptr;  // FP64 staging of one population (conversions)
+    double* d_stage = nullptr;  // FP64 staging of two populations (conversions)
+    cudaStream_t copy_stream = nullptr;  // host copies overlapping the conversions
+    cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_converted[2] = {nullptr, nullptr};
     double* d_part = nullptr;   // reduction partials
     double* d_red = nullptr;    // reduction result
     double* d_uprev = nullptr;  // velocity field saved by the last mph_residual (dim x N)
@@ -237,6 +239,11 @@ void free_all(mph_sim* s) {
     cudaFree(s->d_cls);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
+    for (int i = 0; i < 2; ++i) {
+        if (s->ev_copied[i]) cudaEventDestroy(s->ev_copied[i]);
+        if (s->ev_converted[i]) cudaEventDestroy(s->ev_converted[i]);
+    }
+    if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
     if (s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -247,7 +254,14 @@ int ensure_macro(mph_sim* s) {
 }
 
 int ensure_stage(mph_sim* s) {
-    if (!s->d_stage) MPH_CK(cudaMalloc(&s->d_stage, sizeof(double) * s->kp.ncell), "cudaMalloc(stage)");
+    if (!s->d_stage) {
+        MPH_CK(cudaMalloc(&s->d_stage, 2 * sizeof(double) * s->kp.ncell), "cudaMalloc(stage)");
+        MPH_CK(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking), "copy stream");
+        for (int i = 0; i < 2; ++i) {
+            MPH_CK(cudaEventCreateWithFlags(&s->ev_copied[i], cudaEventDisableTiming), "copy event");
+            MPH_CK(cudaEventCreateWithFlags(&s->ev_converted[i], cudaEventDisableTiming), "copy event");
+        }
+    }
     return MPH_OK;
 }
 
@@ -306,10 +320,21 @@ int upload(mph_sim* s, const double* f) {
     }
     int rc = ensure_stage(s);
     if (rc) return rc;
+    // Double-buffered: the copy of population q into stage q % 2 (copy
+    // stream) overlaps the conversion of population q - 1 (handle stream).
+    const size_t N = (size_t)s->kp.ncell;
+    MPH_CK(cudaEventRecord(s->ev_converted[0], s->stream), "upload order");
+    MPH_CK(cudaEventRecord(s->ev_converted[1], s->stream), "upload order");
     for (int q = 0; q < s->d.q; ++q) {
-        MPH_CK(cudaMemcpyAsync(s->d_stage, f + (size_t)q * s->kp.ncell, sizeof(double) * s->kp.ncell,
-                               cudaMemcpyHostToDevice, s->stream), "upload f");
-        MPH_CK(launch_convert(s->d.precision, s->d.q, true, s->fa, s->d_stage, q, s->kp.ncell, s->stream), "convert f");
+        const int b = q & 1;
+        double* st = s->d_stage + b * N;
+        MPH_CK(cudaStreamWaitEvent(s->copy_stream, s->ev_converted[b], 0), "upload order");
+        MPH_CK(cudaMemcpyAsync(st, f + (size_t)q * N, sizeof(double) * N, cudaMemcpyHostToDevice, s->copy_stream),
+               "upload f");
+        MPH_CK(cudaEventRecord(s->ev_copied[b], s->copy_stream), "upload order");
+        MPH_CK(cudaStreamWaitEvent(s->stream, s->ev_copied[b], 0), "upload order");
+        MPH_CK(launch_convert(s->d.precision, s->d.q, true, s->fa, st, q, s->kp.ncell, s->stream), "convert f");
+        MPH_CK(cudaEventRecord(s->ev_converted[b], s->stream), "upload order");
     }
     return MPH_OK;
 }
@@ -322,11 +347,24 @@ int download(mph_sim* s, double* f) {
     }
     int rc = ensure_stage(s);
     if (rc) return rc;
+    // Double-buffered: the conversion of population q (handle stream)
+    // overlaps the copy of population q - 1 to the host (copy stream); the
+    // handle stream waits for the last copy, so sync() covers everything.
+    const size_t N = (size_t)s->kp.ncell;
+    MPH_CK(cudaEventRecord(s->ev_copied[0], s->copy_stream), "download order");
+    MPH_CK(cudaEventRecord(s->ev_copied[1], s->copy_stream), "download order");
     for (int q = 0; q < s->d.q; ++q) {
-        MPH_CK(launch_convert(s->d.precision, s->d.q, false, s->fa, s->d_stage, q, s->kp.ncell, s->stream), "convert f");
-        MPH_CK(cudaMemcpyAsync(f + (size_t)q * s->kp.ncell, s->d_stage, sizeof(double) * s->kp.ncell,
-                               cudaMemcpyDeviceToHost, s->stream), "download f");
+        const int b = q & 1;
+        double* st = s->d_stage + b * N;
+        MPH_CK(cudaStreamWaitEvent(s->stream, s->ev_copied[b], 0), "download order");
+        MPH_CK(launch_convert(s->d.precision, s->d.q, false, s->fa, st, q, s->kp.ncell, s->stream), "convert f");
+        MPH_CK(cudaEventRecord(s->ev_converted[b], s->stream), "download order");
+        MPH_CK(cudaStreamWaitEvent(s->copy_stream, s->ev_converted[b], 0), "download order");
+        MPH_CK(cudaMemcpyAsync(f + (size_t)q * N, st, sizeof(double) * N, cudaMemcpyDeviceToHost, s->copy_stream),
+               "download f");
+        MPH_CK(cudaEventRecord(s->ev_copied[b], s->copy_stream), "download order");
     }
+    MPH_CK(cudaStreamWaitEvent(s->stream, s->ev_copied[(s->d.q - 1) & 1], 0), "download order");
     return MPH_OK;
 }
 
