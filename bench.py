@@ -254,6 +254,10 @@ def run_warmstart(args):
     ntrain = X.shape[0]
     net, hist = ws.train(X, Y, M, epochs=args.ws_epochs, batch=8, lr=args.ws_lr, log=lambda e, l: log("epoch", e, l))
     train_secs = time.perf_counter() - t1
+    # error on (up to) 64 training fields, the same metric as on the held-out cases
+    sub_idx = keep[:64]
+    p_tr, _ = ws.predict(net, [train_cases[i] for i in sub_idx])
+    train_err = [ws.field_error(train_cases[i], p, fields[i]) for i, p in zip(sub_idx, p_tr)]
     del X, Y, M
     preds, pred_secs = ws.predict(net, test_cases)
     sp, ref, secs_plain, rp = ws.solve(test_cases, None, max_steps=args.ws_max_steps, precision="f64_fast")
@@ -303,6 +307,7 @@ def run_warmstart(args):
             "steps_ratio_total": float(sp[both].sum() / sw[both].sum()) if np.any(both) else None,
             "converged": {"plain": int(np.sum(sp > 0)), "warm": int(np.sum(sw > 0)), "both": int(np.sum(both)),
                           "diverged_plain": int(np.sum(sp == -2))},
+            "surrogate_u_error_train": float(np.median(train_err)),
             "surrogate_u_error": {"median": float(np.median(errs)) if errs else None,
                                   "p90": float(np.percentile(errs, 90)) if errs else None, "by_kind": by_kind},
             "steps_ratio_when_error_below_0.2": {"cases": int(good.sum()),
