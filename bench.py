@@ -393,7 +393,9 @@ def run_batch(args):
                          "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": kind,
                          "bytes_per_cell_update": 2 * q * es},
             "looped_single_domain": {"value": round(looped, 3), "unit": "MLUPS", "launches_per_step": args.domains},
-            "clocks": clk.summary(), "gpu_launches": args.steps}
+            "clocks": clk.summary(),
+            # chunk kernel + wall-cell kernel per step (every cavity has walls)
+            "gpu_launches": 2 * args.steps}
     print(json.dumps(line), flush=True)
     batch.close()
     return 0
