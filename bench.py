@@ -38,11 +38,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 LATTICE_Q = {"D2Q9": 9, "D3Q15": 15, "D3Q19": 19, "D3Q27": 27}
-ELEM = {"f64": 8, "f64_fast": 8, "f32": 4, "f16s": 2, "bf16s": 2, "f64x": 8, "i16s": 2}
+ELEM = {"f64": 8, "f64_fast": 8, "f32": 4, "f16s": 2, "bf16s": 2, "f64x": 8}
 DTYPE = {"f64": "f64", "f64_fast": "f64", "f32": "f32", "f16s": "f16 storage / f32 arithmetic",
          "bf16s": "bf16 storage / f32 arithmetic",
-         "f64x": "int64 fixed point (f/w in units of 2^-56), FP64-accurate",
-         "i16s": "int16 fixed point of (f-w)/w (2^-16) / f32 arithmetic"}
+         "f64x": "int64 fixed point (f/w in units of 2^-56), FP64-accurate"}
 METRIC = "MLUPS"
 
 
@@ -179,7 +178,7 @@ def run_tgv3d(args):
     every, total = args.every, args.tgv_steps
     rho, u = tgv3d_fields(n, u0)
     N = n ** 3
-    names = [args.tgv_ref, "f16s", "bf16s", "i16s"]
+    names = [args.tgv_ref, "f16s", "bf16s"]
     sims = {}
     for p in names:
         s = m.Simulation(m.make_desc("D3Q27", (n, n, n), 1.0 / tau, precision=p))
@@ -211,7 +210,7 @@ def run_tgv3d(args):
         table.append(row)
         print(json.dumps({"progress": row}), file=sys.stderr, flush=True)
     mlups = {p: N * total / (ms[p] / 1e3) / 1e6 for p in names}
-    bytes_cell = {"f64x": 432, "f64": 432, "f64_fast": 432, "f32": 216, "f16s": 108, "bf16s": 108, "i16s": 108}
+    bytes_cell = {"f64x": 432, "f64": 432, "f64_fast": 432, "f32": 216, "f16s": 108, "bf16s": 108}
     peak, kind = peaks()
     last = table[-1]
     line = {"metric": "velocity L2 error vs FP64-accurate reference (and MLUPS)",

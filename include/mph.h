@@ -70,11 +70,6 @@ extern "C" {
  * whose FP64 pipes run at 1/64 of the FP32 rate.  Conversions to FP64 happen
  * only in mph_set_f / mph_get_f / moments / sums. */
 #define MPH_PREC_F64X 5
-/* 16-bit fixed point of (f_n - w_n) / w_n (resolution 2^-16, range (-1/2, 1/2),
- * i.e. |u| up to about 0.12), FP32 collide: the bandwidth of FP16 storage with
- * ~8x finer steps at the deviations a low-Mach flow carries; a value outside
- * the range reports MPH_ERR_NONFINITE after the step.  Single domains. */
-#define MPH_PREC_I16S 6
 
 /* ---- lattice-unit description of one domain ---------------------------- */
 typedef struct {

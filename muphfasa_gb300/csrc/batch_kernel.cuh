@@ -95,10 +95,10 @@ __global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __rest
             for (int n = 0; n < Q; ++n) {
                 const unsigned e = (unsigned)n * N + (unsigned)ca[j];
                 if (okb[j] && (e & 1u) == 0) {
-                    St::template str2<Q>(fout, n, e, g[j][n]);
+                    St::str2(fout, e, g[j][n]);
                 } else {
-                    St::template str1<Q>(fout, n, e, g[j][n].x);
-                    if (okb[j]) St::template str1<Q>(fout, n, e + 1, g[j][n].y);
+                    St::str1(fout, e, g[j][n].x);
+                    if (okb[j]) St::str1(fout, e + 1, g[j][n].y);
                 }
             }
         }

@@ -38,7 +38,6 @@ cudaError_t with_store(int prec, F&& f) {
         case MPH_PREC_F16S: return f(StF16S{});
         case MPH_PREC_BF16S: return f(StBF16S{});
         case MPH_PREC_F64X: return f(StF64X{});
-        case MPH_PREC_I16S: return f(StI16S{});
     }
     return cudaErrorInvalidValue;
 }
@@ -327,18 +326,6 @@ cudaError_t launch_batch_exact(int q, bool forced, int K, bool persistent, const
                                const int2* walls, int nwalls, const KParams* dp, const long long* offs,
                                cudaStream_t s) {
     return launch_batch_t<StF64, kExact>(q, forced, K, persistent, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
-}
-
-// Range flag of the 16-bit fixed-point stores made by this translation unit
-// (initialisation, conversions from FP64).
-int i16_range_flag_exact(bool reset) {
-    int v = 0;
-    if (cudaMemcpyFromSymbol(&v, g_range16, sizeof(int)) != cudaSuccess) return -1;
-    if (reset && v) {
-        const int z = 0;
-        if (cudaMemcpyToSymbol(g_range16, &z, sizeof(int)) != cudaSuccess) return -1;
-    }
-    return v;
 }
 
 }  // namespace mph

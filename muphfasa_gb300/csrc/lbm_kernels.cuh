@@ -124,16 +124,12 @@ struct StF16S {
     // Shifted kernels work on g = f - w directly: one value (ldr1/str1) or an
     // aligned pair of neighbouring cells (ldr2/str2, e even).
     static constexpr bool kShift = true;
-    template <int Q> static __device__ __forceinline__ float ldr1(const T* __restrict__ f, int, unsigned e) {
-        return __half2float(f[e]);
-    }
-    template <int Q> static __device__ __forceinline__ float2 ldr2(const T* __restrict__ f, int, unsigned e) {
+    static __device__ __forceinline__ float ldr1(const T* __restrict__ f, unsigned e) { return __half2float(f[e]); }
+    static __device__ __forceinline__ float2 ldr2(const T* __restrict__ f, unsigned e) {
         return __half22float2(*reinterpret_cast<const __half2*>(f + e));
     }
-    template <int Q> static __device__ __forceinline__ void str1(T* __restrict__ f, int, unsigned e, float v) {
-        f[e] = __float2half_rn(v);
-    }
-    template <int Q> static __device__ __forceinline__ void str2(T* __restrict__ f, int, unsigned e, float2 v) {
+    static __device__ __forceinline__ void str1(T* __restrict__ f, unsigned e, float v) { f[e] = __float2half_rn(v); }
+    static __device__ __forceinline__ void str2(T* __restrict__ f, unsigned e, float2 v) {
         *reinterpret_cast<__half2*>(f + e) = __floats2half2_rn(v.x, v.y);
     }
     template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int n, unsigned e) {
@@ -157,17 +153,15 @@ struct StBF16S {
     using R = float;
     static constexpr bool kShift = true;
     // bf16 is the high half of an FP32 word: widening is a shift / mask.
-    template <int Q> static __device__ __forceinline__ float ldr1(const T* __restrict__ f, int, unsigned e) {
+    static __device__ __forceinline__ float ldr1(const T* __restrict__ f, unsigned e) {
         return __uint_as_float((unsigned)__ldg(reinterpret_cast<const unsigned short*>(f) + e) << 16);
     }
-    template <int Q> static __device__ __forceinline__ float2 ldr2(const T* __restrict__ f, int, unsigned e) {
+    static __device__ __forceinline__ float2 ldr2(const T* __restrict__ f, unsigned e) {
         const unsigned w = __ldg(reinterpret_cast<const unsigned*>(f + e));
         return make_float2(__uint_as_float(w << 16), __uint_as_float(w & 0xffff0000u));
     }
-    template <int Q> static __device__ __forceinline__ void str1(T* __restrict__ f, int, unsigned e, float v) {
-        f[e] = __float2bfloat16_rn(v);
-    }
-    template <int Q> static __device__ __forceinline__ void str2(T* __restrict__ f, int, unsigned e, float2 v) {
+    static __device__ __forceinline__ void str1(T* __restrict__ f, unsigned e, float v) { f[e] = __float2bfloat16_rn(v); }
+    static __device__ __forceinline__ void str2(T* __restrict__ f, unsigned e, float2 v) {
         *reinterpret_cast<__nv_bfloat162*>(f + e) = __floats2bfloat162_rn(v.x, v.y);
     }
     template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int n, unsigned e) {
@@ -184,64 +178,6 @@ struct StBF16S {
     }
     template <int Q> static __device__ __forceinline__ R rt(int n, R v) {
         return __bfloat162float(__float2bfloat16_rn(v - (float)Lat<Q>::w(n))) + (float)Lat<Q>::w(n);
-    }
-};
-
-// 16-bit fixed point of the relative deviation (MPH_PREC_I16S): stored
-// s_n = round((f_n - w_n) / w_n * 2^16), i.e. |f / w - 1| < 1/2 with a
-// resolution of 2^-16 (FP16 keeps 11 significant bits of f - w, about 2^-13 of
-// the deviation at u ~ 0.05).  Decoding g = s w 2^-16 is one FP32 multiply;
-// encoding rounds g w^-1 2^16 (w^-1 2^16 is exact in FP32).  A value outside
-// the range saturates and raises g_range16 (one per translation unit; the host
-// reads them after a step and reports MPH_ERR_NONFINITE).
-static __device__ int g_range16 = 0;
-
-struct StI16S {
-    using T = short;
-    using R = float;
-    static constexpr bool kShift = true;
-    template <int Q> static __device__ __forceinline__ float dec(int n) { return (float)Lat<Q>::w(n) * 0x1p-16f; }
-    template <int Q> static __device__ __forceinline__ float enc(int n) { return (float)(Lat<Q>::iw(n) * 65536.0); }
-    static __device__ __forceinline__ int quant(float h) {
-        const float r = rintf(h);
-        if (!(fabsf(r) <= 32767.f)) {
-            atomicOr(&g_range16, 1);
-            return r > 0.f ? 32767 : -32767;
-        }
-        return (int)r;
-    }
-    template <int Q> static __device__ __forceinline__ float ldr1(const T* __restrict__ f, int n, unsigned e) {
-        return (float)__ldg(f + e) * dec<Q>(n);
-    }
-    template <int Q> static __device__ __forceinline__ float2 ldr2(const T* __restrict__ f, int n, unsigned e) {
-        const unsigned w = __ldg(reinterpret_cast<const unsigned*>(f + e));
-        const float d = dec<Q>(n);
-        return make_float2((float)(short)(w & 0xffffu) * d, (float)(short)(w >> 16) * d);
-    }
-    template <int Q> static __device__ __forceinline__ void str1(T* __restrict__ f, int n, unsigned e, float v) {
-        f[e] = (short)quant(v * enc<Q>(n));
-    }
-    template <int Q> static __device__ __forceinline__ void str2(T* __restrict__ f, int n, unsigned e, float2 v) {
-        const float k = enc<Q>(n);
-        const unsigned lo = (unsigned)quant(v.x * k) & 0xffffu, hi = (unsigned)quant(v.y * k) << 16;
-        *reinterpret_cast<unsigned*>(f + e) = lo | hi;
-    }
-    template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int n, unsigned e) {
-        return ldr1<Q>(f, n, e) + (float)Lat<Q>::w(n);
-    }
-    template <int Q> static __device__ __forceinline__ void ste(T* __restrict__ f, int n, unsigned e, R v) {
-        str1<Q>(f, n, e, v - (float)Lat<Q>::w(n));
-    }
-    template <int Q> static __device__ __forceinline__ R ld(const T* __restrict__ f, int n, long long i, long long N) {
-        return (float)__ldg(f + n * N + i) * dec<Q>(n) + (float)Lat<Q>::w(n);
-    }
-    template <int Q> static __device__ __forceinline__ void st(T* __restrict__ f, int n, long long i, long long N, R v) {
-        f[n * N + i] = (short)quant((v - (float)Lat<Q>::w(n)) * enc<Q>(n));
-    }
-    template <int Q> static __device__ __forceinline__ R rt(int n, R v) {
-        float r = rintf((v - (float)Lat<Q>::w(n)) * enc<Q>(n));
-        r = fminf(fmaxf(r, -32767.f), 32767.f);
-        return r * dec<Q>(n) + (float)Lat<Q>::w(n);
     }
 };
 
@@ -424,7 +360,7 @@ __device__ __forceinline__ void pull_shift_interior(const KParams& p, const type
     const Nbr o = neighbours<L::D>(p, x, y, z);
     const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
 #pragma unroll
-    for (int n = 0; n < Q; ++n) g[n] = St::template ldr1<Q>(fin, n, (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(o, n)));
+    for (int n = 0; n < Q; ++n) g[n] = St::ldr1(fin, (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(o, n)));
 }
 
 // Pull of all Q populations into f.  Cells away from non-periodic faces use
@@ -753,7 +689,7 @@ __device__ __forceinline__ void pull_shift(const KParams& p, const KParams* __re
     if (!o.wall && !(p.cls && p.cls[c] != kFluid)) {
         const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
 #pragma unroll
-        for (int n = 0; n < Q; ++n) g[n] = St::template ldr1<Q>(fin, n, (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(o, n)));
+        for (int n = 0; n < Q; ++n) g[n] = St::ldr1(fin, (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(o, n)));
     } else {
         pull_edge<Q, St>(p, pg, fin, x, y, z, c, g);
 #pragma unroll
@@ -772,7 +708,7 @@ __device__ __forceinline__ void step_cell(const KParams& p, const KParams* __res
     if (p.cls && p.cls[c] == kSolid) {  // obstacle cell: rest state f = w
 #pragma unroll
         for (int n = 0; n < Q; ++n) {
-            if constexpr (St::kShift) St::template str1<Q>(fout, n, (unsigned)n * N + ci, 0.0f);
+            if constexpr (St::kShift) St::str1(fout, (unsigned)n * N + ci, 0.0f);
             else St::template ste<Q>(fout, n, (unsigned)n * N + ci, (typename St::R)Lat<Q>::w(n));
         }
         return;
@@ -782,7 +718,7 @@ __device__ __forceinline__ void step_cell(const KParams& p, const KParams* __res
         pull_shift<Q, St>(p, pg, fin, x, y, z, c, g);
         collide_shift<Q, A1, FORCED>(p, g);
 #pragma unroll
-        for (int n = 0; n < Q; ++n) St::template str1<Q>(fout, n, (unsigned)n * N + ci, g[n]);
+        for (int n = 0; n < Q; ++n) St::str1(fout, (unsigned)n * N + ci, g[n]);
     } else {
         R f[Q];
         pull<Q, St>(p, pg, fin, x, y, z, c, f);
@@ -834,10 +770,10 @@ __global__ void __launch_bounds__(256, 3) k_step_pair(const typename St::T* __re
         for (int n = 0; n < Q; ++n) {
             const unsigned ea = (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(oa, n));
             if (L::cx(n) == 0) {
-                g[n] = St::template ldr2<Q>(fin, n, ea);
+                g[n] = St::ldr2(fin, ea);
             } else {
                 const unsigned eb = (unsigned)n * N + (unsigned)((int)ci + 1 + upstream<Q>(ob, n));
-                g[n] = make_float2(St::template ldr1<Q>(fin, n, ea), St::template ldr1<Q>(fin, n, eb));
+                g[n] = make_float2(St::ldr1(fin, ea), St::ldr1(fin, eb));
             }
         }
     } else {
@@ -849,7 +785,7 @@ __global__ void __launch_bounds__(256, 3) k_step_pair(const typename St::T* __re
     }
     collide_shift<Q, A2, FORCED>(p, g);
 #pragma unroll
-    for (int n = 0; n < Q; ++n) St::template str2<Q>(fout, n, (unsigned)n * N + ci, g[n]);
+    for (int n = 0; n < Q; ++n) St::str2(fout, (unsigned)n * N + ci, g[n]);
 }
 
 // updateMacroscopic (SimulationSetup.cpp:142-166): moments of the streamed

@@ -83,12 +83,4 @@ cudaError_t launch_step_f64x_pipe(int q, bool forced, const long long* fin, long
 cudaError_t launch_residual(int prec, int q, const void* f, long long ncell, double* uprev, bool first, double* part,
                             int nblocks, double* out2, cudaStream_t s);
 
-// ---- k_fast_i16.cu / k_f64_exact.cu: 16-bit fixed point ------------------
-cudaError_t launch_step_fast_i16s(int q, bool forced, const void* fin, void* fout, const KParams& p,
-                                  const KParams* pg, cudaStream_t s);
-// 1 when a 16-bit fixed-point store of that translation unit saturated, -1 on
-// a CUDA error; reset clears it.
-int i16_range_flag_step(bool reset);
-int i16_range_flag_exact(bool reset);
-
 }  // namespace mph

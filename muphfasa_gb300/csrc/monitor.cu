@@ -136,7 +136,6 @@ cudaError_t mon_with_store(int prec, F&& f) {
         case MPH_PREC_F16S: return f(StF16S{});
         case MPH_PREC_BF16S: return f(StBF16S{});
         case MPH_PREC_F64X: return f(StF64X{});
-        case MPH_PREC_I16S: return f(StI16S{});
     }
     return cudaErrorInvalidValue;
 }

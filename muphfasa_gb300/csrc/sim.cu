@@ -63,8 +63,7 @@ size_t elem_size(int prec) {
         case MPH_PREC_F64X: return 8;
         case MPH_PREC_F32: return 4;
         case MPH_PREC_F16S:
-        case MPH_PREC_BF16S:
-        case MPH_PREC_I16S: return 2;
+        case MPH_PREC_BF16S: return 2;
     }
     return 0;
 }
@@ -282,8 +281,6 @@ cudaError_t launch_one_step(mph_sim* s) {
             return launch_step_fast_f16s(q, forced, s->fa, s->fb, s->kp, s->d_kp, s->stream);
         case MPH_PREC_BF16S:
             return launch_step_fast_bf16s(q, forced, s->fa, s->fb, s->kp, s->d_kp, s->stream);
-        case MPH_PREC_I16S:
-            return launch_step_fast_i16s(q, forced, s->fa, s->fb, s->kp, s->d_kp, s->stream);
         case MPH_PREC_F64X:
             if (s->pipe_ctas > 0)
                 return launch_step_f64x_pipe(q, forced, (const long long*)s->fa, (long long*)s->fb, s->kp, s->kpx,
@@ -296,15 +293,6 @@ cudaError_t launch_one_step(mph_sim* s) {
 
 // Range flag of the fixed-point step: a cell left the representable range.
 int check_flag(mph_sim* s) {
-    if (s->d.precision == MPH_PREC_I16S) {
-        MPH_CK(cudaStreamSynchronize(s->stream), "read flag");
-        const int a = i16_range_flag_step(true), b = i16_range_flag_exact(true);
-        if (a < 0 || b < 0) return fail(MPH_ERR_CUDA, "reading the 16-bit range flag");
-        if (a || b)
-            return fail(MPH_ERR_NONFINITE, "16-bit fixed-point storage: a population left (1/2, 3/2) w "
-                                           "(|u| too large for this storage)");
-        return MPH_OK;
-    }
     if (s->d.precision != MPH_PREC_F64X) return MPH_OK;
     int flag = 0;
     MPH_CK(cudaMemcpyAsync(&flag, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "read flag");

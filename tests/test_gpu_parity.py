@@ -159,21 +159,6 @@ def test_f64x_pipelined_kernel_equals_direct_kernel(case, mph, monkeypatch):
     assert np.array_equal(out[0], out[1])
 
 
-def test_i16s_range_flag_reports_saturation(mph):
-    """A flow too fast for the 16-bit fixed point (|f / w - 1| >= 1/2) is
-    reported as MPH_ERR_NONFINITE, and a fresh in-range handle runs clean."""
-    d = mph.make_desc("D2Q9", (16, 16), 1.2, precision="i16s")
-    s = mph.Simulation(d)
-    N = 256
-    s.initialize(np.ones(N), np.concatenate([np.full(N, 0.3), np.zeros(N)]))
-    with pytest.raises(mph.MphError) as e:
-        s.advance(1)
-    assert e.value.code == 6
-    ok = mph.Simulation(d)
-    ok.initialize(np.ones(N), np.concatenate([np.full(N, 0.02), np.zeros(N)]))
-    ok.advance(10)
-
-
 def test_f64x_range_flag_reports_instead_of_wrapping(mph):
     """Fault injection on the host: a near-vacuum state (rho = 1e-3, below the
     fixed-point range) makes the step report MPH_ERR_NONFINITE."""
@@ -191,10 +176,10 @@ def test_f64x_range_flag_reports_instead_of_wrapping(mph):
 # from a random (non-smooth) field.  Plain FP32 storage rounds f ~ w to 24 bits
 # (measured 3e-6..8e-5); shifted FP16 / BF16 keep 11 / 8 bits of f - w
 # (measured 2e-4..7e-4 / 1.4e-3..3.2e-3).
-TOL_LOWP = {"f32": 3e-4, "f16s": 3e-3, "bf16s": 1.5e-2, "i16s": 1e-3}
+TOL_LOWP = {"f32": 3e-4, "f16s": 3e-3, "bf16s": 1.5e-2}
 
 
-@pytest.mark.parametrize("prec", ["f32", "f16s", "bf16s", "i16s"])
+@pytest.mark.parametrize("prec", ["f32", "f16s", "bf16s"])
 @pytest.mark.parametrize("case", LONG[:3], ids=[f"{c[0]}_{c[6]}" for c in LONG[:3]])
 def test_reduced_precision_velocity_error(case, prec, mph, oracle_mod):
     lat, n, faces, omega, force, U, steps = case
@@ -203,8 +188,7 @@ def test_reduced_precision_velocity_error(case, prec, mph, oracle_mod):
         face_U[k] = v
     o, s = _pair(mph, oracle_mod, lat, n, faces, omega, force, face_U, precision=prec)
     rng = np.random.default_rng(13)
-    # the 16-bit fixed point holds |f / w - 1| < 1/2: a gentler random field
-    rho, u = _fields(rng, o.N, o.cfg.dim, amp=0.01 if prec == "i16s" else 0.02)
+    rho, u = _fields(rng, o.N, o.cfg.dim, amp=0.02)
     o.init_fields(rho, u)
     s.initialize(rho, u)
     steps = min(steps, 200)
