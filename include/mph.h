@@ -302,8 +302,9 @@ int mph_nn_sync(void* stream);
 int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const void* B, long long ldb, int tb,
                 float* C, long long ldc, int accumulate, void* stream);
 /* GEMM kernel choice for later calls: 1 = mma.sync (m16n8k16) tiles, 2 =
- * tcgen05.mma with the accumulator in tensor memory (128 x 64 tiles), 0 =
- * tcgen05 for M >= 128 and N >= 16, else mma.sync. */
+ * tcgen05.mma with the accumulator in tensor memory (128 x 64 tiles, three
+ * cp.async stages), 3 = the same single-buffered, 0 = mode 2 for M >= 128 and
+ * N >= 16, else mma.sync.  Not thread-safe (process-wide setting). */
 int mph_nn_gemm_mode(int mode);
 /* Reads (and with reset != 0 clears) the flag the tcgen05 GEMM sets when a
  * bounded wait for its tensor-core work runs out. */

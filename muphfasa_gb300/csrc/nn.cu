@@ -310,6 +310,190 @@ __global__ void __launch_bounds__(128) k_gemm_tc05(int M, int N, int K, const bf
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_BN));
 }
 
+// Pipelined variant: three shared-memory stages of 32-wide K slices.  Rows
+// that are K-contiguous and 16-byte aligned arrive by cp.async (16 bytes per
+// core-matrix row), others by plain loads; while the tensor core works on
+// slice t the threads fill slice t + 2.  Each stage's mbarrier is waited on
+// (bounded) before the stage is refilled, and the last commit before the
+// accumulator is read.
+constexpr int TP_BK = 32, TP_STAGES = 3;
+constexpr int TP_A_BYTES = TC_BM * TP_BK * 2, TP_B_BYTES = TC_BN * TP_BK * 2;
+
+__device__ __forceinline__ unsigned cm_off32(int row, int k) {
+    return (unsigned)((((row >> 3) * (TP_BK / 8) + (k >> 3)) << 7) + ((row & 7) << 4) + ((k & 7) << 1));
+}
+
+__device__ __forceinline__ unsigned long long smem_desc32(unsigned addr) {
+    const unsigned long long lbo = 128 >> 4, sbo = ((TP_BK / 8) * 128) >> 4;
+    return (unsigned long long)((addr >> 4) & 0x3FFF) | (lbo << 16) | (sbo << 32) | (1ull << 46);
+}
+
+// One rows x 32 K slice of an operand into stage memory `dst`.
+template <bool T, int ROWS>
+__device__ __forceinline__ void tp_stage(unsigned char* dst, const bf16* __restrict__ X, long long ld, long long r0,
+                                         long long rmax, int k0, int ke, bool vec_ok) {
+    const bf16 zero = __float2bfloat16(0.f);
+    for (int ch = threadIdx.x; ch < ROWS * (TP_BK / 8); ch += 128) {
+        const int row = ch % ROWS, kc = ch / ROWS;
+        const long long gr = r0 + row;
+        const int gk0 = k0 + kc * 8;
+        unsigned char* d = dst + cm_off32(row, kc * 8);
+        if (!T && vec_ok && gr < rmax && gk0 + 8 <= ke && ((gr * ld + gk0) & 7) == 0) {
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(d)), "l"(X + gr * ld + gk0)
+                         : "memory");
+            continue;
+        }
+        unsigned short v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int gk = gk0 + j;
+            bf16 x = zero;
+            if (gr < rmax && gk < ke) x = T ? X[(long long)gk * ld + gr] : X[gr * ld + gk];
+            v[j] = __bfloat16_as_ushort(x);
+        }
+        uint4 w;
+        w.x = v[0] | ((unsigned)v[1] << 16);
+        w.y = v[2] | ((unsigned)v[3] << 16);
+        w.z = v[4] | ((unsigned)v[5] << 16);
+        w.w = v[6] | ((unsigned)v[7] << 16);
+        *reinterpret_cast<uint4*>(d) = w;
+    }
+}
+
+__device__ __forceinline__ bool mbar_wait(unsigned addr, unsigned phase) {
+    unsigned done = 0;
+    for (unsigned long long it = 0; it < kSpinLimit && !done; ++it) {
+        asm volatile(
+            "{\n.reg .pred q;\nmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\nselp.u32 %0, 1, 0, q;\n}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(phase));
+    }
+    return done != 0;
+}
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(128) k_gemm_tc05p(int M, int N, int K, const bf16* __restrict__ A, long long lda,
+                                                    const bf16* __restrict__ B, long long ldb, float* __restrict__ C,
+                                                    long long ldc, int accumulate, int kchunk) {
+    __shared__ __align__(1024) unsigned char As[TP_STAGES][TP_A_BYTES];
+    __shared__ __align__(1024) unsigned char Bs[TP_STAGES][TP_B_BYTES];
+    __shared__ __align__(8) unsigned long long mbar[TP_STAGES];
+    __shared__ unsigned tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long long m0 = (long long)blockIdx.y * TC_BM, n0 = (long long)blockIdx.x * TC_BN;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
+                     "r"(TC_BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    if (tid == 0) {
+        for (int s = 0; s < TP_STAGES; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[s])));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    const unsigned tmem = tmem_base;
+    const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(TC_BN >> 3) << 17) |
+                           ((unsigned)(TC_BM >> 4) << 24);
+    const bool a_vec = (reinterpret_cast<unsigned long long>(A) & 15) == 0;
+    const bool b_vec = (reinterpret_cast<unsigned long long>(B) & 15) == 0;
+    const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+    const int nk = (ke - kb + TP_BK - 1) / TP_BK;
+    C += (long long)blockIdx.z * M * ldc;
+    unsigned phase[TP_STAGES] = {0, 0, 0};
+    bool ok = true;
+    // prologue: slices 0 .. STAGES-2
+    for (int s = 0; s < TP_STAGES - 1; ++s) {
+        if (s < nk) {
+            tp_stage<TA, TC_BM>(As[s], A, lda, m0, M, kb + s * TP_BK, ke, a_vec);
+            tp_stage<TB, TC_BN>(Bs[s], B, ldb, n0, N, kb + s * TP_BK, ke, b_vec);
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    }
+    for (int t = 0; t < nk && ok; ++t) {
+        const int s = t % TP_STAGES;
+        asm volatile("cp.async.wait_group %0;\n" ::"n"(TP_STAGES - 2) : "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+        if (tid == 0) {
+#pragma unroll
+            for (int kk = 0; kk < TP_BK / 16; ++kk) {
+                const unsigned long long ad = smem_desc32(smem_u32(As[s]) + kk * 256);
+                const unsigned long long bd = smem_desc32(smem_u32(Bs[s]) + kk * 256);
+                const unsigned acc = (t > 0 || kk > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                smem_u32(&mbar[s])));
+        }
+        // refill the stage of slice t - 1 with slice t + STAGES - 1
+        const int tn = t + TP_STAGES - 1;
+        if (tn < nk) {
+            const int sn = tn % TP_STAGES;
+            if (t >= 1) {
+                if (!mbar_wait(smem_u32(&mbar[sn]), phase[sn])) {
+                    ok = false;
+                    atomicExch(&g_nn_timeout, 1);
+                }
+                phase[sn] ^= 1;
+            }
+            if (ok) {
+                tp_stage<TA, TC_BM>(As[sn], A, lda, m0, M, kb + tn * TP_BK, ke, a_vec);
+                tp_stage<TB, TC_BN>(Bs[sn], B, ldb, n0, N, kb + tn * TP_BK, ke, b_vec);
+            }
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    if (ok) {
+        const int sl = (nk - 1) % TP_STAGES;
+        if (!mbar_wait(smem_u32(&mbar[sl]), phase[sl])) {
+            ok = false;
+            atomicExch(&g_nn_timeout, 1);
+        }
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    __syncthreads();
+    if (ok) {
+        float acc[TC_BN];
+        unsigned r[TC_BN];
+        const unsigned taddr = tmem + ((unsigned)(32 * warp) << 16);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x64.b32 "
+            "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,"
+            "%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,"
+            "%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];\n"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+              "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
+              "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
+              "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
+              "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
+              "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < TC_BN; ++j) acc[j] = __uint_as_float(r[j]);
+        const long long row = m0 + 32 * warp + lane;
+        if (row < M) {
+            float* crow = C + row * ldc + n0;
+#pragma unroll
+            for (int j = 0; j < TC_BN; ++j)
+                if (n0 + j < N) crow[j] = accumulate ? crow[j] + acc[j] : acc[j];
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_BN));
+}
+
 // C[m][n] (+)= sum over splits z of W[z][m][n] (W rows of width N), in split order.
 __global__ void k_splitk_reduce(const float* __restrict__ W, int S, int M, int N, float* __restrict__ C, long long ldc,
                                 int accumulate) {
@@ -592,10 +776,11 @@ int mph_nn_sync(void* stream) {
     return MPH_OK;
 }
 
-static int g_gemm_mode = 0;  // 0 auto, 1 mma.sync, 2 tcgen05
+static int g_gemm_mode = 0;  // 0 auto, 1 mma.sync, 2 tcgen05 pipelined, 3 tcgen05 single-buffered
 
 int mph_nn_gemm_mode(int mode) {
-    if (mode < 0 || mode > 2) return mph::fail(MPH_ERR_ARG, "mph_nn_gemm_mode: 0 auto, 1 mma.sync, 2 tcgen05");
+    if (mode < 0 || mode > 3)
+        return mph::fail(MPH_ERR_ARG, "mph_nn_gemm_mode: 0 auto, 1 mma.sync, 2 tcgen05, 3 tcgen05 single-buffered");
     g_gemm_mode = mode;
     return MPH_OK;
 }
@@ -623,7 +808,7 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     auto a = static_cast<const bf16*>(A);
     auto b = static_cast<const bf16*>(B);
-    const bool tc = g_gemm_mode == 2 || (g_gemm_mode == 0 && M >= TC_BM && N >= 16);
+    const bool tc = g_gemm_mode >= 2 || (g_gemm_mode == 0 && M >= TC_BM && N >= 16);
     const int tm = tc ? TC_BM : BM, tn = tc ? TC_BN : BN;
     const long long gx = (N + tn - 1) / tn, gy = (M + tm - 1) / tm;
     if (gy > 65535) return mph::fail(MPH_ERR_ARG, "mph_nn_gemm: M too large for one launch");
@@ -660,8 +845,10 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
     else if (!ta && tb) KERN<false, true><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, out, ldo, acc, kchunk);   \
     else if (ta && !tb) KERN<true, false><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, out, ldo, acc, kchunk);   \
     else KERN<true, true><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, out, ldo, acc, kchunk);
-    if (tc) {
+    if (tc && g_gemm_mode == 3) {
         MPH_GEMM_LAUNCH(k_gemm_tc05)
+    } else if (tc) {
+        MPH_GEMM_LAUNCH(k_gemm_tc05p)
     } else {
         MPH_GEMM_LAUNCH(k_gemm_bf16)
     }

@@ -48,11 +48,11 @@ def test_gemm_layouts(ta, tb, S):
     assert np.all(np.abs(got2 - 2 * ref) <= 2e-5 * scale + 2e-6)
 
 
-@pytest.mark.parametrize("shape", [(200, 70, 100), (1024, 256, 576), (128, 64, 64)])
+@pytest.mark.parametrize("shape", [(200, 70, 100), (1024, 256, 576), (128, 64, 64), (130, 70, 32), (300, 64, 4096)])
 @pytest.mark.parametrize("ta,tb", [(0, 0), (0, 1), (1, 0), (1, 1)])
 def test_tcgen05_gemm_matches_mma_sync_and_numpy(ta, tb, shape, S):
-    """The tensor-memory GEMM (tcgen05.mma, 128 x 64 tiles) against NumPy and
-    against the mma.sync kernel."""
+    """The tensor-memory GEMMs (tcgen05.mma, 128 x 64 tiles; pipelined and
+    single-buffered) against NumPy and against the mma.sync kernel."""
     rng = np.random.default_rng(10 + ta * 2 + tb)
     M, N, K = shape
     A = NO.to_bf16(rng.standard_normal((M, K)).astype(np.float32))
@@ -61,7 +61,7 @@ def test_tcgen05_gemm_matches_mma_sync_and_numpy(ta, tb, shape, S):
     L = S._lib()
     out = {}
     try:
-        for mode in (1, 2):
+        for mode in (1, 2, 3):
             S.check(L.mph_nn_gemm_mode(mode))
             c = S._f32(M * N)
             S.check(L.mph_nn_gemm(M, N, K, da.ptr, M if ta else K, ta, db.ptr, N if tb else K, tb, c.ptr, N, 0, None))
@@ -73,8 +73,9 @@ def test_tcgen05_gemm_matches_mma_sync_and_numpy(ta, tb, shape, S):
     assert flag.value == 0
     ref = A.astype(np.float64) @ B.astype(np.float64)
     scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64)
-    assert np.all(np.abs(out[2] - ref) <= 1e-5 * scale + 1e-6)
-    assert np.all(np.abs(out[2] - out[1]) <= 2e-5 * scale + 2e-6)
+    for mode in (2, 3):
+        assert np.all(np.abs(out[mode] - ref) <= 1e-5 * scale + 1e-6), mode
+        assert np.all(np.abs(out[mode] - out[1]) <= 2e-5 * scale + 2e-6), mode
 
 
 def test_im2col_col2im_adjoint(S):
