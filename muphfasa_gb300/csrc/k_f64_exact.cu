@@ -51,6 +51,17 @@ __global__ void __launch_bounds__(256) k_convert(typename St::T* __restrict__ st
     else f64[i] = (double)St::template ld<Q>(store, n, i, N);
 }
 
+template <int Q, class St>
+__global__ void __launch_bounds__(256) k_convert_slab(typename St::T* __restrict__ store, double* __restrict__ stage,
+                                                      long long c0, long long cnt, long long N, int to_store) {
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= cnt) return;
+    const int n = blockIdx.y;
+    double* v = stage + n * cnt + j;
+    if (to_store) St::template st<Q>(store, n, c0 + j, N, (typename St::R)*v);
+    else *v = (double)St::template ld<Q>(store, n, c0 + j, N);
+}
+
 __global__ void k_reduce_final(const double* __restrict__ part, int nblocks, double* __restrict__ out) {
     // One warp per component, fixed order: deterministic.
     const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -265,6 +276,21 @@ cudaError_t launch_convert(int prec, int q, bool to_store, void* store, double* 
         return with_q(q, [&](auto qc) {
             constexpr int Q = decltype(qc)::value;
             k_convert<Q, St><<<g, b, 0, s>>>(static_cast<typename St::T*>(store), f64, n, ncell, to_store ? 1 : 0);
+            return cudaGetLastError();
+        });
+    });
+}
+
+cudaError_t launch_convert_slab(int prec, int q, bool to_store, void* store, double* stage, long long c0,
+                                long long cnt, long long ncell, cudaStream_t s) {
+    if (cnt <= 0) return cudaSuccess;
+    const dim3 g((unsigned)((cnt + 255) / 256), (unsigned)q, 1), b(256, 1, 1);
+    return with_store(prec, [&](auto st) {
+        using St = decltype(st);
+        return with_q(q, [&](auto qc) {
+            constexpr int Q = decltype(qc)::value;
+            k_convert_slab<Q, St><<<g, b, 0, s>>>(static_cast<typename St::T*>(store), stage, c0, cnt, ncell,
+                                                  to_store ? 1 : 0);
             return cudaGetLastError();
         });
     });

@@ -300,9 +300,9 @@ __global__ void __launch_bounds__(256) k_step_x(const i64* __restrict__ fin, i64
                                                 const KParamsX px, const KParams* __restrict__ pg,
                                                 const i64* __restrict__ kbb, int* __restrict__ flag) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z;
-    if (x >= p.nx || y >= p.ny) return;
+    const int y = p.y0 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = p.z0 + blockIdx.z;
+    if (x >= p.nx || y >= p.y1) return;
     const long long c = ((long long)z * p.ny + y) * p.nx + x;
     const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
     if (OBST && p.cls[c] == kSolid) {  // obstacle cell: rest state, h = f / w = 1

@@ -54,6 +54,9 @@ struct KParams {
     // cell, kFluid / kNearSolid (a fluid cell with a solid upstream cell) /
     // kSolid; nullptr when the domain has none (no extra traffic then).
     const unsigned char* cls;
+    // Window of one step launch: rows [y0, y1) of planes [z0, z1).  The full
+    // domain is (0, ny, 0, nz); a host-copy pipeline steps slabs of planes.
+    int y0, y1, z0, z1;
 };
 
 // Parameters in the compute type R of a collide.
@@ -737,9 +740,9 @@ template <int Q, class St, int ARITH, bool FORCED>
 __global__ void __launch_bounds__(256) k_step(const typename St::T* __restrict__ fin, typename St::T* __restrict__ fout,
                                               const KParams p, const KParams* __restrict__ pg) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z;
-    if (x >= p.nx || y >= p.ny) return;
+    const int y = p.y0 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = p.z0 + blockIdx.z;
+    if (x >= p.nx || y >= p.y1) return;
     step_cell<Q, St, ARITH, FORCED>(p, pg, fin, fout, x, y, z);
 }
 
@@ -753,9 +756,9 @@ __global__ void __launch_bounds__(256, 3) k_step_pair(const typename St::T* __re
                                                    const KParams* __restrict__ pg) {
     using L = Lat<Q>;
     const int x = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z;
-    if (x >= p.nx || y >= p.ny) return;
+    const int y = p.y0 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = p.z0 + blockIdx.z;
+    if (x >= p.nx || y >= p.y1) return;
     const long long c = ((long long)z * p.ny + y) * p.nx + x;
     const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
     if (p.cls && (p.cls[c] | p.cls[c + 1]) != kFluid) {  // obstacle or its neighbour: one cell at a time

@@ -11,12 +11,14 @@ namespace mph {
 
 // Block of 256 threads with lanes along x (rows of one (y, z)), grid over
 // (x-blocks, y-blocks, z).
+// Step kernels cover the window rows [y0, y1) x planes [z0, z1) of KParams;
+// other kernels (init, moments) are launched on the full domain only.
 inline void step_shape(const KParams& p, dim3& grid, dim3& block, int threads = 256) {
     int bx = ((p.nx + 31) / 32) * 32;
     if (bx > threads) bx = threads;
     const int by = threads / bx;
     block = dim3(bx, by, 1);
-    grid = dim3((p.nx + bx - 1) / bx, (p.ny + by - 1) / by, p.nz);
+    grid = dim3((p.nx + bx - 1) / bx, (p.y1 - p.y0 + by - 1) / by, p.z1 - p.z0);
 }
 
 // Plain 1-D shape over the cells.
@@ -42,6 +44,10 @@ cudaError_t launch_init_neq(int prec, int q, void* f, const double* rho, const d
                             cudaStream_t s);
 cudaError_t launch_convert(int prec, int q, bool to_store, void* store, double* f64, int n, long long ncell,
                            cudaStream_t s);
+// All Q populations of the cells [c0, c0 + cnt) between the store and an FP64
+// staging block laid out [q][cnt].
+cudaError_t launch_convert_slab(int prec, int q, bool to_store, void* store, double* stage, long long c0,
+                                long long cnt, long long ncell, cudaStream_t s);
 
 struct A4 {
     double* p;

@@ -32,6 +32,13 @@ struct mph_sim {
     double* d_stage = nullptr;  // FP64 staging of two populations (conversions)
     cudaStream_t copy_stream = nullptr;  // host copies overlapping the conversions
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_converted[2] = {nullptr, nullptr};
+    // Slab pipeline of mph_step_host: uploads on copy_stream, upload
+    // conversions and slab steps on stream, download conversions on
+    // conv_stream, downloads on d2h_stream.
+    double* d_slab = nullptr;    // FP64 staging [4][q][slab_cells]: two upload, two download blocks
+    long long slab_cells = 0;    // cells of the largest slab
+    cudaStream_t d2h_stream = nullptr, conv_stream = nullptr;
+    cudaEvent_t ev_slab[10] = {};  // up copied[2], up free[2], down converted[2], down free[2], start, stepped
     double* d_part = nullptr;   // reduction partials
     double* d_red = nullptr;    // reduction result
     double* d_uprev = nullptr;  // velocity field saved by the last mph_residual (dim x N)
@@ -87,6 +94,8 @@ void build_params(const mph_desc& d, const mph_resolved_bc* tab, KParams& kp) {
     kp.nz = d.dim == 3 ? d.n[2] : 1;
     for (int a = 0; a < 3; ++a) kp.periodic[a] = (a < d.dim) && d.face_type[2 * a] == MPH_BC_PERIODIC;
     kp.ncell = (long long)kp.nx * kp.ny * kp.nz;
+    kp.y1 = kp.ny;
+    kp.z1 = kp.nz;
     kp.omega = d.omega;
     kp.omc = 1.0 - d.omega;
     for (int a = 0; a < 3; ++a) {
@@ -244,6 +253,11 @@ void free_all(mph_sim* s) {
         if (s->ev_converted[i]) cudaEventDestroy(s->ev_converted[i]);
     }
     if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+    cudaFree(s->d_slab);
+    for (cudaEvent_t e : s->ev_slab)
+        if (e) cudaEventDestroy(e);
+    if (s->d2h_stream) cudaStreamDestroy(s->d2h_stream);
+    if (s->conv_stream) cudaStreamDestroy(s->conv_stream);
     if (s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -253,9 +267,8 @@ int ensure_macro(mph_sim* s) {
     return MPH_OK;
 }
 
-int ensure_stage(mph_sim* s) {
-    if (!s->d_stage) {
-        MPH_CK(cudaMalloc(&s->d_stage, 2 * sizeof(double) * s->kp.ncell), "cudaMalloc(stage)");
+int ensure_copy_stream(mph_sim* s) {
+    if (!s->copy_stream) {
         MPH_CK(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking), "copy stream");
         for (int i = 0; i < 2; ++i) {
             MPH_CK(cudaEventCreateWithFlags(&s->ev_copied[i], cudaEventDisableTiming), "copy event");
@@ -265,31 +278,40 @@ int ensure_stage(mph_sim* s) {
     return MPH_OK;
 }
 
+int ensure_stage(mph_sim* s) {
+    if (!s->d_stage) MPH_CK(cudaMalloc(&s->d_stage, 2 * sizeof(double) * s->kp.ncell), "cudaMalloc(stage)");
+    return ensure_copy_stream(s);
+}
+
 bool is_f64(const mph_sim* s) { return s->d.precision == MPH_PREC_F64 || s->d.precision == MPH_PREC_F64_FAST; }
 
-cudaError_t launch_one_step(mph_sim* s) {
+// One step fa -> fb over the window of kp (the whole domain, or a slab of
+// planes for the host-copy pipeline; slabs take the direct fixed-point kernel).
+cudaError_t launch_step_window(mph_sim* s, const KParams& kp, bool whole) {
     const int q = s->d.q;
     const bool forced = s->d.forced != 0;
     switch (s->d.precision) {
         case MPH_PREC_F64:
-            return launch_step_exact(q, forced, (const double*)s->fa, (double*)s->fb, s->kp, s->d_kp, s->stream);
+            return launch_step_exact(q, forced, (const double*)s->fa, (double*)s->fb, kp, s->d_kp, s->stream);
         case MPH_PREC_F64_FAST:
-            return launch_step_fast_f64(q, forced, (const double*)s->fa, (double*)s->fb, s->kp, s->d_kp, s->stream);
+            return launch_step_fast_f64(q, forced, (const double*)s->fa, (double*)s->fb, kp, s->d_kp, s->stream);
         case MPH_PREC_F32:
-            return launch_step_fast_f32(q, forced, (const float*)s->fa, (float*)s->fb, s->kp, s->d_kp, s->stream);
+            return launch_step_fast_f32(q, forced, (const float*)s->fa, (float*)s->fb, kp, s->d_kp, s->stream);
         case MPH_PREC_F16S:
-            return launch_step_fast_f16s(q, forced, s->fa, s->fb, s->kp, s->d_kp, s->stream);
+            return launch_step_fast_f16s(q, forced, s->fa, s->fb, kp, s->d_kp, s->stream);
         case MPH_PREC_BF16S:
-            return launch_step_fast_bf16s(q, forced, s->fa, s->fb, s->kp, s->d_kp, s->stream);
+            return launch_step_fast_bf16s(q, forced, s->fa, s->fb, kp, s->d_kp, s->stream);
         case MPH_PREC_F64X:
-            if (s->pipe_ctas > 0)
-                return launch_step_f64x_pipe(q, forced, (const long long*)s->fa, (long long*)s->fb, s->kp, s->kpx,
+            if (whole && s->pipe_ctas > 0)
+                return launch_step_f64x_pipe(q, forced, (const long long*)s->fa, (long long*)s->fb, kp, s->kpx,
                                              s->d_kp, s->d_kbb, s->d_flag, s->pipe_ctas, s->stream);
-            return launch_step_f64x(q, forced, (const long long*)s->fa, (long long*)s->fb, s->kp, s->kpx, s->d_kp,
+            return launch_step_f64x(q, forced, (const long long*)s->fa, (long long*)s->fb, kp, s->kpx, s->d_kp,
                                     s->d_kbb, s->d_flag, s->stream);
     }
     return cudaErrorInvalidValue;
 }
+
+cudaError_t launch_one_step(mph_sim* s) { return launch_step_window(s, s->kp, true); }
 
 // Range flag of the fixed-point step: a cell left the representable range.
 int check_flag(mph_sim* s) {
@@ -365,6 +387,166 @@ int download(mph_sim* s, double* f) {
         MPH_CK(cudaEventRecord(s->ev_copied[b], s->copy_stream), "download order");
     }
     MPH_CK(cudaStreamWaitEvent(s->stream, s->ev_copied[(s->d.q - 1) & 1], 0), "download order");
+    return MPH_OK;
+}
+
+// ---- host-copy pipeline of mph_step_host ------------------------------
+// The domain is cut into S slabs of whole planes of its outermost axis (z in
+// 3-D, y in 2-D); a slab's populations are q contiguous runs of the SoA
+// arrays.  Uploads run in the order S-1, 0, 1, ..., S-2 on copy_stream; slab
+// k steps once slabs k-1, k, k+1 are resident (the pull reaches one plane),
+// and its result goes back on d2h_stream while later slabs still upload, so
+// the two copy directions overlap each other and the kernels.  Download
+// conversions run on their own stream: a download waiting for a free staging
+// block never holds up the uploads.  Slabs touch disjoint host ranges, so
+// f_in may alias f_out.
+int slab_count(const mph_sim* s) {
+    const int E = s->d.dim == 3 ? s->kp.nz : s->kp.ny;
+    if ((long long)s->d.q * s->kp.ncell * 8 < (32LL << 20) || E < 3) return 0;  // small: one block copy
+    return E < 32 ? E : 32;
+}
+
+void slab_window(const mph_sim* s, int k, int S, KParams& w, long long& c0, long long& cnt) {
+    const bool d3 = s->d.dim == 3;
+    const int E = d3 ? s->kp.nz : s->kp.ny;
+    const long long plane = d3 ? (long long)s->kp.nx * s->kp.ny : s->kp.nx;
+    const int a = (int)((long long)k * E / S), b = (int)((long long)(k + 1) * E / S);
+    w = s->kp;
+    if (d3) { w.z0 = a; w.z1 = b; }
+    else { w.y0 = a; w.y1 = b; }
+    c0 = a * plane;
+    cnt = (b - a) * plane;
+}
+
+int ensure_slabs(mph_sim* s, int S) {
+    int rc = ensure_copy_stream(s);
+    if (rc) return rc;
+    if (!s->d2h_stream) {
+        MPH_CK(cudaStreamCreateWithFlags(&s->d2h_stream, cudaStreamNonBlocking), "d2h stream");
+        MPH_CK(cudaStreamCreateWithFlags(&s->conv_stream, cudaStreamNonBlocking), "conversion stream");
+        for (cudaEvent_t& e : s->ev_slab) MPH_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "slab event");
+    }
+    const int E = s->d.dim == 3 ? s->kp.nz : s->kp.ny;
+    const long long plane = s->kp.ncell / E;
+    const long long cells = ((E + S - 1) / S) * plane;
+    if (!is_f64(s) && cells > s->slab_cells) {
+        cudaFree(s->d_slab);
+        s->d_slab = nullptr;
+        s->slab_cells = 0;
+        MPH_CK(cudaMalloc(&s->d_slab, 4 * sizeof(double) * s->d.q * cells), "cudaMalloc(slab stage)");
+        s->slab_cells = cells;
+    }
+    return MPH_OK;
+}
+
+int slab_up(mph_sim* s, const double* f, int k, int S, int b) {
+    KParams w;
+    long long c0, cnt;
+    slab_window(s, k, S, w, c0, cnt);
+    const long long N = s->kp.ncell;
+    cudaEvent_t copied = s->ev_slab[b], freed = s->ev_slab[2 + b];
+    if (is_f64(s)) {
+        for (int n = 0; n < s->d.q; ++n)
+            MPH_CK(cudaMemcpyAsync((double*)s->fa + n * N + c0, f + n * N + c0, sizeof(double) * cnt,
+                                   cudaMemcpyHostToDevice, s->copy_stream), "upload slab");
+        MPH_CK(cudaEventRecord(copied, s->copy_stream), "upload order");
+        MPH_CK(cudaStreamWaitEvent(s->stream, copied, 0), "upload order");
+        return MPH_OK;
+    }
+    double* st = s->d_slab + (size_t)b * s->d.q * s->slab_cells;
+    MPH_CK(cudaStreamWaitEvent(s->copy_stream, freed, 0), "upload order");
+    for (int n = 0; n < s->d.q; ++n)
+        MPH_CK(cudaMemcpyAsync(st + n * cnt, f + n * N + c0, sizeof(double) * cnt, cudaMemcpyHostToDevice,
+                               s->copy_stream), "upload slab");
+    MPH_CK(cudaEventRecord(copied, s->copy_stream), "upload order");
+    MPH_CK(cudaStreamWaitEvent(s->stream, copied, 0), "upload order");
+    MPH_CK(launch_convert_slab(s->d.precision, s->d.q, true, s->fa, st, c0, cnt, N, s->stream), "convert slab");
+    MPH_CK(cudaEventRecord(freed, s->stream), "upload order");
+    return MPH_OK;
+}
+
+// Result of slab k, in fb, to the host.
+int slab_down(mph_sim* s, double* f, int k, int S, int b) {
+    KParams w;
+    long long c0, cnt;
+    slab_window(s, k, S, w, c0, cnt);
+    const long long N = s->kp.ncell;
+    cudaEvent_t converted = s->ev_slab[4 + b], freed = s->ev_slab[6 + b];
+    if (is_f64(s)) {
+        MPH_CK(cudaEventRecord(converted, s->stream), "download order");
+        MPH_CK(cudaStreamWaitEvent(s->d2h_stream, converted, 0), "download order");
+        for (int n = 0; n < s->d.q; ++n)
+            MPH_CK(cudaMemcpyAsync(f + n * N + c0, (const double*)s->fb + n * N + c0, sizeof(double) * cnt,
+                                   cudaMemcpyDeviceToHost, s->d2h_stream), "download slab");
+        MPH_CK(cudaEventRecord(freed, s->d2h_stream), "download order");
+        return MPH_OK;
+    }
+    double* st = s->d_slab + (size_t)(2 + b) * s->d.q * s->slab_cells;
+    MPH_CK(cudaEventRecord(s->ev_slab[9], s->stream), "download order");  // slab k stepped
+    MPH_CK(cudaStreamWaitEvent(s->conv_stream, s->ev_slab[9], 0), "download order");
+    MPH_CK(cudaStreamWaitEvent(s->conv_stream, freed, 0), "download order");
+    MPH_CK(launch_convert_slab(s->d.precision, s->d.q, false, s->fb, st, c0, cnt, N, s->conv_stream),
+           "convert slab");
+    MPH_CK(cudaEventRecord(converted, s->conv_stream), "download order");
+    MPH_CK(cudaStreamWaitEvent(s->d2h_stream, converted, 0), "download order");
+    for (int n = 0; n < s->d.q; ++n)
+        MPH_CK(cudaMemcpyAsync(f + n * N + c0, st + n * cnt, sizeof(double) * cnt, cudaMemcpyDeviceToHost,
+                               s->d2h_stream), "download slab");
+    MPH_CK(cudaEventRecord(freed, s->d2h_stream), "download order");
+    return MPH_OK;
+}
+
+int slab_step(mph_sim* s, int k, int S) {
+    KParams w;
+    long long c0, cnt;
+    slab_window(s, k, S, w, c0, cnt);
+    MPH_CK(launch_step_window(s, w, false), "slab step launch");
+    return MPH_OK;
+}
+
+// mph_step_host with nsteps >= 1 over S >= 3 slabs: the first step runs slab
+// by slab behind the uploads, the last slab by slab ahead of the downloads.
+int step_host_slabs(mph_sim* s, const double* f_in, double* f_out, int nsteps, int S) {
+    int rc = ensure_slabs(s, S);
+    if (rc) return rc;
+    cudaEvent_t start = s->ev_slab[8];
+    // Earlier work on the handle's stream comes first; both staging pairs start free.
+    MPH_CK(cudaEventRecord(start, s->stream), "pipeline order");
+    MPH_CK(cudaStreamWaitEvent(s->copy_stream, start, 0), "pipeline order");
+    MPH_CK(cudaStreamWaitEvent(s->d2h_stream, start, 0), "pipeline order");
+    for (int b = 0; b < 2; ++b) {
+        MPH_CK(cudaEventRecord(s->ev_slab[2 + b], s->stream), "pipeline order");
+        MPH_CK(cudaEventRecord(s->ev_slab[6 + b], s->d2h_stream), "pipeline order");
+    }
+    const bool one = nsteps == 1;
+    int nd = 0;  // downloads issued (staging block nd % 2)
+    auto step_and_send = [&](int k) {
+        int r = slab_step(s, k, S);
+        if (!r && one) r = slab_down(s, f_out, k, S, nd++ & 1);
+        return r;
+    };
+    // Step 1 behind the uploads S-1, 0, 1, ..., S-2.
+    for (int i = 0; i < S; ++i) {
+        const int k = i == 0 ? S - 1 : i - 1;
+        if ((rc = slab_up(s, f_in, k, S, i & 1))) return rc;
+        if (i >= 2 && (rc = step_and_send(i - 2))) return rc;
+    }
+    if ((rc = step_and_send(S - 2)) || (rc = step_and_send(S - 1))) return rc;
+    std::swap(s->fa, s->fb);
+    if (!one) {
+        for (int t = 1; t < nsteps - 1; ++t) {
+            cudaError_t e = launch_one_step(s);
+            if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
+            std::swap(s->fa, s->fb);
+        }
+        for (int k = 0; k < S; ++k) {
+            if ((rc = slab_step(s, k, S)) || (rc = slab_down(s, f_out, k, S, nd++ & 1))) return rc;
+        }
+        std::swap(s->fa, s->fb);
+    }
+    s->time += nsteps;  // SimulationSetup.cpp:138
+    // The handle's stream waits for the last download.
+    MPH_CK(cudaStreamWaitEvent(s->stream, s->ev_slab[6 + ((nd - 1) & 1)], 0), "pipeline order");
     return MPH_OK;
 }
 
@@ -662,6 +844,13 @@ int mph_launches_per_step(const mph_sim* s, int* n) {
 
 int mph_step_host(mph_sim* s, const double* f_in, double* f_out, int nsteps) {
     if (!s || !f_in || !f_out || nsteps < 0) return fail(MPH_ERR_ARG, "mph_step_host: bad argument");
+    const int S = nsteps > 0 ? slab_count(s) : 0;
+    if (S > 0) {
+        s->has_state = true;
+        int rc = step_host_slabs(s, f_in, f_out, nsteps, S);
+        if (!rc) rc = sync(s, "mph_step_host");
+        return rc ? rc : check_flag(s);
+    }
     int rc = upload(s, f_in);
     if (rc) return rc;
     s->has_state = true;
