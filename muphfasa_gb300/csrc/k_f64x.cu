@@ -23,6 +23,8 @@
 // Range: class sums of h within +-128, rho in (1/16, 64), |J|, |u| < 4 and
 // |feq/w - h| < 32; a cell outside sets the handle's error flag (reported as
 // MPH_ERR_NONFINITE by the host) instead of producing silent wrap-around.
+#include <type_traits>
+
 #include "lbm_launch.h"
 
 namespace mph {
@@ -295,14 +297,16 @@ __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) 
 // OBST: the domain has obstacles (p.cls set); the plain instantiation
 // carries no class-byte test.  (128-thread blocks capped at 96 registers, 20
 // warps per SM, measured slower: 17.7 against 18.0 GLUPS at 512^3.)
-template <int Q, bool FORCED, bool OBST>
+// WIN: the launch covers the window (y0, y1, z0, z1) of p rather than the
+// whole domain (the offsets cost about 1 % at 512^3 when always applied).
+template <int Q, bool FORCED, bool OBST, bool WIN>
 __global__ void __launch_bounds__(256) k_step_x(const i64* __restrict__ fin, i64* __restrict__ fout, const KParams p,
                                                 const KParamsX px, const KParams* __restrict__ pg,
                                                 const i64* __restrict__ kbb, int* __restrict__ flag) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = p.y0 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = p.z0 + blockIdx.z;
-    if (x >= p.nx || y >= p.y1) return;
+    const int y = (WIN ? p.y0 : 0) + blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = (WIN ? p.z0 : 0) + blockIdx.z;
+    if (x >= p.nx || y >= (WIN ? p.y1 : p.ny)) return;
     const long long c = ((long long)z * p.ny + y) * p.nx + x;
     const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
     if (OBST && p.cls[c] == kSolid) {  // obstacle cell: rest state, h = f / w = 1
@@ -407,6 +411,38 @@ __global__ void __launch_bounds__(kPipeThreads) k_step_x_pipe(const i64* __restr
 }  // namespace
 
 namespace {
+template <int Q, bool FORCED, bool OBST, bool WIN>
+void step_x_launch(const i64* fin, i64* fout, const KParams& p, const KParamsX& px, const KParams* pg, const i64* kbb,
+                   int* flag, cudaStream_t s) {
+    dim3 g, b;
+    step_shape(p, g, b);
+    k_step_x<Q, FORCED, OBST, WIN><<<g, b, 0, s>>>(fin, fout, p, px, pg, kbb, flag);
+}
+
+template <class F>
+cudaError_t with_q(int q, F&& f) {
+    switch (q) {
+        case 9: return f(std::integral_constant<int, 9>{});
+        case 15: return f(std::integral_constant<int, 15>{});
+        case 19: return f(std::integral_constant<int, 19>{});
+        case 27: return f(std::integral_constant<int, 27>{});
+    }
+    return cudaErrorInvalidValue;
+}
+
+// Three run-time flags to compile-time constants.
+template <class F>
+cudaError_t with_flags(bool a, bool b, bool c, F&& f) {
+    using T = std::true_type;
+    using N = std::false_type;
+    if (a) {
+        if (b) return c ? f(T{}, T{}, T{}) : f(T{}, T{}, N{});
+        return c ? f(T{}, N{}, T{}) : f(T{}, N{}, N{});
+    }
+    if (b) return c ? f(N{}, T{}, T{}) : f(N{}, T{}, N{});
+    return c ? f(N{}, N{}, T{}) : f(N{}, N{}, N{});
+}
+
 template <int Q, bool FORCED>
 cudaError_t pipe_setup(size_t& smem) {
     smem = 2 * Q * kPipeThreads * sizeof(long long);
@@ -465,26 +501,15 @@ cudaError_t launch_step_f64x_pipe(int q, bool forced, const long long* fin, long
 cudaError_t launch_step_f64x(int q, bool forced, const long long* fin, long long* fout, const KParams& p,
                              const KParamsX& px, const KParams* pg, const long long* kbb, int* flag,
                              cudaStream_t s) {
-    dim3 g, b;
-    step_shape(p, g, b);
-#define MPH_X_CASE(QQ)                                                                        \
-    case QQ:                                                                                  \
-        if (p.cls) {                                                                          \
-            if (forced) k_step_x<QQ, true, true><<<g, b, 0, s>>>(fin, fout, p, px, pg, kbb, flag);  \
-            else k_step_x<QQ, false, true><<<g, b, 0, s>>>(fin, fout, p, px, pg, kbb, flag);        \
-        } else {                                                                              \
-            if (forced) k_step_x<QQ, true, false><<<g, b, 0, s>>>(fin, fout, p, px, pg, kbb, flag); \
-            else k_step_x<QQ, false, false><<<g, b, 0, s>>>(fin, fout, p, px, pg, kbb, flag);       \
-        }                                                                                     \
-        return cudaGetLastError();
-    switch (q) {
-        MPH_X_CASE(9)
-        MPH_X_CASE(15)
-        MPH_X_CASE(19)
-        MPH_X_CASE(27)
-    }
-#undef MPH_X_CASE
-    return cudaErrorInvalidValue;
+    const bool win = p.y0 != 0 || p.y1 != p.ny || p.z0 != 0 || p.z1 != p.nz;
+    return with_q(q, [&](auto qc) {
+        constexpr int Q = decltype(qc)::value;
+        return with_flags(forced, p.cls != nullptr, win, [&](auto fc, auto oc, auto wc) {
+            step_x_launch<Q, decltype(fc)::value, decltype(oc)::value, decltype(wc)::value>(fin, fout, p, px, pg,
+                                                                                            kbb, flag, s);
+            return cudaGetLastError();
+        });
+    });
 }
 
 }  // namespace mph

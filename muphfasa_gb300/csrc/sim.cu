@@ -35,10 +35,13 @@ struct mph_sim {
     // Slab pipeline of mph_step_host: uploads on copy_stream, upload
     // conversions and slab steps on stream, download conversions on
     // conv_stream, downloads on d2h_stream.
-    double* d_slab = nullptr;    // FP64 staging [4][q][slab_cells]: two upload, two download blocks
+    static constexpr int kRing = 4;  // staging blocks per copy direction
+    double* d_slab = nullptr;    // FP64 staging [2 kRing][q][slab_cells]: upload ring, download ring
     long long slab_cells = 0;    // cells of the largest slab
+    long long max_pitch = 0;     // cudaDevAttrMaxPitch (row stride limit of 2-D copies)
     cudaStream_t d2h_stream = nullptr, conv_stream = nullptr;
-    cudaEvent_t ev_slab[10] = {};  // up copied[2], up free[2], down converted[2], down free[2], start, stepped
+    // up copied[kRing], up free[kRing], down converted[kRing], down free[kRing], start, stepped
+    cudaEvent_t ev_slab[4 * kRing + 2] = {};
     double* d_part = nullptr;   // reduction partials
     double* d_red = nullptr;    // reduction result
     double* d_uprev = nullptr;  // velocity field saved by the last mph_residual (dim x N)
@@ -400,10 +403,18 @@ int download(mph_sim* s, double* f) {
 // conversions run on their own stream: a download waiting for a free staging
 // block never holds up the uploads.  Slabs touch disjoint host ranges, so
 // f_in may alias f_out.
+// MPH_STEP_HOST_SLABS overrides the slab count (0: one block copy each way).
 int slab_count(const mph_sim* s) {
     const int E = s->d.dim == 3 ? s->kp.nz : s->kp.ny;
-    if ((long long)s->d.q * s->kp.ncell * 8 < (32LL << 20) || E < 3) return 0;  // small: one block copy
-    return E < 32 ? E : 32;
+    int S = 64;
+    if (const char* env = std::getenv("MPH_STEP_HOST_SLABS")) {
+        S = std::atoi(env);
+        if (S <= 0) return 0;
+    } else if ((long long)s->d.q * s->kp.ncell * 8 < (32LL << 20)) {
+        return 0;  // small: one block copy
+    }
+    if (E < 3 || S < 3) return 0;
+    return E < S ? E : S;
 }
 
 void slab_window(const mph_sim* s, int k, int S, KParams& w, long long& c0, long long& cnt) {
@@ -425,6 +436,10 @@ int ensure_slabs(mph_sim* s, int S) {
         MPH_CK(cudaStreamCreateWithFlags(&s->d2h_stream, cudaStreamNonBlocking), "d2h stream");
         MPH_CK(cudaStreamCreateWithFlags(&s->conv_stream, cudaStreamNonBlocking), "conversion stream");
         for (cudaEvent_t& e : s->ev_slab) MPH_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "slab event");
+        int dev = 0, pitch = 0;
+        MPH_CK(cudaGetDevice(&dev), "cudaGetDevice");
+        MPH_CK(cudaDeviceGetAttribute(&pitch, cudaDevAttrMaxPitch, dev), "max pitch");
+        s->max_pitch = pitch;
     }
     const int E = s->d.dim == 3 ? s->kp.nz : s->kp.ny;
     const long long plane = s->kp.ncell / E;
@@ -433,9 +448,25 @@ int ensure_slabs(mph_sim* s, int S) {
         cudaFree(s->d_slab);
         s->d_slab = nullptr;
         s->slab_cells = 0;
-        MPH_CK(cudaMalloc(&s->d_slab, 4 * sizeof(double) * s->d.q * cells), "cudaMalloc(slab stage)");
+        MPH_CK(cudaMalloc(&s->d_slab, 2 * mph_sim::kRing * sizeof(double) * s->d.q * cells),
+               "cudaMalloc(slab stage)");
         s->slab_cells = cells;
     }
+    return MPH_OK;
+}
+
+// q rows of cnt values with the given row strides (elements): one 2-D copy,
+// or one copy per row when a stride exceeds the 2-D pitch limit.
+int copy_rows(const mph_sim* s, double* dst, long long dstride, const double* src, long long sstride, long long cnt,
+              cudaMemcpyKind kind, cudaStream_t st) {
+    const long long dp = dstride * (long long)sizeof(double), sp = sstride * (long long)sizeof(double);
+    if (dp <= s->max_pitch && sp <= s->max_pitch) {
+        MPH_CK(cudaMemcpy2DAsync(dst, (size_t)dp, src, (size_t)sp, sizeof(double) * cnt, (size_t)s->d.q, kind, st),
+               "slab copy");
+        return MPH_OK;
+    }
+    for (int n = 0; n < s->d.q; ++n)
+        MPH_CK(cudaMemcpyAsync(dst + n * dstride, src + n * sstride, sizeof(double) * cnt, kind, st), "slab copy");
     return MPH_OK;
 }
 
@@ -444,20 +475,19 @@ int slab_up(mph_sim* s, const double* f, int k, int S, int b) {
     long long c0, cnt;
     slab_window(s, k, S, w, c0, cnt);
     const long long N = s->kp.ncell;
-    cudaEvent_t copied = s->ev_slab[b], freed = s->ev_slab[2 + b];
+    constexpr int R = mph_sim::kRing;
+    cudaEvent_t copied = s->ev_slab[b], freed = s->ev_slab[R + b];
+    int rc;
     if (is_f64(s)) {
-        for (int n = 0; n < s->d.q; ++n)
-            MPH_CK(cudaMemcpyAsync((double*)s->fa + n * N + c0, f + n * N + c0, sizeof(double) * cnt,
-                                   cudaMemcpyHostToDevice, s->copy_stream), "upload slab");
+        if ((rc = copy_rows(s, (double*)s->fa + c0, N, f + c0, N, cnt, cudaMemcpyHostToDevice, s->copy_stream)))
+            return rc;
         MPH_CK(cudaEventRecord(copied, s->copy_stream), "upload order");
         MPH_CK(cudaStreamWaitEvent(s->stream, copied, 0), "upload order");
         return MPH_OK;
     }
     double* st = s->d_slab + (size_t)b * s->d.q * s->slab_cells;
     MPH_CK(cudaStreamWaitEvent(s->copy_stream, freed, 0), "upload order");
-    for (int n = 0; n < s->d.q; ++n)
-        MPH_CK(cudaMemcpyAsync(st + n * cnt, f + n * N + c0, sizeof(double) * cnt, cudaMemcpyHostToDevice,
-                               s->copy_stream), "upload slab");
+    if ((rc = copy_rows(s, st, cnt, f + c0, N, cnt, cudaMemcpyHostToDevice, s->copy_stream))) return rc;
     MPH_CK(cudaEventRecord(copied, s->copy_stream), "upload order");
     MPH_CK(cudaStreamWaitEvent(s->stream, copied, 0), "upload order");
     MPH_CK(launch_convert_slab(s->d.precision, s->d.q, true, s->fa, st, c0, cnt, N, s->stream), "convert slab");
@@ -471,27 +501,26 @@ int slab_down(mph_sim* s, double* f, int k, int S, int b) {
     long long c0, cnt;
     slab_window(s, k, S, w, c0, cnt);
     const long long N = s->kp.ncell;
-    cudaEvent_t converted = s->ev_slab[4 + b], freed = s->ev_slab[6 + b];
+    constexpr int R = mph_sim::kRing;
+    cudaEvent_t converted = s->ev_slab[2 * R + b], freed = s->ev_slab[3 * R + b], stepped = s->ev_slab[4 * R + 1];
     if (is_f64(s)) {
-        MPH_CK(cudaEventRecord(converted, s->stream), "download order");
-        MPH_CK(cudaStreamWaitEvent(s->d2h_stream, converted, 0), "download order");
-        for (int n = 0; n < s->d.q; ++n)
-            MPH_CK(cudaMemcpyAsync(f + n * N + c0, (const double*)s->fb + n * N + c0, sizeof(double) * cnt,
-                                   cudaMemcpyDeviceToHost, s->d2h_stream), "download slab");
+        MPH_CK(cudaEventRecord(stepped, s->stream), "download order");
+        MPH_CK(cudaStreamWaitEvent(s->d2h_stream, stepped, 0), "download order");
+        int rc = copy_rows(s, f + c0, N, (const double*)s->fb + c0, N, cnt, cudaMemcpyDeviceToHost, s->d2h_stream);
+        if (rc) return rc;
         MPH_CK(cudaEventRecord(freed, s->d2h_stream), "download order");
         return MPH_OK;
     }
-    double* st = s->d_slab + (size_t)(2 + b) * s->d.q * s->slab_cells;
-    MPH_CK(cudaEventRecord(s->ev_slab[9], s->stream), "download order");  // slab k stepped
-    MPH_CK(cudaStreamWaitEvent(s->conv_stream, s->ev_slab[9], 0), "download order");
+    double* st = s->d_slab + (size_t)(R + b) * s->d.q * s->slab_cells;
+    MPH_CK(cudaEventRecord(stepped, s->stream), "download order");
+    MPH_CK(cudaStreamWaitEvent(s->conv_stream, stepped, 0), "download order");
     MPH_CK(cudaStreamWaitEvent(s->conv_stream, freed, 0), "download order");
     MPH_CK(launch_convert_slab(s->d.precision, s->d.q, false, s->fb, st, c0, cnt, N, s->conv_stream),
            "convert slab");
     MPH_CK(cudaEventRecord(converted, s->conv_stream), "download order");
     MPH_CK(cudaStreamWaitEvent(s->d2h_stream, converted, 0), "download order");
-    for (int n = 0; n < s->d.q; ++n)
-        MPH_CK(cudaMemcpyAsync(f + n * N + c0, st + n * cnt, sizeof(double) * cnt, cudaMemcpyDeviceToHost,
-                               s->d2h_stream), "download slab");
+    int rc = copy_rows(s, f + c0, N, st, cnt, cnt, cudaMemcpyDeviceToHost, s->d2h_stream);
+    if (rc) return rc;
     MPH_CK(cudaEventRecord(freed, s->d2h_stream), "download order");
     return MPH_OK;
 }
@@ -509,26 +538,27 @@ int slab_step(mph_sim* s, int k, int S) {
 int step_host_slabs(mph_sim* s, const double* f_in, double* f_out, int nsteps, int S) {
     int rc = ensure_slabs(s, S);
     if (rc) return rc;
-    cudaEvent_t start = s->ev_slab[8];
-    // Earlier work on the handle's stream comes first; both staging pairs start free.
+    constexpr int R = mph_sim::kRing;
+    cudaEvent_t start = s->ev_slab[4 * R];
+    // Earlier work on the handle's stream comes first; every staging block starts free.
     MPH_CK(cudaEventRecord(start, s->stream), "pipeline order");
     MPH_CK(cudaStreamWaitEvent(s->copy_stream, start, 0), "pipeline order");
     MPH_CK(cudaStreamWaitEvent(s->d2h_stream, start, 0), "pipeline order");
-    for (int b = 0; b < 2; ++b) {
-        MPH_CK(cudaEventRecord(s->ev_slab[2 + b], s->stream), "pipeline order");
-        MPH_CK(cudaEventRecord(s->ev_slab[6 + b], s->d2h_stream), "pipeline order");
+    for (int b = 0; b < R; ++b) {
+        MPH_CK(cudaEventRecord(s->ev_slab[R + b], s->stream), "pipeline order");
+        MPH_CK(cudaEventRecord(s->ev_slab[3 * R + b], s->d2h_stream), "pipeline order");
     }
     const bool one = nsteps == 1;
-    int nd = 0;  // downloads issued (staging block nd % 2)
+    int nd = 0;  // downloads issued (staging block nd % R)
     auto step_and_send = [&](int k) {
         int r = slab_step(s, k, S);
-        if (!r && one) r = slab_down(s, f_out, k, S, nd++ & 1);
+        if (!r && one) r = slab_down(s, f_out, k, S, nd++ % R);
         return r;
     };
     // Step 1 behind the uploads S-1, 0, 1, ..., S-2.
     for (int i = 0; i < S; ++i) {
         const int k = i == 0 ? S - 1 : i - 1;
-        if ((rc = slab_up(s, f_in, k, S, i & 1))) return rc;
+        if ((rc = slab_up(s, f_in, k, S, i % R))) return rc;
         if (i >= 2 && (rc = step_and_send(i - 2))) return rc;
     }
     if ((rc = step_and_send(S - 2)) || (rc = step_and_send(S - 1))) return rc;
@@ -540,13 +570,13 @@ int step_host_slabs(mph_sim* s, const double* f_in, double* f_out, int nsteps, i
             std::swap(s->fa, s->fb);
         }
         for (int k = 0; k < S; ++k) {
-            if ((rc = slab_step(s, k, S)) || (rc = slab_down(s, f_out, k, S, nd++ & 1))) return rc;
+            if ((rc = slab_step(s, k, S)) || (rc = slab_down(s, f_out, k, S, nd++ % R))) return rc;
         }
         std::swap(s->fa, s->fb);
     }
     s->time += nsteps;  // SimulationSetup.cpp:138
     // The handle's stream waits for the last download.
-    MPH_CK(cudaStreamWaitEvent(s->stream, s->ev_slab[6 + ((nd - 1) & 1)], 0), "pipeline order");
+    MPH_CK(cudaStreamWaitEvent(s->stream, s->ev_slab[3 * R + (nd - 1) % R], 0), "pipeline order");
     return MPH_OK;
 }
 

@@ -150,3 +150,12 @@ def test_small_domain_takes_block_copies(mph):
     out = np.empty_like(f0)
     b.step_host(f0, out, 2)
     assert np.array_equal(out, a.f())
+
+
+@pytest.mark.parametrize("slabs", ["0", "3", "5", "64"])
+def test_slab_count_override(slabs, mph, monkeypatch):
+    """MPH_STEP_HOST_SLABS: 0 forces the block copies, others the slab count
+    (capped at the number of planes)."""
+    monkeypatch.setenv("MPH_STEP_HOST_SLABS", slabs)
+    d = mph.make_desc("D3Q19", (64, 64, 64), 1 / 0.6, faces=CH3, force=(1e-5, 0, 0), precision="f64x")
+    _check(mph, d, 2, inplace=True, pinned=True, seed=12)
