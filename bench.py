@@ -409,7 +409,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=512, help="cells per side of the channel")
     ap.add_argument("--precision", default="f64x", choices=list(ELEM))
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-sweep", default="", help="comma-separated slab counts of the step_host pipeline to time")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--domains", type=int, default=512, help="domains of the batch512 workload")
     ap.add_argument("--probes", action="store_true", help="build and run bench_probes.cu (pipe rates, pull-copy)")
@@ -498,6 +499,20 @@ def main():
         e2e = {"value": round(total_cells * args.e2e_steps / dt / 1e6, 3), "unit": "MLUPS",
                "h2d_bytes_per_step": q * cells * 8, "d2h_bytes_per_step": q * cells * 8,
                "steps": args.e2e_steps, "host_buffers": "pinned (cudaHostAlloc)", "api": "mph_step_host"}
+        if args.e2e_sweep and rank == 0:
+            # Slab count of the host-copy pipeline (0: one block copy each
+            # way), three interleaved rounds: the host link is shared.
+            sweep = {}
+            for _ in range(3):
+                for S in args.e2e_sweep.split(","):
+                    os.environ["MPH_STEP_HOST_SLABS"] = S
+                    sim.step_host(f_host, f_host, 1)
+                    t0 = time.perf_counter()
+                    for _ in range(args.e2e_steps):
+                        sim.step_host(f_host, f_host, 1)
+                    sweep.setdefault(S, []).append(round(cells * args.e2e_steps / (time.perf_counter() - t0) / 1e6, 1))
+            os.environ.pop("MPH_STEP_HOST_SLABS", None)
+            e2e["slab_sweep_mlups"] = sweep
         del f_host
         pinned.close()
     except StopIteration:

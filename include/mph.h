@@ -198,7 +198,11 @@ int mph_launches_per_step(const mph_sim* sim, int* n);
  * *ms is the elapsed device time of the whole sequence. */
 int mph_advance_timed(mph_sim* sim, int nsteps, float* ms);
 /* Drop-in with host buffers: uploads f_in, advances nsteps, downloads the
- * result into f_out (both host valid-cell SoA FP64; may alias). */
+ * result into f_out (both host valid-cell SoA FP64; may alias).  Domains of
+ * 32 MB and more move in slabs of planes so that uploads, slab steps and
+ * downloads overlap (MPH_STEP_HOST_SLABS sets the slab count, 0 disables);
+ * the result is the same bits either way.  Page-locked buffers
+ * (mph_host_alloc) reach the full host-link rate. */
 int mph_step_host(mph_sim* sim, const double* f_in, double* f_out, int nsteps);
 
 /* ---- plugin level: caller-owned device memory in AMReX Array4 layout ----- */
