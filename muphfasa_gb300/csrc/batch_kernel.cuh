@@ -68,6 +68,41 @@ __global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __rest
         float2 g[P][Q];
         int ca[P];
         bool oka[P], okb[P];
+        if ((p.nx & 1) == 0) {
+            // nx even: a pair (c, c + 1), c even, shares its row, and N and
+            // every row offset are even, so the c_x = 0 populations of both
+            // cells are one aligned 32-bit word and every store is a word.
+            using L = Lat<Q>;
+#pragma unroll
+            for (int j = 0; j < P; ++j) {
+                const int l = 2 * (threadIdx.x + 256 * j);
+                ca[j] = ch.c0 + l;
+                oka[j] = ca[j] < (int)N;
+                if (oka[j]) {
+                    int x, y, z;
+                    chunk_cell(p, ch, l, x, y, z);
+                    const Nbr oa = neighbours<L::D>(p, x, y, z), ob = neighbours<L::D>(p, x + 1, y, z);
+#pragma unroll
+                    for (int n = 0; n < Q; ++n) {
+                        const unsigned ea = (unsigned)n * N + (unsigned)(ca[j] + upstream<Q>(oa, n));
+                        if (L::cx(n) == 0) {
+                            g[j][n] = St::ldr2(fin, ea);
+                        } else {
+                            const unsigned eb = (unsigned)n * N + (unsigned)(ca[j] + 1 + upstream<Q>(ob, n));
+                            g[j][n] = make_float2(St::ldr1(fin, ea), St::ldr1(fin, eb));
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < P; ++j) {
+                if (!oka[j]) continue;
+                collide_shift<Q, A2, FORCED>(p, g[j]);
+#pragma unroll
+                for (int n = 0; n < Q; ++n) St::str2(fout, (unsigned)n * N + (unsigned)ca[j], g[j][n]);
+            }
+            continue;
+        }
 #pragma unroll
         for (int j = 0; j < P; ++j) {
             const int l = 2 * (threadIdx.x + 256 * j);
