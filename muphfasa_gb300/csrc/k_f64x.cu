@@ -23,6 +23,8 @@
 // Range: class sums of h within +-128, rho in (1/16, 64), |J|, |u| < 4 and
 // |feq/w - h| < 32; a cell outside sets the handle's error flag (reported as
 // MPH_ERR_NONFINITE by the host) instead of producing silent wrap-around.
+#include <cstdio>
+#include <cstdlib>
 #include <type_traits>
 
 #include "lbm_launch.h"
@@ -295,8 +297,10 @@ __device__ __forceinline__ void collide_x(const KParamsX& px, i64* h, int& bad) 
 }
 
 // OBST: the domain has obstacles (p.cls set); the plain instantiation
-// carries no class-byte test.  (128-thread blocks capped at 96 registers, 20
-// warps per SM, measured slower: 17.7 against 18.0 GLUPS at 512^3.)
+// carries no class-byte test.  Launched in blocks of 128 threads along x
+// (104 registers: 4 blocks, 16 warps per SM): 18.3 GLUPS at 512^3 against
+// 17.9 for blocks of 256 with the same occupancy; capping the registers at
+// 96 for 20 warps per SM measured 17.7.
 // WIN: the launch covers the window (y0, y1, z0, z1) of p rather than the
 // whole domain (the offsets cost about 1 % at 512^3 when always applied).
 template <int Q, bool FORCED, bool OBST, bool WIN>
@@ -415,7 +419,14 @@ template <int Q, bool FORCED, bool OBST, bool WIN>
 void step_x_launch(const i64* fin, i64* fout, const KParams& p, const KParamsX& px, const KParams* pg, const i64* kbb,
                    int* flag, cudaStream_t s) {
     dim3 g, b;
-    step_shape(p, g, b);
+    step_shape(p, g, b, 128);
+    if (const char* env = std::getenv("MPH_F64X_BLOCK")) {  // "BXxBY": other block shapes
+        int bx = 0, by = 0;
+        if (std::sscanf(env, "%dx%d", &bx, &by) == 2 && bx >= 32 && bx % 32 == 0 && by >= 1 && bx * by <= 256) {
+            b = dim3(bx, by, 1);
+            g = dim3((p.nx + bx - 1) / bx, (p.y1 - p.y0 + by - 1) / by, p.z1 - p.z0);
+        }
+    }
     k_step_x<Q, FORCED, OBST, WIN><<<g, b, 0, s>>>(fin, fout, p, px, pg, kbb, flag);
 }
 
