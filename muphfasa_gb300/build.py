@@ -20,6 +20,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libmph.so")
 DRIVER = os.path.join(BUILD, "mph_run")
+BATCH_DRIVER = os.path.join(BUILD, "mph_batch_run")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler",
@@ -38,8 +39,8 @@ def _nvcc() -> str:
 
 
 def _headers():
-    return [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))] + [
-        os.path.join(INCLUDE, "mph.h")]
+    return [os.path.join(CSRC, f) for f in os.listdir(CSRC)
+            if f.endswith((".h", ".cuh")) and f != "driver_util.h"] + [os.path.join(INCLUDE, "mph.h")]
 
 
 def _stale(obj: str, src: str) -> bool:
@@ -81,16 +82,20 @@ def build(verbose: bool = False) -> str:
 
 
 def _driver():
-    """The host driver executable (csrc/mph_run.cpp) over libmph.so."""
-    src = os.path.join(CSRC, "mph_run.cpp")
-    if os.path.exists(DRIVER) and os.path.getmtime(DRIVER) >= max(os.path.getmtime(src), os.path.getmtime(LIB)):
-        return
-    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I", INCLUDE, src, "-o", DRIVER + ".tmp", "-L", BUILD, "-lmph",
-           "-Wl,-rpath,$ORIGIN"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"driver build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
-    os.replace(DRIVER + ".tmp", DRIVER)
+    """The host drivers over libmph.so: mph_run (csrc/mph_run.cpp, one
+    domain) and mph_batch_run (csrc/mph_batch_run.cpp, many domains)."""
+    util = os.path.join(CSRC, "driver_util.h")
+    for exe, src_name in ((DRIVER, "mph_run.cpp"), (BATCH_DRIVER, "mph_batch_run.cpp")):
+        src = os.path.join(CSRC, src_name)
+        deps = [src, util, LIB, os.path.join(INCLUDE, "mph.h")]
+        if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(f) for f in deps):
+            continue
+        cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I", INCLUDE, "-I", CSRC, src, "-o", exe + ".tmp", "-L", BUILD,
+               "-lmph", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        os.replace(exe + ".tmp", exe)
 
 
 def _link(objs):

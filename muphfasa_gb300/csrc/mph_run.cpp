@@ -23,82 +23,20 @@
 //     (state.raw) so that every precision resumes bit for bit;
 //   * amr.restart = <checkpoint directory> resumes from such a checkpoint
 //     with step + 1 (SimulationSetup.cpp:107-117), bit for bit.
-#include <sys/stat.h>
-
-#include <cerrno>
-#include <cmath>
-#include <cstdio>
 #include <cstdlib>
-#include <cstring>
 #include <fstream>
 #include <iomanip>
 #include <iostream>
-#include <sstream>
 #include <string>
 #include <vector>
 
+#include "driver_util.h"
 #include "mph.h"
 
+using namespace drv;
+
 namespace {
-
 constexpr const char* kCheckpointVersion = "muphfasa_gb300_checkpoint_v1";
-
-[[noreturn]] void die(const std::string& what) {
-    std::cerr << "mph_run: " << what << "\n";
-    std::exit(1);
-}
-
-void ck(int rc, const char* what) {
-    if (rc != MPH_OK) die(std::string(what) + ": " + mph_last_error());
-}
-
-std::string get(const mph_inputs* in, const char* key, const std::string& dflt) {
-    char buf[4096];
-    if (mph_inputs_get(in, key, buf, sizeof buf) != MPH_OK) return dflt;
-    std::string s(buf);
-    // a single token value
-    const size_t a = s.find_first_not_of(" \t"), b = s.find_last_not_of(" \t");
-    return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
-}
-
-std::string numbered(const std::string& prefix, int step) {
-    std::ostringstream ss;
-    ss << prefix << std::setw(7) << std::setfill('0') << step;
-    return ss.str();
-}
-
-void make_dir(const std::string& d) {
-    if (mkdir(d.c_str(), 0755) != 0 && errno != EEXIST) die("cannot create directory " + d);
-}
-
-std::string domain_box(const mph_desc& d) {
-    std::ostringstream ss;
-    if (d.dim == 2) ss << "((0,0) (" << d.n[0] - 1 << "," << d.n[1] - 1 << ") (0,0))";
-    else ss << "((0,0,0) (" << d.n[0] - 1 << "," << d.n[1] - 1 << "," << d.n[2] - 1 << ") (0,0,0))";
-    return ss.str();
-}
-
-void write_npy(const std::string& path, const double* v, const mph_desc& d) {
-    std::ostringstream hdr;
-    hdr << "{'descr': '<f8', 'fortran_order': False, 'shape': (";
-    if (d.dim == 3) hdr << d.n[2] << ", ";
-    hdr << d.n[1] << ", " << d.n[0] << "), }";
-    std::string h = hdr.str();
-    const size_t total = 10 + h.size() + 1;
-    h.append((64 - total % 64) % 64, ' ');
-    h.push_back('\n');
-    std::ofstream f(path, std::ios::binary);
-    const unsigned char magic[8] = {0x93, 'N', 'U', 'M', 'P', 'Y', 1, 0};
-    f.write(reinterpret_cast<const char*>(magic), 8);
-    const unsigned short len = (unsigned short)h.size();
-    const unsigned char le[2] = {(unsigned char)(len & 0xff), (unsigned char)(len >> 8)};
-    f.write(reinterpret_cast<const char*>(le), 2);
-    f.write(h.data(), (std::streamsize)h.size());
-    const long long n = (long long)d.n[0] * d.n[1] * (d.dim == 3 ? d.n[2] : 1);
-    f.write(reinterpret_cast<const char*>(v), (std::streamsize)(n * sizeof(double)));
-    if (!f) die("cannot write " + path);
-}
-
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -109,11 +47,7 @@ int main(int argc, char** argv) {
     mph_inputs* in = nullptr;
     ck(mph_inputs_load(argv[1], argc - 2, const_cast<const char* const*>(argv + 2), &in), "inputs");
     const std::string prec_name = get(in, "mph.precision", "f64");
-    const char* names[] = {"f64", "f64_fast", "f32", "f16s", "bf16s", "f64x"};
-    const int precs[] = {MPH_PREC_F64, MPH_PREC_F64_FAST, MPH_PREC_F32, MPH_PREC_F16S, MPH_PREC_BF16S, MPH_PREC_F64X};
-    int prec = -1;
-    for (int i = 0; i < 6; ++i)
-        if (prec_name == names[i]) prec = precs[i];
+    const int prec = precision_code(prec_name);
     if (prec < 0) die("mph.precision must be one of f64 f64_fast f32 f16s bf16s f64x");
     ck(mph_set_device(std::atoi(get(in, "mph.device", "0").c_str())), "device");
 
@@ -122,7 +56,7 @@ int main(int argc, char** argv) {
     ck(mph_inputs_derive(in, prec, &d, &info), "inputs");
     mph_sim* sim = nullptr;
     ck(mph_create(&d, &sim), "create");
-    const long long N = (long long)d.n[0] * d.n[1] * (d.dim == 3 ? d.n[2] : 1);
+    const long long N = cells(d);
     const std::string plot_prefix = get(in, "amr.plot_file", "plt");
     const std::string chk_prefix = get(in, "amr.check_file", "chk");
     const std::string restart = get(in, "amr.restart", "");
@@ -173,16 +107,7 @@ int main(int argc, char** argv) {
         if (info.plot_int > 0 && step % info.plot_int == 0) {
             ck(mph_update_macroscopic(sim, rho.data(), u.data()), "moments");
             const std::string dir = numbered(plot_prefix, step);
-            make_dir(dir);
-            for (auto& r : rho) r *= info.ref_density;
-            for (auto& v : u) v *= info.dx / info.dt;
-            write_npy(dir + "/density.npy", rho.data(), d);
-            const char* vn[3] = {"vx", "vy", "vz"};
-            for (int a = 0; a < d.dim; ++a) write_npy(dir + "/" + vn[a] + ".npy", u.data() + (size_t)a * N, d);
-            std::ofstream h(dir + "/Header");
-            h << "muphfasa_gb300_plotfile_v1\n" << (d.dim + 1) << "\ndensity\n";
-            for (int a = 0; a < d.dim; ++a) h << vn[a] << "\n";
-            h << d.dim << "\n" << std::setprecision(17) << t * info.dt << "\n" << step << "\n" << domain_box(d) << "\n";
+            write_plot(dir, rho, u, d, info, t, step);
             std::cout << "Plotfile: wrote " << dir << "  step=" << step << "  time=" << t * info.dt << "\n";
         }
         if (info.chk_int > 0 && step % info.chk_int == 0) {
