@@ -656,7 +656,7 @@ int mph_create(const mph_desc* desc, mph_sim** out) {
         if (e == cudaSuccess) e = cudaMemcpy(s->d_kbb, kbb, sizeof(kbb), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMalloc(&s->d_flag, sizeof(int));
         if (e == cudaSuccess) e = cudaMemset(s->d_flag, 0, sizeof(int));
-        // Kernel choice: one cell per thread (measured faster on GB300: 18.0
+        // Kernel choice: one cell per thread (measured faster on GB300: 18.3
         // vs 16.5 GLUPS at 512^3 D3Q19), or the persistent cp.async pipeline
         // with MPH_F64X_KERNEL=pipe.
         const char* kv = std::getenv("MPH_F64X_KERNEL");
@@ -878,7 +878,14 @@ int mph_step_host(mph_sim* s, const double* f_in, double* f_out, int nsteps) {
     if (S > 0) {
         s->has_state = true;
         int rc = step_host_slabs(s, f_in, f_out, nsteps, S);
-        if (!rc) rc = sync(s, "mph_step_host");
+        if (rc) {
+            // Copies already queued may still touch the caller's buffers:
+            // let them finish before the error reaches the caller.
+            for (cudaStream_t st : {s->copy_stream, s->conv_stream, s->d2h_stream, s->stream})
+                if (st) cudaStreamSynchronize(st);
+            return rc;
+        }
+        rc = sync(s, "mph_step_host");
         return rc ? rc : check_flag(s);
     }
     int rc = upload(s, f_in);
