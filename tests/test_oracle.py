@@ -217,3 +217,71 @@ def test_obstacle_plane_blocks_forced_flow(oracle_mod):
     fluid = mask.ravel() == 0
     ub = blocked.moments()[1][: blocked.N][fluid].mean()
     assert uf > 5e-4 and abs(ub) < 1e-3 * uf, (uf, ub)
+
+
+@pytest.mark.parametrize("lat", ["D2Q9", "D3Q15", "D3Q19", "D3Q27"])
+def test_zero_force_path_is_bit_identical_to_unforced(lat, oracle_mod):
+    # test_forcing.cpp: the forced kernel with F = 0 gives the unforced bits
+    # (u gets + 0.5 * 0, the Guo term is exactly 0 and added as +0).
+    O = oracle_mod
+    dim, q = O.LATTICE_DQ[lat]
+    n = (5, 4, 3) if dim == 3 else (6, 5)
+    rng = np.random.default_rng(31)
+    f0 = None
+    out = []
+    for force in (None, (0.0, 0.0, 0.0)):
+        sim = O.OracleSim(O.Config(lat, n, omega=1.37, force=force), "port")
+        if f0 is None:
+            f0 = rng.uniform(0.5, 1.5, q * sim.N) / q
+        sim.set_f(f0)
+        sim.fill_ghosts()
+        sim.step(7)
+        out.append(sim.get_f())
+    assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("lat", ["D2Q9", "D3Q19", "D3Q27"])
+def test_guo_step_moments(lat, oracle_mod):
+    # test_forcing.cpp: one forced BGK step leaves the mass unchanged and adds
+    # F to the momentum (a one-cell periodic domain streams onto itself, so the
+    # step is the collision alone), from random non-equilibrium populations.
+    O = oracle_mod
+    dim, q = O.LATTICE_DQ[lat]
+    n = (1, 1, 1) if dim == 3 else (1, 1)
+    rng = np.random.default_rng(32)
+    c = _velocities(O, lat)
+    for _ in range(10):
+        F = tuple(rng.uniform(-1e-3, 1e-3, dim)) + (0.0,) * (3 - dim)
+        sim = O.OracleSim(O.Config(lat, n, omega=rng.uniform(0.6, 1.9), force=F), "port")
+        f0 = _lattice(O, lat) * (1 + 0.05 * rng.standard_normal(q))
+        sim.set_f(f0)
+        sim.fill_ghosts()
+        sim.step(1)
+        f1 = sim.get_f()
+        assert abs(f1.sum() - f0.sum()) < 1e-15
+        assert np.abs(c.T @ f1 - c.T @ f0 - np.array(F[:dim])).max() < 1e-15
+
+
+def _velocities(O, lat):
+    """Velocity table of the oracle's lattice, recovered from streaming: on a
+    3^D periodic box at rest, population n raised on one cell appears, after a
+    pure-streaming step (omega = 0: no collision), at x + c_n."""
+    dim, q = O.LATTICE_DQ[lat]
+    n = (3, 3, 3) if dim == 3 else (3, 3)
+    sim = O.OracleSim(O.Config(lat, n, omega=0.0), "port")
+    N = sim.N
+    c = np.zeros((q, dim))
+    centre = 13 if dim == 3 else 4
+    w = _lattice(O, lat)
+    for k in range(q):
+        f = np.repeat(w, N)
+        f[k * N + centre] += 1.0
+        sim.set_f(f)
+        sim.fill_ghosts()
+        sim.step(1)
+        g = sim.get_f().reshape(q, N)[k]
+        cell = int(np.argmax(g))
+        coords = np.unravel_index(cell, tuple(reversed(n)))[::-1]
+        base = np.unravel_index(centre, tuple(reversed(n)))[::-1]
+        c[k] = np.array(coords) - np.array(base)
+    return c
