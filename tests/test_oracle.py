@@ -285,3 +285,26 @@ def _velocities(O, lat):
         base = np.unravel_index(centre, tuple(reversed(n)))[::-1]
         c[k] = np.array(coords) - np.array(base)
     return c
+
+
+@pytest.mark.parametrize("lat", ["D2Q9", "D3Q15", "D3Q19", "D3Q27"])
+@pytest.mark.parametrize("forced", [False, True])
+def test_macroscopic_moments(lat, forced, oracle_mod):
+    # test_macroscopic.cpp:59-158: rho = sum f, u = (sum c f [+ F / 2]) / rho,
+    # on random populations (a one-cell periodic domain streams onto itself).
+    O = oracle_mod
+    dim, q = O.LATTICE_DQ[lat]
+    n = (1, 1, 1) if dim == 3 else (1, 1)
+    c = _velocities(O, lat)
+    rng = np.random.default_rng(33)
+    for _ in range(10):
+        F = tuple(rng.uniform(-1e-3, 1e-3, dim)) + (0.0,) * (3 - dim) if forced else None
+        sim = O.OracleSim(O.Config(lat, n, omega=1.0, force=F), "port")
+        f = _lattice(O, lat) * rng.uniform(0.8, 1.2, q)
+        sim.set_f(f)
+        sim.fill_ghosts()
+        rho, u = sim.moments()
+        r = f.sum()
+        j = c.T @ f + (0.5 * np.array(F[:dim]) if forced else 0.0)
+        assert abs(rho[0] - r) < 1e-15
+        assert np.abs(u - j / r).max() < 1e-16
