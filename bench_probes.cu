@@ -2,7 +2,8 @@
 // memory pattern, used to explain the step kernels' rooflines:
 //   FP64 (DFMA/DADD/DDIV), FP32 FFMA, INT32 IMAD, 64-bit high multiplies,
 //   int64<->double and int32->float conversions, a plain copy, and a
-//   19-population pull-copy (the step's memory traffic without its arithmetic).
+//   19-population pull-copy (the step's memory traffic without its arithmetic),
+//   and the host link (page-locked copies each way and both at once).
 // Build and run: python bench.py --probes   (nvcc -O3 -gencode arch=compute_103a,code=sm_103a)
 #include <cstdio>
 #include <cstdint>
@@ -256,4 +257,44 @@ static int probes_conv_stream() {
     return 0;
 }
 
-int main() { return probes_pipes() | probes_conv_stream(); }
+// Host link: page-locked host memory to the device and back, 4 GiB copies,
+// one direction at a time and both at once on two streams (the bound of
+// mph_step_host, which moves every population across the link twice).
+static int probes_host_link() {
+    const size_t bytes = (size_t)1 << 32;
+    void *h0, *h1, *d0, *d1;
+    CK(cudaHostAlloc(&h0, bytes, cudaHostAllocDefault));
+    CK(cudaHostAlloc(&h1, bytes, cudaHostAllocDefault));
+    CK(cudaMalloc(&d0, bytes));
+    CK(cudaMalloc(&d1, bytes));
+    CK(cudaMemset(d1, 0, bytes));
+    for (size_t i = 0; i < bytes; i += 4096) static_cast<char*>(h0)[i] = 1;  // touch the pages
+    cudaStream_t s0, s1;
+    CK(cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking));
+    cudaEvent_t e0, e1; cudaEventCreate(&e0); cudaEventCreate(&e1);
+    for (int mode = 0; mode < 3; ++mode) {  // h2d, d2h, both
+        float best = 1e9;
+        for (int r = 0; r < 3; ++r) {
+            CK(cudaDeviceSynchronize());
+            cudaEventRecord(e0, s0);
+            CK(cudaStreamWaitEvent(s1, e0, 0));
+            if (mode != 1) CK(cudaMemcpyAsync(d0, h0, bytes, cudaMemcpyHostToDevice, s0));
+            if (mode != 0) CK(cudaMemcpyAsync(h1, d1, bytes, cudaMemcpyDeviceToHost, mode == 2 ? s1 : s0));
+            cudaEvent_t done; cudaEventCreateWithFlags(&done, cudaEventDisableTiming);
+            cudaEventRecord(done, s1);
+            CK(cudaStreamWaitEvent(s0, done, 0));
+            cudaEventRecord(e1, s0);
+            CK(cudaEventSynchronize(e1));
+            cudaEventDestroy(done);
+            float ms; cudaEventElapsedTime(&ms, e0, e1); if (ms < best) best = ms;
+        }
+        const double moved = (mode == 2 ? 2.0 : 1.0) * (double)bytes;
+        printf("host link %s: %.1f GB/s\n", mode == 0 ? "host->device" : mode == 1 ? "device->host" : "both at once", moved / best / 1e6);
+    }
+    cudaStreamDestroy(s0); cudaStreamDestroy(s1);
+    cudaFreeHost(h0); cudaFreeHost(h1); cudaFree(d0); cudaFree(d1);
+    return 0;
+}
+
+int main() { return probes_pipes() | probes_conv_stream() | probes_host_link(); }
