@@ -34,3 +34,16 @@ def test_reference_arm_other_ranks_exit_quietly():
     r = _bench("--impl", "reference", "--steps", "1", "--warmup", "0",
                env={"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_gpu_arm_fails_loudly_without_a_device():
+    """No CPU fallback: without a GPU the measured arm exits non-zero and
+    prints no result line."""
+    import pytest
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    r = _bench("--steps", "1", "--warmup", "0", "--no-cpu", "--e2e-steps", "0")
+    assert r.returncode != 0
+    assert not any(ln.startswith("{") for ln in r.stdout.splitlines())
+    assert "MPH_ERR_CUDA" in r.stderr
