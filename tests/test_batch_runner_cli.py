@@ -1,5 +1,5 @@
-"""mph_batch_run argument handling that needs no GPU: usage, and the
-precisions a batch cannot take."""
+"""Argument handling of the host drivers (mph_batch_run, mph_run) that needs
+no GPU: usage, precisions they cannot take, missing inputs files."""
 import os
 import subprocess
 
@@ -16,3 +16,15 @@ def test_usage_and_precision_errors(mph, tmp_path):
     assert r.returncode == 1 and "mph.precision" in r.stderr
     r = subprocess.run([exe, str(tmp_path / "missing.inputs")], cwd=tmp_path, capture_output=True, text=True)
     assert r.returncode == 1 and r.stderr.startswith("mph_batch_run:")
+
+
+def test_single_driver_usage_and_precision_errors(mph, tmp_path):
+    """mph_run: usage without arguments, a bad precision and a missing inputs
+    file are reported before any device work."""
+    exe = os.path.join(os.path.dirname(mph.__file__), "_build", "mph_run")
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 2 and "usage" in r.stderr
+    r = subprocess.run([exe, INPUTS, "mph.precision=f128"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 1 and "mph.precision" in r.stderr and r.stderr.startswith("mph_run:")
+    r = subprocess.run([exe, str(tmp_path / "missing.inputs")], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 1 and r.stderr.startswith("mph_run:")
