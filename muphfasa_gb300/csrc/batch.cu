@@ -12,7 +12,9 @@
 // collide device code as a single domain, so every domain's result is
 // bit-identical to a single-domain handle with the same description.
 //
-// Step pairs (A->B, B->A) are captured once in a CUDA graph and replayed.
+// Step pairs are captured once as CUDA graphs and replayed: one graph per
+// buffer the state starts in (A->B->A and B->A->B), chosen at each replay,
+// so an odd number of steps before a replay keeps the right input.
 // K (cells per thread) is chosen by an autotuner that times the candidates
 // on the batch itself and caches the winner per (Q, precision, size class).
 // mph_batch_advance_looped_timed runs the same steps as one launch per domain
@@ -121,7 +123,8 @@ struct mph_batch {
     int k_idx = -1;  // candidate chosen by the autotuner
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    cudaGraphExec_t graph = nullptr;  // two steps A->B->A
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};  // two steps from graph_in[i] back to it
+    void* graph_in[2] = {nullptr, nullptr};          // the buffer graph[i] starts from
     int graph_k = -1;
     double time = 0.0;
 };
@@ -153,7 +156,8 @@ void free_batch(mph_batch* b) {
     cudaFree(b->d_rout);
     cudaFree(b->d_walls);
     cudaFree(b->d_cls);
-    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (cudaGraphExec_t g : b->graph)
+        if (g) cudaGraphExecDestroy(g);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -281,20 +285,48 @@ int autotune(mph_batch* b) {
     return MPH_OK;
 }
 
-// Two steps (A->B, B->A) captured once as a CUDA graph.
+void drop_graphs(mph_batch* b) {
+    for (int i = 0; i < 2; ++i) {
+        if (b->graph[i]) cudaGraphExecDestroy(b->graph[i]);
+        b->graph[i] = nullptr;
+        b->graph_in[i] = nullptr;
+    }
+    b->graph_k = -1;
+}
+
+// Two steps captured as a CUDA graph for each buffer the state can start in
+// (A->B->A and B->A->B).  Capture only records the launches; the two host-side
+// swaps of step_once cancel, and fa / fb are put back as they were.
 int ensure_graph(mph_batch* b) {
-    if (b->graph && b->graph_k == b->k_idx) return MPH_OK;
-    if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
-    cudaGraph_t g = nullptr;
-    MPH_CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "graph capture begin");
-    int rc = step_once(b, b->k_idx);
-    if (!rc) rc = step_once(b, b->k_idx);
-    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
-    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
-    if (e != cudaSuccess) return cuda_fail(e, "graph capture end");
-    e = cudaGraphInstantiate(&b->graph, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
+    if (b->graph[0] && b->graph[1] && b->graph_k == b->k_idx) return MPH_OK;
+    drop_graphs(b);
+    void* const fa0 = b->fa;
+    void* const fb0 = b->fb;
+    for (int i = 0; i < 2; ++i) {
+        b->fa = i == 0 ? fa0 : fb0;
+        b->fb = i == 0 ? fb0 : fa0;
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+        int rc = e == cudaSuccess ? MPH_OK : cuda_fail(e, "graph capture begin");
+        if (!rc) {
+            rc = step_once(b, b->k_idx);
+            if (!rc) rc = step_once(b, b->k_idx);
+            e = cudaStreamEndCapture(b->stream, &g);
+            if (!rc && e != cudaSuccess) rc = cuda_fail(e, "graph capture end");
+        }
+        if (!rc) {
+            e = cudaGraphInstantiate(&b->graph[i], g, 0);
+            if (e != cudaSuccess) rc = cuda_fail(e, "graph instantiate");
+        }
+        if (g) cudaGraphDestroy(g);
+        b->graph_in[i] = i == 0 ? fa0 : fb0;
+        b->fa = fa0;
+        b->fb = fb0;
+        if (rc) {
+            drop_graphs(b);
+            return rc;
+        }
+    }
     b->graph_k = b->k_idx;
     return MPH_OK;
 }
@@ -304,7 +336,9 @@ int advance_batch(mph_batch* b, int nsteps) {
     if (rc) return rc;
     rc = ensure_graph(b);
     if (rc) return rc;
-    for (int t = 0; t + 1 < nsteps; t += 2) MPH_CK(cudaGraphLaunch(b->graph, b->stream), "graph launch");
+    // The graph that starts from the buffer holding the state now.
+    const cudaGraphExec_t pair = b->fa == b->graph_in[0] ? b->graph[0] : b->graph[1];
+    for (int t = 0; t + 1 < nsteps; t += 2) MPH_CK(cudaGraphLaunch(pair, b->stream), "graph launch");
     if (nsteps % 2) {
         rc = step_once(b, b->k_idx);
         if (rc) return rc;
@@ -543,11 +577,7 @@ int mph_batch_set_obstacles(mph_batch* b, int domain, const unsigned char* mask)
     MPH_CK(cudaMemcpy(b->d_params + domain, &p, sizeof(KParams), cudaMemcpyHostToDevice), "batch parameters");
     int rc = build_walls(b);
     if (rc) return rc;
-    if (b->graph) {  // the captured steps name the old wall list
-        cudaGraphExecDestroy(b->graph);
-        b->graph = nullptr;
-        b->graph_k = -1;
-    }
+    drop_graphs(b);  // the captured steps name the old wall list
     return MPH_OK;
 }
 

@@ -111,3 +111,22 @@ def test_cavity_ensemble_draw(mph):
     sides = np.array([d.n[0] for d in descs])
     assert len(descs) == 512 and np.all((taus > 0.5) & (taus < 2.0))
     assert sides.min() >= 64 and sides.max() <= 512
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32", "f16s"])
+def test_odd_step_counts_between_graph_replays(precision, mph):
+    """Advances of odd length leave the state in the other buffer; the step
+    pairs replayed afterwards (CUDA graphs) must start from it: 1 + 15 + 2 + 3
+    steps, and a timed advance after an odd warm-up, equal single handles."""
+    descs = [_cavity(mph, (24, 24), 1.3, 0.1, precision), _cavity(mph, (40, 32), 1.6, 0.05, precision)]
+    b = mph.Batch(descs)
+    singles = [mph.Simulation(d) for d in descs]
+    for i, s in enumerate(singles):
+        b.initialize(i)
+        s.initialize()
+    for n in (1, 15, 2, 3):
+        b.advance(n)
+    b.advance_timed(6)
+    for i, s in enumerate(singles):
+        s.advance(27)
+        assert np.array_equal(b.f(i), s.f()), i
