@@ -175,8 +175,10 @@ int mph_set_obstacles(mph_sim* sim, const unsigned char* mask);
  * with u = (sum c f) / (sum f) of the stored populations,
  *   out[0] = ||u - u_prev||_2 / ||u||_2, out[1] = ||u||_2,
  * where u_prev is the field saved by the previous call (out[0] = +inf on the
- * first call after mph_create / mph_init_fields / mph_set_f).  Calling it
- * every k steps gives the relative change over k steps. */
+ * first call after a call that replaces the state: mph_create,
+ * mph_init_fields, mph_init_fields_neq, mph_set_f, mph_set_state,
+ * mph_step_host).  Calling it every k steps gives the relative change over
+ * k steps. */
 int mph_residual(mph_sim* sim, double* out);
 /* Velocity set of a lattice (LatticeDescriptor.H:23-263): c[3 n + d],
  * w[n], opp[n] for n < q; any pointer may be NULL. */

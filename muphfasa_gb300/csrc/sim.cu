@@ -874,6 +874,7 @@ int mph_launches_per_step(const mph_sim* s, int* n) {
 
 int mph_step_host(mph_sim* s, const double* f_in, double* f_out, int nsteps) {
     if (!s || !f_in || !f_out || nsteps < 0) return fail(MPH_ERR_ARG, "mph_step_host: bad argument");
+    s->has_uprev = false;  // the state is replaced, as by mph_set_f
     const int S = nsteps > 0 ? slab_count(s) : 0;
     if (S > 0) {
         s->has_state = true;
