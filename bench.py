@@ -13,11 +13,12 @@ Prints one JSON line (rank 0):
             populations from pinned host memory, advances, downloads them
   roofline  achieved HBM bandwidth of the step kernel (algorithmic bytes
             2*Q*8 per cell update) against the measured copy peak
-  cpu_baseline  the CPU oracle (restated reference CPU path) on the host
-            cores, bounded sample of the same workload
+  cpu_baseline  the reference's CPU step on the host cores, bounded sample of
+            the same workload: its own src/LBM code (built by
+            oracle/build_ref.sh from the checkout or the copy staged in
+            baseline/_ref, kind "reference"), else the restatement ("port")
 
---impl reference: the reference's CPU implementation of the step (the CPU
-oracle, restated from the reference sources) on the host cores with all
+--impl reference: the same reference CPU step on the host cores with all
 threads, on the same workload and metric.
 """
 from __future__ import annotations
@@ -132,13 +133,28 @@ def channel_fields(n, seed=20261203):
     return 1.0 + rng.uniform(-1e-4, 1e-4, N), np.zeros(3 * N)
 
 
-def cpu_reference(n, steps, warmup, threads):
-    """The restated reference CPU path on `threads` host threads: MLUPS."""
+def cpu_kind():
+    """'reference' when the reference's own LBM sources are built on this host
+    (oracle/_ref, from the checkout or the copy staged in baseline/_ref),
+    else 'port' (the restatement, bit-identical to it)."""
+    from oracle import oracle as O
+    if not O.ref_available():
+        try:
+            O.build_ref()
+        except Exception:
+            pass
+    return "reference" if O.ref_available() else "port"
+
+
+def cpu_reference(n, steps, warmup, threads, kind="port"):
+    """The reference CPU path on `threads` host threads: MLUPS.  kind
+    'reference' runs the reference's own pullCollideFusedMF (its OpenMP
+    MFIter loops over 8-cell tiles) and ghost fill; 'port' the restatement."""
     from oracle import oracle as O
     O.build()
     cfg = O.Config("D3Q19", n, omega=1.0 / 0.6, faces=["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic",
                                                        "Periodic"], force=(1e-6, 0.0, 0.0))
-    sim = O.OracleSim(cfg, "port")
+    sim = O.OracleSim(cfg, "ref" if kind == "reference" else "port")
     rho, u = channel_fields(n)
     sim.init_fields(rho, u)
     if warmup:
@@ -343,61 +359,79 @@ def run_reference(args):
         return 0
     threads = os.cpu_count() or 1
     n = (256, 256, 256)
-    value, dt = cpu_reference(n, args.steps, args.warmup, threads)
+    kind = cpu_kind()
+    value, dt = cpu_reference(n, args.steps, args.warmup, threads, kind)
+    what = ("the reference's own pullCollideFusedMF (src/LBM, OpenMP MFIter loops over 8-cell tiles) and ghost fill"
+            if kind == "reference" else "the restated reference CPU path, OpenMP over cells")
+    extra = {}
+    if kind == "reference":  # the restatement beside it, 5 steps
+        vp, _ = cpu_reference(n, 5, 1, threads, "port")
+        extra = {"port": {"value": round(vp, 3), "unit": "MLUPS", "sample": f"{n[0]}^3, 5 steps, {threads} threads"}}
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "MLUPS", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * dt / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"channel_d3q19_{args.n}^3", "lattice": "D3Q19", "grid": [args.n] * 3, "tau": 0.6,
                    "force": 1e-6, "sample_grid": list(n), "parallelism": "replicas"},
-        "cpu_baseline": {"value": round(value, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": round(value, 3), "unit": "MLUPS", "cores": threads, "kind": kind,
                          "sample": f"{n[0]}^3 domain of the workload, {args.steps} steps after {args.warmup} warm-up, "
-                                   f"OpenMP over cells, {threads} threads",
-                         "host": cpu_model()},
+                                   f"{what}, {threads} threads",
+                         "host": cpu_model(), **extra},
         "e2e": {"value": round(value, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
 
 
-def run_batch(args):
+def batch_measure(m, domains, steps, warmup, prec, device=0):
     """512 independent lid-driven cavities, D2Q9, side log-uniform in [64, 512],
-    Re log-uniform in [100, 5000] (tau = 0.5 + 3 u_lid N / Re), FP32 storage:
-    one batched kernel per step (CUDA graph) against one launch per domain."""
-    import muphfasa_gb300 as m
-    m.set_device(0)
-    prec = args.precision if args.precision in ("f32", "f16s", "bf16s", "f64", "f64_fast") else "f32"
-    descs = m.cavity_batch_descs(args.domains, precision=prec)
+    Re log-uniform in [100, 5000] (tau = 0.5 + 3 u_lid N / Re): one batched
+    kernel per step (CUDA graph) against one launch per domain.  Returns the
+    record (MLUPS, roofline, looped MLUPS) and the clock summary."""
+    descs = m.cavity_batch_descs(domains, precision=prec)
     batch = m.Batch(descs)
     for i in range(len(descs)):
         batch.initialize(i)
-    batch.advance(args.warmup)
+    batch.advance(warmup)
     total, kcells, nchunks, persistent = batch.info()
-    with ClockSampler(0) as clk:
-        ms = batch.advance_timed(args.steps)
-    ms_loop = batch.advance_looped_timed(max(2, args.steps // 4))
-    steps_loop = max(2, args.steps // 4)
-    q, es = 9, ELEM[prec]
-    value = total * args.steps / (ms / 1e3) / 1e6
-    looped = total * steps_loop / (ms_loop / 1e3) / 1e6
-    achieved = 2 * q * es * total / (ms / args.steps / 1e3) / 1e9
-    peak, kind = peaks()
-    line = {"metric": METRIC, "value": round(value, 3), "unit": "MLUPS", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[prec], "data": "synthetic",
-            "config": {"workload": f"batch{args.domains}_cavities_d2q9", "domains": args.domains, "total_cells": total,
-                       "side": [64, 512], "Re": [100, 5000], "lid": 0.1, "precision": prec,
-                       "cells_per_thread": kcells, "chunks": nchunks, "persistent_grid": persistent,
-                       "graph": "2-step CUDA graph"},
-            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": kind,
-                         "bytes_per_cell_update": 2 * q * es},
-            "looped_single_domain": {"value": round(looped, 3), "unit": "MLUPS", "launches_per_step": args.domains},
-            "clocks": clk.summary(),
-            # chunk kernel + wall-cell kernel per step (every cavity has walls)
-            "gpu_launches": 2 * args.steps}
-    print(json.dumps(line), flush=True)
+    with ClockSampler(device) as clk:
+        ms = batch.advance_timed(steps)
+    steps_loop = max(2, steps // 4)
+    ms_loop = batch.advance_looped_timed(steps_loop)
     batch.close()
+    q, es = 9, ELEM[prec]
+    value = total * steps / (ms / 1e3) / 1e6
+    looped = total * steps_loop / (ms_loop / 1e3) / 1e6
+    achieved = 2 * q * es * total / (ms / steps / 1e3) / 1e9
+    peak, kind = peaks()
+    rec = {"metric": METRIC, "value": round(value, 3), "unit": "MLUPS", "steps": steps, "warmup": warmup,
+           "ms_per_step": round(ms / steps, 4), "dtype": DTYPE[prec],
+           "config": {"workload": f"batch{domains}_cavities_d2q9", "domains": domains, "total_cells": total,
+                      "side": [64, 512], "Re": [100, 5000], "lid": 0.1, "precision": prec,
+                      "cells_per_thread": kcells, "chunks": nchunks, "persistent_grid": persistent,
+                      "graph": "2-step CUDA graph", "l2": "inputs larger than L2 (no flush needed)"},
+           "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": kind,
+                        "bytes_per_cell_update": 2 * q * es},
+           "looped_single_domain": {"value": round(looped, 3), "unit": "MLUPS", "steps": steps_loop,
+                                    "launches_per_step": domains},
+           # chunk kernel + wall-cell kernel per step (every cavity has walls)
+           "gpu_launches": 2 * steps}
+    return rec, clk.summary()
+
+
+def run_batch(args):
+    import muphfasa_gb300 as m
+    m.set_device(0)
+    prec = args.precision if args.precision in ("f32", "f16s", "bf16s", "f64", "f64_fast", "f64x") else "f32"
+    rec, clocks = batch_measure(m, args.domains, args.steps, args.warmup, prec)
+    line = {k: rec[k] for k in ("metric", "value", "unit")}
+    line.update({"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": rec["ms_per_step"],
+                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": rec["dtype"],
+                 "data": "synthetic", "config": rec["config"], "roofline": rec["roofline"],
+                 "looped_single_domain": rec["looped_single_domain"], "clocks": clocks,
+                 "gpu_launches": rec["gpu_launches"]})
+    print(json.dumps(line), flush=True)
     return 0
 
 
@@ -412,8 +446,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--e2e-sweep", default="", help="comma-separated slab counts of the step_host pipeline to time")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--secondary-steps", type=int, default=40,
+                    help="steps of the 512-cavity batch record added to the channel line (0: skip)")
     ap.add_argument("--domains", type=int, default=512, help="domains of the batch512 workload")
-    ap.add_argument("--probes", action="store_true", help="build and run bench_probes.cu (pipe rates, pull-copy)")
     ap.add_argument("--workload", default="channel", choices=["channel", "batch512", "tgv3d", "warmstart"],
                     help="channel: the D3Q19 channel (headline); batch512: 512 uneven D2Q9 cavities; "
                          "tgv3d: the D3Q27 precision study (use --n 384)")
@@ -433,12 +468,6 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
-    if args.probes:
-        exe = os.path.join(ROOT, "muphfasa_gb300", "_build", "bench_probes")
-        os.makedirs(os.path.dirname(exe), exist_ok=True)
-        subprocess.run(["nvcc", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-o", exe,
-                        os.path.join(ROOT, "bench_probes.cu")], check=True)
-        return subprocess.run([exe]).returncode
     if args.workload == "tgv3d":
         return run_tgv3d(args)
     if args.workload == "warmstart":
@@ -520,16 +549,32 @@ def main():
     except Exception as ex:  # report, do not hide
         e2e = {"value": None, "unit": "MLUPS", "error": str(ex)[:200]}
 
+    # Secondary record: the 512-cavity batch (FP32, 40 steps), timed in the
+    # same run so its roofline fraction is on the driver's record.
+    secondary = None
+    if rank == 0 and args.secondary_steps > 0:
+        try:
+            rec, bclk = batch_measure(m, 512, args.secondary_steps, 4, "f32", device=local)
+            rec["clocks"] = bclk
+            secondary = {"batch512": rec}
+        except Exception as ex:  # report, do not hide
+            secondary = {"batch512": {"error": str(ex)[:200]}}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         sn = (256, 256, 256)
-        v, dt = cpu_reference(sn, 20, 1, threads)
-        v1, dt1 = cpu_reference((128, 128, 128), 10, 1, 1)
-        cpu = {"value": round(v, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
-               "sample": f"{sn[0]}^3 domain of the workload, 20 steps after 1 warm-up, FP64, OpenMP {threads} threads "
-                         f"({dt:.2f} s)",
-               "single_thread": {"value": round(v1, 3), "sample": f"128^3, 10 steps, 1 thread ({dt1:.2f} s)"},
+        kind = cpu_kind()
+        v, dt = cpu_reference(sn, 20 if kind == "port" else 10, 1, threads, kind)
+        v1, dt1 = cpu_reference((128, 128, 128), 4, 1, 1, kind)
+        vp, dtp = cpu_reference(sn, 10, 1, threads, "port")
+        cpu = {"value": round(v, 3), "unit": "MLUPS", "cores": threads, "kind": kind,
+               "sample": f"{sn[0]}^3 domain of the workload, {20 if kind == 'port' else 10} steps after 1 warm-up, "
+                         f"FP64, OpenMP {threads} threads ({dt:.2f} s)"
+                         + ("; the reference's own src/LBM code" if kind == "reference" else ""),
+               "single_thread": {"value": round(v1, 3), "sample": f"128^3, 4 steps, 1 thread ({dt1:.2f} s)"},
+               "port": {"value": round(vp, 3), "sample": f"the restatement, {sn[0]}^3, 10 steps, {threads} threads "
+                                                          f"({dtp:.2f} s)"},
                "host": cpu_model()}
 
     if rank == 0:
@@ -548,6 +593,7 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": args.steps * sim.launches_per_step(),
+            "secondary": secondary,
         }
         print(json.dumps(line), flush=True)
     sim.close()

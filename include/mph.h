@@ -242,9 +242,11 @@ int mph_bc_fill_arr(int dim, int q, const int dom_lo[3], const int dom_hi[3],
  * process): one kernel per step covers every domain through a flat tile list,
  * step pairs are replayed from a CUDA graph, and the tile shape is chosen by
  * timing the candidates on the batch itself.  All domains share lattice,
- * precision (not MPH_PREC_F64X) and forcing flag; each has its own size,
+ * precision (any MPH_PREC_*) and forcing flag; each has its own size,
  * omega, boundary faces and force.  Domain d's results equal those of a
- * single handle created from descs[d]. */
+ * single handle created from descs[d], bit for bit.  With MPH_PREC_F64X a
+ * cell leaving the fixed-point range makes the advance return
+ * MPH_ERR_NONFINITE, as for a single handle. */
 typedef struct mph_batch mph_batch;
 int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out);
 int mph_batch_destroy(mph_batch* b);
@@ -284,7 +286,10 @@ int mph_batch_info(const mph_batch* b, long long* total_cells, int* cells_per_th
  * ncell at 134,217,728 (2048 slots x 65536 cells); larger sizes return
  * MPH_ERR_ARG.  No cudaMalloc/cudaFree or other allocating call is made.  The
  * first call on a device looks up the array's device address (once per
- * device), so that first call should come before any stream capture.  Every
+ * device), so that first call should come before any stream capture.  The
+ * address stays cached for the life of the process: after cudaDeviceReset on
+ * a device the library image is reloaded and the array may move, so do not
+ * call this entry point on that device again in the same process.  Every
  * call shares the one array: calls that overlap on the GPU race and must be
  * ordered by the caller.  Nothing in the array needs to start at zero; every
  * slot a call reads is written earlier in the same call. */

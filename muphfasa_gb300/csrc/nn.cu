@@ -137,13 +137,41 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf
 // BF16 in, FP32 accumulate in TMEM) and commits them to an mbarrier that every
 // thread waits on before the buffer is refilled.  Each warp then reads its 32
 // TMEM lanes (rows) with tcgen05.ld.  Every wait is bounded: on timeout the
-// kernel records an error flag and skips its tile.
+// kernel records an error flag and skips its tile.  The outcome of a wait is
+// combined over the block (__syncthreads_and) before anything depends on it,
+// so every thread leaves the K loop at the same iteration and the warp-
+// collective tcgen05.ld / dealloc see one decision.  After a timeout the
+// dealloc is best effort: MMAs still in flight may write the released
+// columns, and the tile's result is discarded.
 constexpr int TC_BM = 128, TC_BN = 64, TC_BK = 64;
+// A wait gives up after kWaitNs of %globaltimer time (checked every 256
+// polls) or kSpinLimit polls, whichever comes first.
 constexpr unsigned long long kSpinLimit = 1ull << 26;
+constexpr unsigned long long kWaitNs = 250ull * 1000 * 1000;
 
 __device__ int g_nn_timeout = 0;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    return t;
+}
+
+// Bounded wait for phase `phase` of the mbarrier at shared address `addr`.
+__device__ __forceinline__ bool mbar_wait(unsigned addr, unsigned phase) {
+    unsigned done = 0;
+    const unsigned long long t0 = global_ns();
+    for (unsigned long long it = 0; it < kSpinLimit && !done; ++it) {
+        asm volatile(
+            "{\n.reg .pred q;\nmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\nselp.u32 %0, 1, 0, q;\n}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(phase));
+        if (!done && (it & 255) == 255 && global_ns() - t0 > kWaitNs) break;
+    }
+    return done != 0;
+}
 
 // Core-matrix layout offset (bytes) of element (row, k) in a rows x TC_BK tile.
 __device__ __forceinline__ unsigned cm_off(int row, int k) {
@@ -259,21 +287,13 @@ __global__ void __launch_bounds__(128) k_gemm_tc05(int M, int N, int K, const bf
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
                 smem_u32(&mbar)));
         }
-        // Every thread waits for the MMAs (they read the staged tiles).
-        unsigned done = 0;
-        for (unsigned long long it = 0; it < kSpinLimit && !done; ++it) {
-            asm volatile(
-                "{\n.reg .pred q;\nmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\nselp.u32 %0, 1, 0, q;\n}\n"
-                : "=r"(done)
-                : "r"(smem_u32(&mbar)), "r"(phase));
-        }
-        if (!done) {
-            ok = false;
-            atomicExch(&g_nn_timeout, 1);
-        }
+        // Every thread waits for the MMAs (they read the staged tiles); the
+        // block continues only if every thread's wait succeeded.
+        const bool done = mbar_wait(smem_u32(&mbar), phase);
         phase ^= 1;
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-        __syncthreads();
+        ok = __syncthreads_and(done) != 0;
+        if (!ok && tid == 0) atomicExch(&g_nn_timeout, 1);
     }
     if (ok) {
         // Warp w reads TMEM lanes 32 w .. 32 w + 31 (rows), 64 columns.
@@ -360,17 +380,6 @@ __device__ __forceinline__ void tp_stage(unsigned char* dst, const bf16* __restr
     }
 }
 
-__device__ __forceinline__ bool mbar_wait(unsigned addr, unsigned phase) {
-    unsigned done = 0;
-    for (unsigned long long it = 0; it < kSpinLimit && !done; ++it) {
-        asm volatile(
-            "{\n.reg .pred q;\nmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\nselp.u32 %0, 1, 0, q;\n}\n"
-            : "=r"(done)
-            : "r"(addr), "r"(phase));
-    }
-    return done != 0;
-}
-
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(128) k_gemm_tc05p(int M, int N, int K, const bf16* __restrict__ A, long long lda,
                                                     const bf16* __restrict__ B, long long ldb, float* __restrict__ C,
@@ -434,14 +443,13 @@ __global__ void __launch_bounds__(128) k_gemm_tc05p(int M, int N, int K, const b
         }
         // refill the stage of slice t - 1 with slice t + STAGES - 1
         const int tn = t + TP_STAGES - 1;
-        if (tn < nk) {
+        if (tn < nk) {  // uniform over the block (t and nk are)
             const int sn = tn % TP_STAGES;
             if (t >= 1) {
-                if (!mbar_wait(smem_u32(&mbar[sn]), phase[sn])) {
-                    ok = false;
-                    atomicExch(&g_nn_timeout, 1);
-                }
+                const bool done = mbar_wait(smem_u32(&mbar[sn]), phase[sn]);
                 phase[sn] ^= 1;
+                ok = __syncthreads_and(done) != 0;
+                if (!ok && tid == 0) atomicExch(&g_nn_timeout, 1);
             }
             if (ok) {
                 tp_stage<TA, TC_BM>(As[sn], A, lda, m0, M, kb + tn * TP_BK, ke, a_vec);
@@ -451,15 +459,12 @@ __global__ void __launch_bounds__(128) k_gemm_tc05p(int M, int N, int K, const b
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     }
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-    if (ok) {
-        const int sl = (nk - 1) % TP_STAGES;
-        if (!mbar_wait(smem_u32(&mbar[sl]), phase[sl])) {
-            ok = false;
-            atomicExch(&g_nn_timeout, 1);
-        }
-    }
+    bool done = true;
+    if (ok) done = mbar_wait(smem_u32(&mbar[(nk - 1) % TP_STAGES]), phase[(nk - 1) % TP_STAGES]);
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-    __syncthreads();
+    const bool last_ok = __syncthreads_and(done) != 0;
+    if (ok && !last_ok && tid == 0) atomicExch(&g_nn_timeout, 1);
+    ok = ok && last_ok;
     if (ok) {
         float acc[TC_BN];
         unsigned r[TC_BN];

@@ -70,11 +70,21 @@ def build(verbose: bool = False) -> str:
     return LIB_PATH
 
 
+# Root of a reference checkout: the MPH_REFERENCE_ROOT environment variable,
+# else the default of build_ref.sh.  Hosts without a checkout build the copy
+# of its src/LBM that build_ref.sh stages under baseline/_ref/.
+REFERENCE_ROOT = os.environ.get("MPH_REFERENCE_ROOT") or "/root/reference"
+STAGED_SRC = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "src")
+
+
 def build_ref() -> bool:
-    """Builds oracle/_ref from the reference sources when they are present."""
-    if not os.path.isdir("/root/reference/src"):
-        return False
-    subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True, capture_output=True)
+    """Builds oracle/_ref from the reference sources (the checkout, else the
+    staged copy) when either is present; True when the libraries exist."""
+    srcs = [os.path.join(REFERENCE_ROOT, "src", "LBM", "Collision.cpp"),
+            os.path.join(STAGED_SRC, "LBM", "Collision.cpp")]
+    if not any(os.path.exists(p) for p in srcs):
+        return ref_available()
+    subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT], check=True, capture_output=True)
     return ref_available()
 
 

@@ -119,12 +119,36 @@ struct Impl : Base {
         std::memcpy(f, fin.fab().data().data(), sizeof(double) * fin.fab().data().size());
     }
 
+    // f(i, j, k) on every ghost cell of the ghost-grown box: whole rows
+    // outside the domain in y or z, the row ends otherwise.  Rows are
+    // independent (each pass reads valid cells only and writes its own ghost
+    // cell), so they are shared among the OpenMP threads.
+    template <class F>
+    void for_each_ghost(const amrex::Box& gbox, F&& f) const {
+        const int j0 = gbox.smallEnd(1), nj = gbox.length(1);
+        const int k0 = D == 3 ? gbox.smallEnd(2) : 0, nk = D == 3 ? gbox.length(2) : 1;
+        const long long rows = (long long)nj * nk;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+        for (long long r = 0; r < rows; ++r) {
+            const int j = j0 + (int)(r % nj), k = k0 + (int)(r / nj);
+            const bool inside = j >= dom.smallEnd(1) && j <= dom.bigEnd(1) &&
+                                (D == 2 || (k >= dom.smallEnd(D - 1) && k <= dom.bigEnd(D - 1)));
+            for (int i = gbox.smallEnd(0); i <= gbox.bigEnd(0); ++i) {
+                if (inside && i == dom.smallEnd(0)) i = dom.bigEnd(0) + 1;  // skip the valid run
+                if (i > gbox.bigEnd(0)) break;
+                f(i, j, k);
+            }
+        }
+    }
+
     // fillGhostCells: FillBoundary(periodicity), then PhysBCFunct calling
     // BCManager on the ghost cells outside the domain.
     void fill() override {
         auto a = fin.fab().array();
         const amrex::Box gbox = fin.fab().box();
-        amrex::ParallelFor(gbox, [&](int i, int j, int k) {
+        for_each_ghost(gbox, [&](int i, int j, int k) {
             amrex::IntVect iv(AMREX_D_DECL(i, j, k));
             if (dom.contains(iv)) return;
             amrex::IntVect img = iv;
@@ -137,7 +161,7 @@ struct Impl : Base {
             for (int n = 0; n < L::Q; ++n) a(iv, n) = a(img, n);
         });
         const amrex::GeometryData gd = geom.data();
-        amrex::ParallelFor(gbox, [&](int i, int j, int k) {
+        for_each_ghost(gbox, [&](int i, int j, int k) {
             amrex::IntVect iv(AMREX_D_DECL(i, j, k));
             if (dom.contains(iv)) return;
             bcm(iv, a, 0, L::Q, gd, 0.0, &bcr, 0, 0);
@@ -293,7 +317,14 @@ int orc_get_f_ghost(void* s, double* f) { static_cast<Base*>(s)->getFG(f); retur
 int orc_fill_ghosts(void* s) {
     try { static_cast<Base*>(s)->fill(); return 0; } catch (...) { return 1; }
 }
-int orc_step(void* s, int nsteps, int) {
+// nthreads > 0 sets the OpenMP thread count of the reference's
+// `#pragma omp parallel` MFIter loops (a build with -fopenmp).
+int orc_step(void* s, int nsteps, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
     try { static_cast<Base*>(s)->step(nsteps); return 0; } catch (...) { return 1; }
 }
 int orc_init_fields(void* s, double* rho, double* u) {

@@ -8,6 +8,7 @@
 #ifndef MPH_AMREX_STANDIN_H
 #define MPH_AMREX_STANDIN_H
 
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <cstddef>
@@ -20,6 +21,9 @@
 
 #ifndef AMREX_SPACEDIM
 #error "AMREX_SPACEDIM must be defined"
+#endif
+#ifdef _OPENMP
+#include <omp.h>
 #endif
 
 #define AMREX_GPU_HOST_DEVICE
@@ -157,22 +161,29 @@ private:
 
 class MultiFab;
 
+// Iterator over the tiles of the one box.  With tiling the valid box is cut
+// into tiles of full rows along x and 8 cells along each further direction
+// (AMReX's default CPU tile shape), enumerated x-fastest; inside an OpenMP
+// parallel region each thread takes its own contiguous share of the tiles,
+// the first (tiles mod threads) threads one extra, so the reference's
+// `#pragma omp parallel` MFIter loops run on every host thread.
 class MFIter {
 public:
-    template <class... Args>
-    explicit MFIter(const MultiFab& mf, Args&&...) : m_mf(&mf) {}
-    bool isValid() const noexcept { return m_i == 0; }
+    explicit MFIter(const MultiFab& mf, bool tiling = false);
+    bool isValid() const noexcept { return m_i < m_end; }
     MFIter& operator++() noexcept { ++m_i; return *this; }
-    int index() const noexcept { return m_i; }
+    int index() const noexcept { return 0; }
     Box tilebox() const;
     Box validbox() const;
     Box fabbox() const;
 private:
     const MultiFab* m_mf;
-    int m_i = 0;
+    int m_i = 0, m_end = 1;
+    int m_nt[3] = {1, 1, 1};  // tiles per direction
+    int m_ts[3] = {0, 0, 0};  // tile extent per direction (0: whole box)
 };
 
-inline bool TilingIfNotGPU() { return false; }
+inline bool TilingIfNotGPU() { return true; }
 
 // A single-box MultiFab: valid box plus nGhost layers (no k ghosts in 2-D).
 class MultiFab {
@@ -201,7 +212,42 @@ private:
     FArrayBox m_fab;
 };
 
-inline Box MFIter::tilebox() const { return m_mf->validBox(); }
+inline MFIter::MFIter(const MultiFab& mf, bool tiling) : m_mf(&mf) {
+    const Box& v = mf.validBox();
+    int total = 1;
+    if (tiling) {
+        for (int d = 1; d < AMREX_SPACEDIM; ++d) {
+            m_ts[d] = 8;
+            m_nt[d] = (v.length(d) + 7) / 8;
+            total *= m_nt[d];
+        }
+    }
+    int first = 0, count = total;
+#ifdef _OPENMP
+    if (omp_in_parallel()) {
+        const int nth = omp_get_num_threads(), tid = omp_get_thread_num();
+        const int base = total / nth, extra = total % nth;
+        count = base + (tid < extra ? 1 : 0);
+        first = tid * base + (tid < extra ? tid : extra);
+    }
+#endif
+    m_i = first;
+    m_end = first + count;
+}
+
+inline Box MFIter::tilebox() const {
+    const Box& v = m_mf->validBox();
+    if (m_ts[1] == 0) return v;
+    IntVect lo = v.smallEnd(), hi = v.bigEnd();
+    int t = m_i;
+    for (int d = 1; d < AMREX_SPACEDIM; ++d) {
+        const int td = t % m_nt[d];
+        t /= m_nt[d];
+        lo[d] = v.smallEnd(d) + td * m_ts[d];
+        hi[d] = std::min(lo[d] + m_ts[d] - 1, v.bigEnd(d));
+    }
+    return Box(lo, hi);
+}
 inline Box MFIter::validbox() const { return m_mf->validBox(); }
 inline Box MFIter::fabbox() const { return m_mf->fab().box(); }
 

@@ -45,7 +45,7 @@ def test_derive_matches_reference_units_bitwise(fn, mph):
 def test_reference_inputs_files_parse(mph, oracle_mod):
     """The reference's own inputs files (read where they lie) derive the same
     omega and force as the oracle's unit chain."""
-    ref = "/root/reference"
+    ref = oracle_mod.REFERENCE_ROOT
     files = []
     for dp, _, fns in os.walk(ref):
         files += [os.path.join(dp, f) for f in fns if re.match(r"inputs(\.\w+|3d.*|_\w+)?$", f)]

@@ -60,6 +60,30 @@ def test_oracle_matches_reference_build_directly(oracle_mod):
         assert np.array_equal(a.get_f(), b.get_f())
 
 
+def test_reference_build_threaded_tiles_match_oracle(oracle_mod):
+    """The reference build's OpenMP MFIter loops over 8-cell tiles (the form
+    the reference arm of the benchmark times) give the restatement's bits:
+    ragged last tiles along y and z, 4 threads over 9-12 tiles."""
+    O = oracle_mod
+    if not O.ref_available():
+        pytest.skip("reference-source build (oracle/_ref) not present on this host")
+    rng = np.random.default_rng(5)
+    for lat, n in (("D2Q9", (13, 70)), ("D3Q19", (10, 21, 27)), ("D3Q27", (7, 17, 12))):
+        dim = O.LATTICE_DQ[lat][0]
+        faces = ["Periodic", "Periodic", "NoSlip", "MovingWall", "Periodic", "Periodic"]
+        U = [[0.0] * 3 for _ in range(6)]
+        U[3][0] = 0.05
+        cfg = O.Config(lat, n, omega=1.6, faces=faces, face_U=U, force=(1e-5, 0.0, 0.0))
+        a, b = O.OracleSim(cfg, "port"), O.OracleSim(cfg, "ref")
+        N = a.N
+        rho, u = 1 + 0.01 * rng.standard_normal(N), 0.02 * rng.standard_normal(dim * N)
+        a.init_fields(rho, u)
+        b.init_fields(rho, u)
+        a.step(12, 2)
+        b.step(12, 4)
+        assert np.array_equal(a.get_f(), b.get_f()), lat
+
+
 def _lattice(O, lat):
     """Velocity table of the oracle's lattice recovered through its moments:
     equilibrium populations at rho = 1, u = 0 are the weights."""

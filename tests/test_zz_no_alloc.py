@@ -16,7 +16,12 @@ def _fields(rng, N, dim):
     return 1.0 + 0.01 * rng.standard_normal(N), 0.04 * rng.standard_normal(dim * N)
 
 
-@pytest.mark.parametrize("lat,n", [("D3Q19", (40, 36, 32)), ("D2Q9", (300, 257))])
+# Cell counts against the 65,536-cell chunk of each scratch slot: one partial
+# chunk (D3Q19, 46,080 cells), and two chunks with a partial last one for every
+# lattice (D2Q9 77,100; D3Q15 72,000; D3Q27 84,480), so the cz terms of the
+# 3-D lattices and the multi-slot final pass are both covered.
+@pytest.mark.parametrize("lat,n", [("D3Q19", (40, 36, 32)), ("D2Q9", (300, 257)), ("D3Q15", (50, 40, 36)),
+                                   ("D3Q27", (48, 44, 40))])
 def test_noalloc_sums_match_handle_sums_twice(lat, n, mph):
     torch = pytest.importorskip("torch")
     dim, q = mph.LATTICE_DQ[lat]
