@@ -37,10 +37,14 @@ using namespace mph;
 
 namespace {
 
+// dpx, kbb and flag are used by the fixed-point precision only.
 cudaError_t launch_batch(int prec, int q, bool forced, int K, bool P, const void* fin, void* fout, const Chunk* chunks,
                          int nchunks, const int2* walls, int nwalls, const KParams* dp, const long long* offs,
-                         cudaStream_t s) {
+                         const KParamsX* dpx, const long long* kbb, int* flag, cudaStream_t s) {
     switch (prec) {
+        case MPH_PREC_F64X:
+            return launch_batch_f64x(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, dpx, offs, kbb,
+                                     flag, s);
         case MPH_PREC_F64:
             return launch_batch_exact(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
         case MPH_PREC_F64_FAST:
@@ -56,7 +60,8 @@ cudaError_t launch_batch(int prec, int q, bool forced, int K, bool P, const void
 size_t elem_of(int prec) {
     switch (prec) {
         case MPH_PREC_F64:
-        case MPH_PREC_F64_FAST: return 8;
+        case MPH_PREC_F64_FAST:
+        case MPH_PREC_F64X: return 8;
         case MPH_PREC_F32: return 4;
         case MPH_PREC_F16S:
         case MPH_PREC_BF16S: return 2;
@@ -66,11 +71,18 @@ size_t elem_of(int prec) {
 
 // Candidates of the autotuner: cand % 3 selects K, the cells per thread (a
 // chunk is 256 K cells), cand / 3 a persistent grid; the shifted 16-bit
-// policies take cells in pairs, so K = 1 is skipped for them.
+// policies take cells in pairs, so K = 1 is skipped for them, and the
+// fixed-point step holds at most two cells of int64 populations per thread,
+// so K = 4 is skipped for it.
 constexpr int kCells[3] = {1, 2, 4};
 constexpr int kCands = 6;
 
 bool shifted(int prec) { return prec == MPH_PREC_F16S || prec == MPH_PREC_BF16S; }
+bool candidate_ok(int prec, int cand) {
+    if (shifted(prec)) return cand % 3 != 0;
+    if (prec == MPH_PREC_F64X) return cand % 3 != 2;
+    return true;
+}
 
 // Autotuner cache: (q, precision, log2 total cells, log2 domains) -> K index.
 std::mutex g_tune_mu;
@@ -81,6 +93,8 @@ std::map<std::tuple<int, int, int, int>, int> g_tune;
 // Defined in sim.cu (shared with single domains).
 namespace mph {
 void build_params_public(const mph_desc& d, const mph_resolved_bc* tab, KParams& kp);
+void build_fixed_public(const mph_desc& d, const mph_resolved_bc* tab, const KParams& kp, KParamsX& px,
+                        long long* kbb);
 void build_cls(const KParams& p, int q, const unsigned char* mask, unsigned char* cls);
 }
 namespace mph {
@@ -102,6 +116,12 @@ struct mph_batch {
     double* d_u = nullptr;
     long long max_cells = 0;
     std::vector<KParams> params_h;
+    // fixed-point precision: per-domain constants, bounce-back tables
+    // (27 x 27 per domain) and the range flag of the step kernels
+    std::vector<KParamsX> px_h;
+    KParamsX* d_px = nullptr;
+    long long* d_kbb = nullptr;
+    int* d_flag = nullptr;
     // cells needing the boundary rules {domain, cell}
     int2* d_walls = nullptr;
     int nwalls = 0;
@@ -156,6 +176,9 @@ void free_batch(mph_batch* b) {
     cudaFree(b->d_rout);
     cudaFree(b->d_walls);
     cudaFree(b->d_cls);
+    cudaFree(b->d_px);
+    cudaFree(b->d_kbb);
+    cudaFree(b->d_flag);
     for (cudaGraphExec_t g : b->graph)
         if (g) cudaGraphExecDestroy(g);
     if (b->ev0) cudaEventDestroy(b->ev0);
@@ -223,7 +246,7 @@ int build_walls(mph_batch* b) {
 int step_once(mph_batch* b, int cand) {
     const int ki = cand % 3;
     MPH_CK(launch_batch(b->prec, b->q, b->forced, kCells[ki], cand >= 3, b->fa, b->fb, b->d_chunks[ki], b->nchunks[ki],
-                        b->d_walls, b->nwalls, b->d_params, b->d_offs, b->stream),
+                        b->d_walls, b->nwalls, b->d_params, b->d_offs, b->d_px, b->d_kbb, b->d_flag, b->stream),
            "batch step launch");
     std::swap(b->fa, b->fb);
     return MPH_OK;
@@ -238,8 +261,9 @@ int autotune(mph_batch* b) {
     // MPH_BATCH_CANDIDATE=c (0..5) fixes the launch instead of timing.
     if (const char* env = std::getenv("MPH_BATCH_CANDIDATE")) {
         const int c = std::atoi(env);
-        if (c < 0 || c >= kCands || (shifted(b->prec) && c % 3 == 0))
-            return fail(MPH_ERR_ARG, "MPH_BATCH_CANDIDATE must be 0..5 (1, 2, 4, 5 for 16-bit storage)");
+        if (c < 0 || c >= kCands || !candidate_ok(b->prec, c))
+            return fail(MPH_ERR_ARG, "MPH_BATCH_CANDIDATE must be 0..5 (1, 2, 4, 5 for 16-bit storage; "
+                                     "0, 1, 3, 4 for fixed point)");
         b->k_idx = c;
         return ensure_chunks(b, c % 3);
     }
@@ -260,7 +284,7 @@ int autotune(mph_batch* b) {
     float best = 1e30f;
     int besti = shifted(b->prec) ? 1 : 0;
     for (int wi = 0; wi < kCands && e == cudaSuccess; ++wi) {
-        if (shifted(b->prec) && wi % 3 == 0) continue;
+        if (!candidate_ok(b->prec, wi)) continue;
         int rc = ensure_chunks(b, wi % 3);
         if (rc) { cudaFree(save); return rc; }
         rc = step_once(b, wi);
@@ -276,6 +300,8 @@ int autotune(mph_batch* b) {
         if (e == cudaSuccess && ms < best) { best = ms; besti = wi; }
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->fa, save, bytes, cudaMemcpyDeviceToDevice, b->stream);
+    // only the steps of the caller's advances report the range flag
+    if (e == cudaSuccess && b->d_flag) e = cudaMemsetAsync(b->d_flag, 0, sizeof(int), b->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     cudaFree(save);
     if (e != cudaSuccess) return cuda_fail(e, "autotune");
@@ -331,6 +357,20 @@ int ensure_graph(mph_batch* b) {
     return MPH_OK;
 }
 
+// Range flag of the fixed-point step (read and cleared after an advance).
+int check_flag(mph_batch* b) {
+    if (!b->d_flag) return MPH_OK;
+    int flag = 0;
+    MPH_CK(cudaMemcpyAsync(&flag, b->d_flag, sizeof(int), cudaMemcpyDeviceToHost, b->stream), "read flag");
+    MPH_CK(cudaStreamSynchronize(b->stream), "read flag");
+    if (flag) {
+        MPH_CK(cudaMemsetAsync(b->d_flag, 0, sizeof(int), b->stream), "clear flag");
+        return fail(MPH_ERR_NONFINITE, "fixed-point batch step: a cell left the representable range "
+                                       "(rho outside (1/16, 64) or |J|, |u| >= 4)");
+    }
+    return MPH_OK;
+}
+
 int advance_batch(mph_batch* b, int nsteps) {
     int rc = autotune(b);
     if (rc) return rc;
@@ -363,6 +403,7 @@ int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out) {
     if (elem_of(b->prec) == 0) { delete b; return fail(MPH_ERR_UNSUPPORTED, "mph_batch_create: precision not supported in a batch"); }
     b->descs.assign(descs, descs + ndomains);
     b->params_h.resize(ndomains);
+    std::vector<long long> kbb_h;  // fixed-point bounce-back tables
     b->cls_h.resize(ndomains);
     long long off = 0;
     for (int d = 0; d < ndomains; ++d) {
@@ -376,6 +417,12 @@ int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out) {
         for (int a = 0; a < ds.dim; ++a)
             if (ds.n[a] < 1) { delete b; return fail(MPH_ERR_ARG, "mph_batch_create: cell counts must be positive"); }
         if (!(ds.omega > 0.0 && ds.omega < 2.0)) { delete b; return fail(MPH_ERR_CONFIG, "mph_batch_create: omega must lie in (0, 2)"); }
+        if (ds.precision == MPH_PREC_F64X && ds.forced)
+            for (int a = 0; a < ds.dim; ++a)
+                if (!(std::fabs(ds.force[a]) < 0.5 * ds.omega)) {
+                    delete b;
+                    return fail(MPH_ERR_CONFIG, "mph_batch_create: fixed-point precision needs |force| < omega / 2");
+                }
         // Chunk coordinates pack y | z << 16 and divide by float reciprocals;
         // element indices within a domain are 32-bit.
         if (ds.n[0] > (1 << 23) || ds.n[1] > 65535 || ds.n[2] > 32767 ||
@@ -388,6 +435,11 @@ int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out) {
         int rc = resolve_table(ds, tab);
         if (rc) { delete b; return rc; }
         build_params_public(ds, tab, b->params_h[d]);
+        if (b->prec == MPH_PREC_F64X) {
+            b->px_h.resize(ndomains);
+            kbb_h.resize((size_t)ndomains * 27 * 27);
+            build_fixed_public(ds, tab, b->params_h[d], b->px_h[d], kbb_h.data() + (size_t)d * 27 * 27);
+        }
         const long long cells = (long long)ds.n[0] * ds.n[1] * ds.n[2];
         b->offs_h.push_back(off);
         b->coffs_h.push_back(b->total_cells);
@@ -409,6 +461,16 @@ int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out) {
     if (e == cudaSuccess) e = cudaMemcpy(b->d_params, b->params_h.data(), sizeof(KParams) * ndomains, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_offs, sizeof(long long) * ndomains);
     if (e == cudaSuccess) e = cudaMemcpy(b->d_offs, b->offs_h.data(), sizeof(long long) * ndomains, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && b->prec == MPH_PREC_F64X) {
+        e = cudaMalloc(&b->d_px, sizeof(KParamsX) * ndomains);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(b->d_px, b->px_h.data(), sizeof(KParamsX) * ndomains, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMalloc(&b->d_kbb, sizeof(long long) * kbb_h.size());
+        if (e == cudaSuccess)
+            e = cudaMemcpy(b->d_kbb, kbb_h.data(), sizeof(long long) * kbb_h.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMalloc(&b->d_flag, sizeof(int));
+        if (e == cudaSuccess) e = cudaMemset(b->d_flag, 0, sizeof(int));
+    }
     if (e != cudaSuccess) {
         int rc = cuda_fail(e, "mph_batch_create");
         free_batch(b);
@@ -477,7 +539,7 @@ int mph_batch_advance(mph_batch* b, int nsteps) {
     int rc = advance_batch(b, nsteps);
     if (rc) return rc;
     MPH_CK(cudaStreamSynchronize(b->stream), "mph_batch_advance");
-    return MPH_OK;
+    return check_flag(b);
 }
 
 int mph_batch_advance_timed(mph_batch* b, int nsteps, float* ms) {
@@ -491,7 +553,7 @@ int mph_batch_advance_timed(mph_batch* b, int nsteps, float* ms) {
     MPH_CK(cudaEventRecord(b->ev1, b->stream), "event");
     MPH_CK(cudaEventSynchronize(b->ev1), "event sync");
     MPH_CK(cudaEventElapsedTime(ms, b->ev0, b->ev1), "event elapsed");
-    return MPH_OK;
+    return check_flag(b);
 }
 
 int mph_batch_advance_looped_timed(mph_batch* b, int nsteps, float* ms) {
@@ -511,6 +573,10 @@ int mph_batch_advance_looped_timed(mph_batch* b, int nsteps, float* ms) {
                 case MPH_PREC_F32: e = launch_step_fast_f32(b->q, b->forced, (const float*)in, (float*)outp, kp, pg, b->stream); break;
                 case MPH_PREC_F16S: e = launch_step_fast_f16s(b->q, b->forced, in, outp, kp, pg, b->stream); break;
                 case MPH_PREC_BF16S: e = launch_step_fast_bf16s(b->q, b->forced, in, outp, kp, pg, b->stream); break;
+                case MPH_PREC_F64X:
+                    e = launch_step_f64x(b->q, b->forced, (const long long*)in, (long long*)outp, kp, b->px_h[d], pg,
+                                         b->d_kbb + (size_t)d * 27 * 27, b->d_flag, b->stream);
+                    break;
             }
             if (e != cudaSuccess) return cuda_fail(e, "looped step launch");
         }
@@ -520,7 +586,7 @@ int mph_batch_advance_looped_timed(mph_batch* b, int nsteps, float* ms) {
     MPH_CK(cudaEventRecord(b->ev1, b->stream), "event");
     MPH_CK(cudaEventSynchronize(b->ev1), "event sync");
     MPH_CK(cudaEventElapsedTime(ms, b->ev0, b->ev1), "event elapsed");
-    return MPH_OK;
+    return check_flag(b);
 }
 
 int mph_batch_get_f(mph_batch* b, int domain, double* f) {

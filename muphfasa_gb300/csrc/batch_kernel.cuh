@@ -256,6 +256,12 @@ MPH_DECL_BATCH(launch_batch_f32)
 MPH_DECL_BATCH(launch_batch_f16s)
 MPH_DECL_BATCH(launch_batch_bf16s)
 #undef MPH_DECL_BATCH
+// The fixed-point step (k_f64x_batch.cu): per-domain fixed-point constants
+// dpx, bounce-back tables kbb (27 x 27 per domain) and the range flag.
+cudaError_t launch_batch_f64x(int q, bool forced, int K, bool persistent, const void* fin, void* fout,
+                              const Chunk* chunks, int nchunks, const int2* walls, int nwalls, const KParams* dp,
+                              const KParamsX* dpx, const long long* offs, const long long* kbb, int* flag,
+                              cudaStream_t s);
 
 // Per-domain residual sums of a batch (monitor.cu): out[2 d + {0, 1}].
 cudaError_t launch_batch_residual(int prec, int q, const void* f_base, const Chunk* chunks, int nchunks, int K,

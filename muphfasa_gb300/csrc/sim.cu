@@ -124,10 +124,10 @@ void build_params(const mph_desc& d, const mph_resolved_bc* tab, KParams& kp) {
 }
 
 template <int Q>
-void fixed_params(const mph_sim* s, KParamsX& px, long long* kbb) {
+void fixed_params(const mph_desc& d, const mph_resolved_bc* table, const KParams& kp, KParamsX& px, long long* kbb) {
     using L = Lat<Q>;
     std::memset(&px, 0, sizeof(px));
-    px.W = (unsigned long long)std::ldexp(0.5 * s->d.omega, 64) & ~1ull;
+    px.W = (unsigned long long)std::ldexp(0.5 * d.omega, 64) & ~1ull;
     px.wh1 = (px.W >> 1) - 1;
     // 32 / iw_max, rounded to nearest (iw_max = 1 / smallest weight is an
     // integer: 36, 72, 36, 216).
@@ -138,10 +138,10 @@ void fixed_params(const mph_sim* s, KParamsX& px, long long* kbb) {
         const unsigned __int128 num = (unsigned __int128)1 << 69;
         px.Wm = (unsigned long long)((num + den / 2) / den);
     }
-    const double pre = 3.0 * (1.0 - 0.5 * s->d.omega) / s->d.omega;
+    const double pre = 3.0 * (1.0 - 0.5 * d.omega) / d.omega;
     for (int a = 0; a < 3; ++a) {
-        px.hF[a] = std::llrint(std::ldexp(s->kp.hF[a], 56));
-        px.Fw[a] = std::llrint(std::ldexp(pre * s->kp.F[a], 56));
+        px.hF[a] = std::llrint(std::ldexp(kp.hF[a], 56));
+        px.Fw[a] = std::llrint(std::ldexp(pre * kp.F[a], 56));
         if (px.Fw[a] != 0) px.fmask |= 1 << a;
     }
     // h-space bounce-back constants: contrib(opp n) / w_n with the
@@ -149,13 +149,13 @@ void fixed_params(const mph_sim* s, KParamsX& px, long long* kbb) {
     for (int c = 0; c < 27; ++c)
         for (int n = 0; n < 27; ++n) {
             kbb[c * 27 + n] = 0;
-            const int t = s->table[c].type;
+            const int t = table[c].type;
             if (n >= Q || !(t == MPH_BC_MOVING_WALL || t == MPH_BC_NO_SLIP || t == MPH_BC_INFLOW)) continue;
             const int o = L::opp(n);
             double rho = 1, U[3] = {0., 0., 0.};
             if (t != MPH_BC_NO_SLIP) {
-                rho = s->table[c].rho;
-                for (int a = 0; a < 3; ++a) U[a] = s->table[c].U[a];
+                rho = table[c].rho;
+                for (int a = 0; a < 3; ++a) U[a] = table[c].U[a];
             }
             double cdotu;
             if (L::D == 2) cdotu = L::cx(o) * U[0] + L::cy(o) * U[1];
@@ -231,6 +231,17 @@ void build_cls(const KParams& p, int q, const unsigned char* mask, unsigned char
 }
 // KParams of one domain, shared with the batch (batch.cu).
 void build_params_public(const mph_desc& d, const mph_resolved_bc* tab, KParams& kp) { build_params(d, tab, kp); }
+// Fixed-point constants and the 27 x 27 bounce-back table of one domain
+// (MPH_PREC_F64X), shared with the batch.
+void build_fixed_public(const mph_desc& d, const mph_resolved_bc* tab, const KParams& kp, KParamsX& px,
+                        long long* kbb) {
+    switch (d.q) {
+        case 9: fixed_params<9>(d, tab, kp, px, kbb); break;
+        case 15: fixed_params<15>(d, tab, kp, px, kbb); break;
+        case 19: fixed_params<19>(d, tab, kp, px, kbb); break;
+        case 27: fixed_params<27>(d, tab, kp, px, kbb); break;
+    }
+}
 }  // namespace mph
 
 namespace {
@@ -646,12 +657,7 @@ int mph_create(const mph_desc* desc, mph_sim** out) {
     if (e == cudaSuccess) e = cudaMemcpy(s->d_kp, &s->kp, sizeof(KParams), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && d.precision == MPH_PREC_F64X) {
         long long kbb[27 * 27];
-        switch (d.q) {
-            case 9: fixed_params<9>(s, s->kpx, kbb); break;
-            case 15: fixed_params<15>(s, s->kpx, kbb); break;
-            case 19: fixed_params<19>(s, s->kpx, kbb); break;
-            case 27: fixed_params<27>(s, s->kpx, kbb); break;
-        }
+        build_fixed_public(s->d, s->table, s->kp, s->kpx, kbb);
         e = cudaMalloc(&s->d_kbb, sizeof(kbb));
         if (e == cudaSuccess) e = cudaMemcpy(s->d_kbb, kbb, sizeof(kbb), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMalloc(&s->d_flag, sizeof(int));

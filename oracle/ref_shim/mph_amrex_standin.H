@@ -28,7 +28,10 @@
 
 #define AMREX_GPU_HOST_DEVICE
 #define AMREX_GPU_DEVICE
-#define AMREX_FORCE_INLINE inline
+// As AMReX defines it for GCC/Clang: the reference's per-cell helpers
+// (lattice accessors, streamCell, equilibrium, Guo term) must inline into the
+// cell loop so their constant tables fold.
+#define AMREX_FORCE_INLINE inline __attribute__((always_inline))
 #if (AMREX_SPACEDIM == 2)
 #define AMREX_D_DECL(a, b, c) a, b
 #define AMREX_D_TERM(a, b, c) a b

@@ -18,7 +18,7 @@ def _cavity(mph, n, omega, lid, precision, lattice="D2Q9"):
     return mph.make_desc(lattice, n, omega, faces=faces, face_U=U, precision=precision)
 
 
-@pytest.mark.parametrize("precision", ["f64", "f32", "f16s"])
+@pytest.mark.parametrize("precision", ["f64", "f32", "f16s", "f64x"])
 def test_batch_domains_equal_single_handles(precision, mph):
     descs = [_cavity(mph, (17, 17), 1.2, 0.1, precision), _cavity(mph, (64, 48), 1.7, 0.05, precision),
              _cavity(mph, (100, 100), 0.9, 0.1, precision), _cavity(mph, (33, 65), 1.9, 0.08, precision)]
@@ -39,10 +39,10 @@ def test_batch_domains_equal_single_handles(precision, mph):
         rs, us = s.update_macroscopic()
         assert np.array_equal(rb, rs) and np.array_equal(ub, us)
     total, kcells, nchunks, _ = batch.info()
-    assert total == sum(batch.ncells) and kcells in (1, 2, 4) and nchunks > 0
+    assert total == sum(batch.ncells) and kcells in ((1, 2) if precision == "f64x" else (1, 2, 4)) and nchunks > 0
 
 
-@pytest.mark.parametrize("precision", ["f64", "f16s", "bf16s"])
+@pytest.mark.parametrize("precision", ["f64", "f16s", "bf16s", "f64x"])
 def test_batch_3d_forced_mixed_boundaries(precision, mph):
     faces_a = ["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic", "Periodic"]
     faces_b = ["Inflow", "PressureOutlet", "NoSlip", "MovingWall", "Periodic", "Periodic"]
@@ -65,7 +65,7 @@ def test_batch_3d_forced_mixed_boundaries(precision, mph):
         assert np.array_equal(batch.f(i), s.f())
 
 
-@pytest.mark.parametrize("precision", ["f32", "f16s", "bf16s"])
+@pytest.mark.parametrize("precision", ["f32", "f16s", "bf16s", "f64x"])
 def test_looped_launches_equal_batched(precision, mph):
     """Per-domain launches (the single-domain kernels, two cells per thread
     for the 16-bit policies on even sides) against the batched kernel; the
@@ -84,12 +84,14 @@ def test_looped_launches_equal_batched(precision, mph):
 
 
 @pytest.mark.parametrize("cand", range(6))
-@pytest.mark.parametrize("precision", ["f32", "f16s"])
+@pytest.mark.parametrize("precision", ["f32", "f16s", "f64x"])
 def test_every_launch_candidate_equals_single_handles(cand, precision, mph, monkeypatch):
     """Each autotuner candidate (K = 1, 2, 4 cells per thread; one block per
     chunk or a persistent grid) gives the single-domain bits."""
     if precision == "f16s" and cand % 3 == 0:
         pytest.skip("16-bit storage takes cells in pairs")
+    if precision == "f64x" and cand % 3 == 2:
+        pytest.skip("the fixed-point step holds at most two cells per thread")
     monkeypatch.setenv("MPH_BATCH_CANDIDATE", str(cand))
     descs = mph.cavity_batch_descs(9, seed=4, side=(16, 70), precision=precision)
     b = mph.Batch(descs)
@@ -113,7 +115,7 @@ def test_cavity_ensemble_draw(mph):
     assert sides.min() >= 64 and sides.max() <= 512
 
 
-@pytest.mark.parametrize("precision", ["f64", "f32", "f16s"])
+@pytest.mark.parametrize("precision", ["f64", "f32", "f16s", "f64x"])
 def test_odd_step_counts_between_graph_replays(precision, mph):
     """Advances of odd length leave the state in the other buffer; the step
     pairs replayed afterwards (CUDA graphs) must start from it: 1 + 15 + 2 + 3
@@ -130,3 +132,23 @@ def test_odd_step_counts_between_graph_replays(precision, mph):
     for i, s in enumerate(singles):
         s.advance(27)
         assert np.array_equal(b.f(i), s.f()), i
+
+
+def test_f64x_batch_range_flag_and_candidate_rejection(mph, monkeypatch):
+    """The fixed-point batch reports a cell leaving its range as
+    MPH_ERR_NONFINITE (a near-vacuum state set on the host), and a K = 4
+    candidate is rejected with a clear error."""
+    descs = [_cavity(mph, (16, 16), 1.2, 0.1, "f64x"), _cavity(mph, (24, 20), 1.5, 0.05, "f64x")]
+    b = mph.Batch(descs)
+    b.initialize(0)
+    b.initialize(1, rho=np.full(24 * 20, 1e-3))  # rho far below the 1/16 floor
+    with pytest.raises(mph.MphError) as ei:
+        b.advance(2)
+    assert ei.value.code == 6
+    monkeypatch.setenv("MPH_BATCH_CANDIDATE", "2")
+    c = mph.Batch(descs)
+    for i in range(2):
+        c.initialize(i)
+    with pytest.raises(mph.MphError) as ei:
+        c.advance(1)
+    assert ei.value.code == 1

@@ -45,7 +45,7 @@ def test_residual_matches_host_norm(precision, mph):
     assert np.isinf(s.residual()[0])
 
 
-@pytest.mark.parametrize("precision", ["f64", "f32", "bf16s"])
+@pytest.mark.parametrize("precision", ["f64", "f32", "bf16s", "f64x"])
 def test_batch_residual_equals_single_domains(precision, mph):
     descs = [_cavity(mph, (17, 17), 0.7, precision=precision), _cavity(mph, (64, 48), 0.9, precision=precision),
              _cavity(mph, (33, 65), 0.6, 0.05, precision=precision)]

@@ -114,7 +114,7 @@ def test_removing_obstacles_restores_plain_step(mph):
     assert np.array_equal(a.f(), b.f())
 
 
-@pytest.mark.parametrize("precision", ["f64", "f32", "f16s"])
+@pytest.mark.parametrize("precision", ["f64", "f32", "f16s", "f64x"])
 def test_batch_obstacles_equal_single_handles(precision, mph):
     descs = mph.cavity_batch_descs(6, seed=11, side=(20, 60), precision=precision)
     b = mph.Batch(descs)
