@@ -52,6 +52,11 @@ struct mph_sim {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double time = 0.0;
     bool has_state = false;
+    // Small domains: runs of graph_steps (even) steps replayed from a CUDA
+    // graph, one per buffer the state starts in; 0 = plain launches.
+    int graph_steps = 0;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    void* graph_in[2] = {nullptr, nullptr};
 };
 
 namespace {
@@ -73,7 +78,8 @@ size_t elem_size(int prec) {
         case MPH_PREC_F64X: return 8;
         case MPH_PREC_F32: return 4;
         case MPH_PREC_F16S:
-        case MPH_PREC_BF16S: return 2;
+        case MPH_PREC_BF16S:
+        case MPH_PREC_F16C: return 2;
     }
     return 0;
 }
@@ -260,6 +266,8 @@ void free_all(mph_sim* s) {
     cudaFree(s->d_red);
     cudaFree(s->d_uprev);
     cudaFree(s->d_cls);
+    for (cudaGraphExec_t g : s->graph)
+        if (g) cudaGraphExecDestroy(g);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     for (int i = 0; i < 2; ++i) {
@@ -315,6 +323,8 @@ cudaError_t launch_step_window(mph_sim* s, const KParams& kp, bool whole) {
             return launch_step_fast_f16s(q, forced, s->fa, s->fb, kp, s->d_kp, s->stream);
         case MPH_PREC_BF16S:
             return launch_step_fast_bf16s(q, forced, s->fa, s->fb, kp, s->d_kp, s->stream);
+        case MPH_PREC_F16C:
+            return launch_step_fast_f16c(q, forced, s->fa, s->fb, kp, s->d_kp, s->stream);
         case MPH_PREC_F64X:
             if (whole && s->pipe_ctas > 0)
                 return launch_step_f64x_pipe(q, forced, (const long long*)s->fa, (long long*)s->fb, kp, s->kpx,
@@ -338,7 +348,60 @@ int check_flag(mph_sim* s) {
     return MPH_OK;
 }
 
+void drop_graphs(mph_sim* s) {
+    for (int i = 0; i < 2; ++i) {
+        if (s->graph[i]) cudaGraphExecDestroy(s->graph[i]);
+        s->graph[i] = nullptr;
+        s->graph_in[i] = nullptr;
+    }
+}
+
+// graph_steps steps captured for each buffer the state can start in
+// (A -> B -> ... -> A and B -> A -> ... -> B); the captured launches carry
+// the parameters of the handle as they are now, so anything that changes
+// them (obstacles) drops the graphs.
+int ensure_graphs(mph_sim* s) {
+    if (s->graph[0] && s->graph[1]) return MPH_OK;
+    drop_graphs(s);
+    void* const fa0 = s->fa;
+    void* const fb0 = s->fb;
+    for (int i = 0; i < 2; ++i) {
+        s->fa = i == 0 ? fa0 : fb0;
+        s->fb = i == 0 ? fb0 : fa0;
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            for (int t = 0; t < s->graph_steps && e == cudaSuccess; ++t) {
+                e = launch_one_step(s);
+                std::swap(s->fa, s->fb);
+            }
+            const cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
+            if (e == cudaSuccess) e = e2;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&s->graph[i], g, 0);
+        if (g) cudaGraphDestroy(g);
+        s->graph_in[i] = i == 0 ? fa0 : fb0;
+        s->fa = fa0;
+        s->fb = fb0;
+        if (e != cudaSuccess) {
+            drop_graphs(s);
+            return cuda_fail(e, "step graph capture");
+        }
+    }
+    return MPH_OK;
+}
+
 int advance_async(mph_sim* s, int nsteps) {
+    if (s->graph_steps > 0 && nsteps >= s->graph_steps) {
+        int rc = ensure_graphs(s);
+        if (rc) return rc;
+        // an even run leaves the state in the buffer it started from
+        const cudaGraphExec_t g = s->fa == s->graph_in[0] ? s->graph[0] : s->graph[1];
+        for (; nsteps >= s->graph_steps; nsteps -= s->graph_steps) {
+            MPH_CK(cudaGraphLaunch(g, s->stream), "step graph launch");
+            s->time += s->graph_steps;  // SimulationSetup.cpp:138, per step
+        }
+    }
     for (int t = 0; t < nsteps; ++t) {
         cudaError_t e = launch_one_step(s);
         if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
@@ -674,6 +737,15 @@ int mph_create(const mph_desc* desc, mph_sim** out) {
             }
         }
     }
+    // Domains of up to 2^22 cells (a step of at most a few tens of
+    // microseconds, where the launch cost matters) advance in runs of 32
+    // steps replayed from CUDA graphs; MPH_GRAPH_STEPS sets the run length
+    // (even; 0 = plain launches).
+    s->graph_steps = ncell <= (1LL << 22) ? 32 : 0;
+    if (const char* env = std::getenv("MPH_GRAPH_STEPS")) {
+        const int g = std::atoi(env);
+        s->graph_steps = (g > 0 && g % 2 == 0) ? g : 0;
+    }
     s->red_blocks = 152 * 4;
     if (e == cudaSuccess) e = cudaMalloc(&s->d_part, sizeof(double) * 4 * s->red_blocks);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_red, sizeof(double) * 4);
@@ -804,6 +876,7 @@ int mph_set_obstacles(mph_sim* s, const unsigned char* mask) {
         s->kp.cls = s->d_cls;
     }
     MPH_CK(cudaMemcpy(s->d_kp, &s->kp, sizeof(KParams), cudaMemcpyHostToDevice), "upload parameters");
+    drop_graphs(s);  // the captured launches carry the old parameters
     return MPH_OK;
 }
 

@@ -68,6 +68,33 @@ def test_channel_d3q19_64cubed_2000_steps_f64x(mph, oracle_mod):
     assert err < 1e-12
 
 
+def test_channel_d3q19_512cubed_f64x_vs_exact_f64_2000_steps(mph):
+    """The benchmark's headline workload at full size: the fixed-point path
+    against the bit-exact FP64 kernel (the reference's arithmetic, equal to
+    the oracle bit for bit) after 2000 steps, 1e-12 relative in f.  Both
+    handles together hold 81.6 GB of populations."""
+    n, steps = (512, 512, 512), 2000
+    F = (1e-6, 0.0, 0.0)
+    rho, u = channel_init(n, np.random.default_rng(20261203))
+    exact = mph.Simulation(mph.make_desc("D3Q19", n, 1.0 / 0.6, faces=CH_FACES, force=F, precision="f64"))
+    fixed = mph.Simulation(mph.make_desc("D3Q19", n, 1.0 / 0.6, faces=CH_FACES, force=F, precision="f64x"))
+    exact.initialize(rho, u)
+    fixed.initialize(rho, u)
+    del rho, u
+    exact.advance(steps)
+    fixed.advance(steps)
+    fe = exact.f()
+    exact.close()
+    fx = fixed.f()
+    fixed.close()
+    err, chunk = 0.0, 1 << 27
+    for i in range(0, fe.size, chunk):
+        a, b = fe[i:i + chunk], fx[i:i + chunk]
+        err = max(err, float(np.max(np.abs(b - a) / np.abs(a))))
+    print(f"f64x vs f64 512^3 channel {steps} steps: max rel err {err:.3e}")
+    assert err < 1e-12
+
+
 def test_tgv2d_256_5000_steps_f64x(mph, oracle_mod):
     N, steps, tau, u0 = 256, 5000, 0.8, 0.05
     o = oracle_mod.OracleSim(oracle_mod.Config("D2Q9", (N, N), omega=1.0 / tau), "port")
@@ -180,22 +207,3 @@ def test_closed_box_mass_conservation(mph):
     m0 = s.reduce()[0]
     s.advance(500)
     assert abs(s.reduce()[0] - m0) / m0 < 1e-12
-
-
-def test_lid_cavity_re100_centerline(mph):
-    """Lid-driven cavity at Re = 100 (tests/regression/lid2d): after the flow
-    settles the centre-line velocity minimum lies near the published value
-    -0.2140 U_lid (within 2 %)."""
-    N, U, Re = 64, 0.1, 100.0
-    nu = U * N / Re
-    tau = 3 * nu + 0.5
-    faces = ["NoSlip", "NoSlip", "NoSlip", "MovingWall", "Periodic", "Periodic"]
-    Uw = [[0.0] * 3 for _ in range(6)]
-    Uw[3] = [U, 0.0, 0.0]
-    s = mph.Simulation(mph.make_desc("D2Q9", (N, N), 1.0 / tau, faces=faces, face_U=Uw))
-    s.initialize(np.ones(N * N), np.zeros(2 * N * N))
-    s.advance(20000)
-    _, u = s.update_macroscopic()
-    ux = u[: N * N].reshape(N, N)
-    col = 0.5 * (ux[:, N // 2 - 1] + ux[:, N // 2])
-    assert abs(col.min() / U - (-0.2140417)) < 0.02 * 0.2140417
