@@ -39,9 +39,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 LATTICE_Q = {"D2Q9": 9, "D3Q15": 15, "D3Q19": 19, "D3Q27": 27}
-ELEM = {"f64": 8, "f64_fast": 8, "f32": 4, "f16s": 2, "bf16s": 2, "f64x": 8}
+ELEM = {"f64": 8, "f64_fast": 8, "f32": 4, "f16s": 2, "bf16s": 2, "f64x": 8, "f16c": 2}
 DTYPE = {"f64": "f64", "f64_fast": "f64", "f32": "f32", "f16s": "f16 storage / f32 arithmetic",
-         "bf16s": "bf16 storage / f32 arithmetic",
+         "bf16s": "bf16 storage / f32 arithmetic", "f16c": "custom 1-4-11 16-bit storage / f32 arithmetic",
          "f64x": "int64 fixed point (f/w in units of 2^-56), FP64-accurate"}
 METRIC = "MLUPS"
 
@@ -185,16 +185,17 @@ def tgv3d_fields(n, u0):
 
 
 def run_tgv3d(args):
-    """Precision study: D3Q27 TGV at n^3, tau 0.52, u0 0.05; the shifted FP16 and
-    BF16 storage against the FP64-accurate reference path, velocity L2 and
-    kinetic-energy errors and FP64 mass / momentum sums every `every` steps."""
+    """Precision study: D3Q27 TGV at n^3, tau 0.52, u0 0.05; the shifted FP16,
+    BF16 and custom 1-4-11 (f16c) storage against the FP64-accurate reference
+    path, velocity L2 and kinetic-energy errors and FP64 mass / momentum sums
+    every `every` steps."""
     import muphfasa_gb300 as m
     m.set_device(0)
     n, u0, tau = args.n, 0.05, 0.52
     every, total = args.every, args.tgv_steps
     rho, u = tgv3d_fields(n, u0)
     N = n ** 3
-    names = [args.tgv_ref, "f16s", "bf16s"]
+    names = [args.tgv_ref, "f16s", "bf16s", "f16c"]
     sims = {}
     for p in names:
         s = m.Simulation(m.make_desc("D3Q27", (n, n, n), 1.0 / tau, precision=p))
@@ -226,12 +227,12 @@ def run_tgv3d(args):
         table.append(row)
         print(json.dumps({"progress": row}), file=sys.stderr, flush=True)
     mlups = {p: N * total / (ms[p] / 1e3) / 1e6 for p in names}
-    bytes_cell = {"f64x": 432, "f64": 432, "f64_fast": 432, "f32": 216, "f16s": 108, "bf16s": 108}
+    bytes_cell = {"f64x": 432, "f64": 432, "f64_fast": 432, "f32": 216, "f16s": 108, "bf16s": 108, "f16c": 108}
     peak, kind = peaks()
     last = table[-1]
     line = {"metric": "velocity L2 error vs FP64-accurate reference (and MLUPS)",
             "value": last["f16s"]["u_l2_rel"], "unit": "relative", "n_gpus": 1, "steps": total, "warmup": 0,
-            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f16/bf16 storage, f32 collide",
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f16 / bf16 / custom 1-4-11 storage, f32 collide",
             "data": "synthetic",
             "config": {"workload": f"tgv3d_d3q27_{n}^3", "lattice": "D3Q27", "grid": [n] * 3, "tau": tau, "u0": u0,
                        "reference_precision": names[0], "every": every,
@@ -246,12 +247,113 @@ def run_tgv3d(args):
     return 0
 
 
+def run_ceiling(args):
+    """The step's memory pattern without its arithmetic (mph_pull_copy_timed):
+    pull-stencil copies of the D3Q19 / D3Q27 populations on an n^3 periodic
+    grid for 8-, 4- and 2-byte elements; for 2 bytes the 16-bit step kernel's
+    pattern (16-bit loads for x-shifted populations) and the word-and-shuffle
+    pattern.  GB/s = 2 Q elem bytes x cells / time, against the measured copy
+    peak."""
+    import muphfasa_gb300 as m
+    m.set_device(0)
+    n = args.n
+    peak, kind = peaks()
+    rows = []
+    for q in (19, 27):
+        for elem, mode, name in ((8, 0, "8-byte, one cell per thread"), (4, 0, "4-byte, one cell per thread"),
+                                 (2, 0, "2-byte, one cell per thread"),
+                                 (2, 1, "2-byte pairs, 16-bit loads for x-shifted populations"),
+                                 (2, 2, "2-byte pairs, aligned 32-bit words + warp shuffles")):
+            best = min(m.pull_copy_ms(elem, mode, q, (n, n, n), reps=args.steps) for _ in range(3))
+            gbs = 2 * q * elem * n ** 3 / (best / 1e3) / 1e9
+            rows.append({"q": q, "elem_bytes": elem, "mode": mode, "pattern": name, "ms": round(best, 4),
+                         "gbs": round(gbs, 1), "frac": round(gbs / peak, 4),
+                         "glups": round(n ** 3 / (best / 1e3) / 1e9, 2)})
+            print(json.dumps({"progress": rows[-1]}), file=sys.stderr, flush=True)
+    line = {"metric": "pull-stencil copy bandwidth (the step's memory pattern, no arithmetic)", "value": None,
+            "unit": "GB/s", "n_gpus": 1, "steps": args.steps, "higher_is_better": True, "data": "synthetic",
+            "config": {"workload": f"pull_copy_{n}^3", "best_of": 3, "peak": peak, "peak_kind": kind},
+            "rows": rows}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def tgv2d_fields(N, u0):
+    """2-D Taylor-Green vortex of the benchmark's CPU-runnable configuration:
+    u = u0 (sin kx cos ky, -cos kx sin ky), k = 2 pi / N, cell centres
+    x = i + 1/2, rho = 1 - 3 u0^2 / 4 (cos 2kx + cos 2ky)."""
+    k = 2.0 * math.pi / N
+    x = np.arange(N) + 0.5
+    X, Y = np.meshgrid(x, x, indexing="xy")
+    ux = u0 * np.sin(k * X) * np.cos(k * Y)
+    uy = -u0 * np.cos(k * X) * np.sin(k * Y)
+    rho = 1.0 - 0.75 * u0 * u0 * (np.cos(2 * k * X) + np.cos(2 * k * Y))
+    return rho.ravel(), np.concatenate([ux.ravel(), uy.ravel()])
+
+
+def run_tgv2d(args):
+    """The CPU-runnable configuration: 2-D Taylor-Green vortex, D2Q9, periodic
+    256^2, tau 0.8, u0 0.05, 5000 steps.  MLUPS per precision with the
+    32-step CUDA-graph runs of small domains and with plain launches (one per
+    step), the amplitude decay against exp(-2 nu k^2 t), and the reference's
+    CPU step on the host cores on the same case."""
+    import muphfasa_gb300 as m
+    m.set_device(0)
+    N, tau, u0, steps = args.n, 0.8, 0.05, args.tgv_steps
+    nu = (tau - 0.5) / 3.0
+    k = 2.0 * math.pi / N
+    rho, u = tgv2d_fields(N, u0)
+    rows = {}
+    for p in ("f64", "f64x", "f32"):
+        row = {}
+        for mode, env in (("graph", None), ("plain", "0")):
+            if env is None:
+                os.environ.pop("MPH_GRAPH_STEPS", None)
+            else:
+                os.environ["MPH_GRAPH_STEPS"] = env
+            s = m.Simulation(m.make_desc("D2Q9", (N, N), 1.0 / tau, precision=p))
+            s.initialize(rho.copy(), u.copy())
+            s.advance(args.warmup)
+            with ClockSampler(0) as clk:
+                ms = s.advance_timed(steps)
+            _, us = s.update_macroscopic()
+            amp = float(np.abs(us).max() / u0)
+            row[mode] = {"mlups": round(N * N * steps / (ms / 1e3) / 1e6, 1), "ms_per_step": round(ms / steps, 5),
+                         "decay_rel_err": abs(amp / math.exp(-2 * nu * k * k * (steps + args.warmup)) - 1.0),
+                         "clocks": clk.summary()}
+            s.close()
+        row["graph_gain"] = round(row["graph"]["mlups"] / row["plain"]["mlups"], 3)
+        rows[p] = row
+    os.environ.pop("MPH_GRAPH_STEPS", None)
+    from oracle import oracle as O
+    kind = cpu_kind()
+    o = O.OracleSim(O.Config("D2Q9", (N, N), omega=1.0 / tau), "ref" if kind == "reference" else "port")
+    o.init_fields(rho, u)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    o.step(min(steps, 1000), threads)
+    dt = time.perf_counter() - t0
+    cpu = {"value": round(N * N * min(steps, 1000) / dt / 1e6, 3), "unit": "MLUPS", "cores": threads, "kind": kind,
+           "sample": f"{N}^2, {min(steps, 1000)} steps, FP64, {threads} threads ({dt:.2f} s)"}
+    line = {"metric": METRIC, "value": rows["f64"]["graph"]["mlups"], "unit": "MLUPS", "n_gpus": 1, "steps": steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": f"tgv2d_d2q9_{N}^2", "tau": tau, "u0": u0,
+                                            "l2": "fits in L2 (the configuration's own size)"},
+            "precisions": rows, "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_warmstart(args):
-    """Learned warm start: the plain FP32 batch solver generates steady fields
-    of seeded cavity / channel cases, the U-Net is trained on them with the
-    library's BF16 tensor-core kernels, and held-out cases are solved to the
-    residual 1e-8 (FP64 storage: FP32 stalls near 1e-6) from rest and from
-    the surrogate's prediction (feq + f_neq)."""
+    """Learned warm start: the plain solver (FP64-accurate fixed point, batch
+    of all cases, converged cases leaving the batch) generates steady fields
+    of seeded cavity / channel cases to the residual 1e-8; the U-Net is
+    trained on them with the library's BF16 tensor-core kernels; held-out
+    cases are solved to 1e-8 from rest and from the surrogate's prediction
+    (feq + f_neq), in a batch and on single handles; and the steps to 1e-8
+    are measured against the relative error of an initial field (converged
+    held-out fields plus smooth noise), which says what surrogate error a
+    given gain needs."""
     import muphfasa_gb300 as m
     from muphfasa_gb300 import warmstart as ws
     m.set_device(0)
@@ -259,39 +361,50 @@ def run_warmstart(args):
     log = lambda *a: print(json.dumps({"progress": a}), file=sys.stderr, flush=True)
     train_cases = ws.draw_cases(args.ws_train, seed=101, sizes=(n,))
     test_cases = ws.draw_cases(args.ws_test, seed=202, sizes=(n,))
-    t0 = time.perf_counter()
-    _, fields, gen_secs, last = ws.solve(train_cases, max_steps=args.ws_gen_steps, tol=0.0, precision="f32",
-                                         check_every=5000)
-    keep = [i for i, r in enumerate(last) if np.isfinite(r) and r < args.ws_keep]
+    st, fields, gen_secs, last = ws.solve(train_cases, max_steps=args.ws_gen_steps, tol=1e-8, check_every=2000,
+                                          log=lambda *a: log("gen", *a) if a[0] % 20000 == 0 else None)
+    keep = [i for i in range(len(train_cases)) if st[i] > 0]
     X, Y, M = ws.dataset([train_cases[i] for i in keep], [fields[i] for i in keep])
     log("generated", len(keep), X.shape[0], len(train_cases), round(gen_secs, 1))
     t1 = time.perf_counter()
     X, Y, M = ws.mirror_channels(X, Y, M)
     ntrain = X.shape[0]
-    net, hist = ws.train(X, Y, M, epochs=args.ws_epochs, batch=8, lr=args.ws_lr, log=lambda e, l: log("epoch", e, l))
+    net, hist = ws.train(X, Y, M, epochs=args.ws_epochs, batch=8, lr=args.ws_lr,
+                         log=lambda e, l: log("epoch", e, l) if e % 10 == 0 else None)
     train_secs = time.perf_counter() - t1
-    # error on (up to) 64 training fields, the same metric as on the held-out cases
-    sub_idx = keep[:64]
+    sub_idx = keep[:64]  # error on (up to) 64 training fields, the held-out metric
     p_tr, _ = ws.predict(net, [train_cases[i] for i in sub_idx])
     train_err = [ws.field_error(train_cases[i], p, fields[i]) for i, p in zip(sub_idx, p_tr)]
     del X, Y, M
     preds, pred_secs = ws.predict(net, test_cases)
-    sp, ref, secs_plain, rp = ws.solve(test_cases, None, max_steps=args.ws_max_steps, precision="f64_fast")
+    sp, ref, secs_plain, rp = ws.solve(test_cases, None, max_steps=args.ws_max_steps)
     log("plain", int(np.sum(sp > 0)), round(secs_plain, 1))
-    sw, _, secs_warm, rw = ws.solve(test_cases, preds, max_steps=args.ws_max_steps, precision="f64_fast")
+    sw, _, secs_warm, rw = ws.solve(test_cases, preds, max_steps=args.ws_max_steps)
     log("warm", int(np.sum(sw > 0)), round(secs_warm, 1))
     both = (sp > 0) & (sw > 0)
-    errs = [ws.field_error(c, p, r) for c, p, r, ok in zip(test_cases, preds, ref, sp > 0) if ok]
     err_all = np.array([ws.field_error(c, p, r) if ok else np.nan for c, p, r, ok in zip(test_cases, preds, ref, sp > 0)])
+    errs = err_all[~np.isnan(err_all)]
     by_kind = {k: float(np.nanmedian(err_all[[c["kind"] == k for c in test_cases]])) for k in ("cavity", "channel")}
     good = both & (err_all < 0.2)
-    # single-case wall time (one handle per case, FP64): rest vs predict + warm start
+    # steps to 1e-8 against the initial field's relative error (converged held-out fields + smooth noise)
+    conv = [i for i in range(len(test_cases)) if sp[i] > 0][: args.ws_curve]
+    amps = [0.3, 0.1, 3e-2, 1e-2, 1e-3, 1e-4, 1e-5, 1e-6, 0.0]
+    curve, curve_secs = ws.perturbation_curve([test_cases[i] for i in conv], [ref[i] for i in conv], amps,
+                                              max_steps=args.ws_max_steps)
+    rest = np.array(curve["rest"], float)
+    curve_rows = []
+    for e in amps:
+        se = np.array(curve[e], float)
+        ok = (se > 0) & (rest > 0)
+        curve_rows.append({"rel_error": e, "steps_median": float(np.median(se[se > 0])) if np.any(se > 0) else None,
+                           "gain_median": float(np.median(rest[ok] / se[ok])) if ok.any() else None})
+    # single-case wall time (one FP64-accurate handle per case): rest vs predict + warm start
     single = []
     for c in [c for c, ok in zip(test_cases, both) if ok][: args.ws_single]:
         row = {}
         for mode in ("plain", "warm"):
             tt = time.perf_counter()
-            s = m.Simulation(ws.case_desc(c, "f64_fast"))
+            s = m.Simulation(ws.case_desc(c, "f64x"))
             s.set_obstacles(ws.case_mask(c))
             if mode == "plain":
                 s.initialize()
@@ -313,27 +426,31 @@ def run_warmstart(args):
     line = {"metric": "steps and wall time to residual 1e-8, warm start vs start from rest",
             "value": round(float(np.median(ratio)), 3) if ratio.size else None, "unit": "x (median over cases)",
             "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "surrogate bf16 / f32 accumulate; solver f32 (data), f64 (judge)", "data": "synthetic",
-            "config": {"workload": f"warmstart_d2q9_{n}^2", "train_cases": len(train_cases), "kept": len(keep),
-                       "trained_on": int(ntrain),
-                       "test_cases": len(test_cases), "epochs": args.ws_epochs, "gen_steps": args.ws_gen_steps,
-                       "params": net.n_params(), "Re": list(ws.RE), "U": list(ws.U)},
+            "dtype": "surrogate bf16 / f32 accumulate; solver int64 fixed point (FP64-accurate)", "data": "synthetic",
+            "config": {"workload": f"warmstart_d2q9_{n}^2", "train_cases": len(train_cases),
+                       "kept_at_1e-8": len(keep), "trained_on": int(ntrain), "test_cases": len(test_cases),
+                       "epochs": args.ws_epochs, "gen_max_steps": args.ws_gen_steps, "params": net.n_params(),
+                       "Re": list(ws.RE), "U": list(ws.U)},
             "steps_plain_median": float(np.median(sp[sp > 0])) if np.any(sp > 0) else None,
             "steps_warm_median": float(np.median(sw[sw > 0])) if np.any(sw > 0) else None,
             "steps_ratio_total": float(sp[both].sum() / sw[both].sum()) if np.any(both) else None,
             "converged": {"plain": int(np.sum(sp > 0)), "warm": int(np.sum(sw > 0)), "both": int(np.sum(both)),
                           "diverged_plain": int(np.sum(sp == -2))},
-            "surrogate_u_error_train": float(np.median(train_err)),
-            "surrogate_u_error": {"median": float(np.median(errs)) if errs else None,
-                                  "p90": float(np.percentile(errs, 90)) if errs else None, "by_kind": by_kind},
+            "surrogate_u_error_train": float(np.median(train_err)) if train_err else None,
+            "surrogate_u_error": {"median": float(np.median(errs)) if errs.size else None,
+                                  "p10": float(np.percentile(errs, 10)) if errs.size else None,
+                                  "p90": float(np.percentile(errs, 90)) if errs.size else None, "by_kind": by_kind},
             "steps_ratio_when_error_below_0.2": {"cases": int(good.sum()),
                                                  "median": float(np.median(sp[good] / sw[good])) if good.any() else None},
+            "error_vs_steps": {"cases": len(conv), "rows": curve_rows,
+                               "rest_steps_median": float(np.median(rest[rest > 0])) if np.any(rest > 0) else None},
             "seconds": {"generate": round(gen_secs, 1), "train": round(train_secs, 1),
                         "predict_all": round(pred_secs, 3), "batch_plain": round(secs_plain, 1),
-                        "batch_warm": round(secs_warm, 1)},
+                        "batch_warm": round(secs_warm, 1), "curve": round(curve_secs, 1)},
+            "batch_wall_ratio": round(secs_plain / secs_warm, 3) if secs_warm > 0 else None,
             "single_case_wall": {"cases": single,
                                  "median_ratio": float(np.median(wall_single)) if wall_single else None},
-            "train_loss": [round(h, 6) for h in hist]}
+            "train_loss": [round(h, 6) for h in hist[:: max(1, len(hist) // 20)]] + [round(hist[-1], 6)]}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -449,7 +566,7 @@ def main():
     ap.add_argument("--secondary-steps", type=int, default=40,
                     help="steps of the 512-cavity batch record added to the channel line (0: skip)")
     ap.add_argument("--domains", type=int, default=512, help="domains of the batch512 workload")
-    ap.add_argument("--workload", default="channel", choices=["channel", "batch512", "tgv3d", "warmstart"],
+    ap.add_argument("--workload", default="channel", choices=["channel", "batch512", "tgv3d", "warmstart", "tgv2d", "ceiling"],
                     help="channel: the D3Q19 channel (headline); batch512: 512 uneven D2Q9 cavities; "
                          "tgv3d: the D3Q27 precision study (use --n 384)")
     ap.add_argument("--tgv-steps", type=int, default=10000, help="tgv3d: total steps")
@@ -459,9 +576,10 @@ def main():
     ap.add_argument("--ws-test", type=int, default=200, help="warmstart: held-out cases")
     ap.add_argument("--ws-epochs", type=int, default=200)
     ap.add_argument("--ws-lr", type=float, default=2e-3)
-    ap.add_argument("--ws-gen-steps", type=int, default=300000, help="warmstart: FP32 steps per training field")
-    ap.add_argument("--ws-keep", type=float, default=5e-5, help="warmstart: keep fields with FP32 residual below")
+    ap.add_argument("--ws-gen-steps", type=int, default=400000,
+                    help="warmstart: step limit of the data generation (fields kept when converged to 1e-8)")
     ap.add_argument("--ws-max-steps", type=int, default=400000)
+    ap.add_argument("--ws-curve", type=int, default=24, help="warmstart: held-out cases of the error-vs-steps curve")
     ap.add_argument("--ws-single", type=int, default=6, help="warmstart: cases timed on single handles")
     ap.add_argument("--tgv-ref", default="f64x", choices=["f64x", "f64", "f64_fast"],
                     help="tgv3d: reference precision (FP64 or the FP64-accurate fixed point)")
@@ -470,6 +588,10 @@ def main():
         return run_reference(args)
     if args.workload == "tgv3d":
         return run_tgv3d(args)
+    if args.workload == "tgv2d":
+        return run_tgv2d(args)
+    if args.workload == "ceiling":
+        return run_ceiling(args)
     if args.workload == "warmstart":
         return run_warmstart(args)
     if args.workload == "batch512":

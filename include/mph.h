@@ -70,6 +70,12 @@ extern "C" {
  * whose FP64 pipes run at 1/64 of the FP32 rate.  Conversions to FP64 happen
  * only in mph_set_f / mph_get_f / moments / sums. */
 #define MPH_PREC_F64X 5
+/* f_i - w_i stored as a custom 16-bit float with one more significand bit
+ * than FP16 (sign, 4 exponent bits biased by 16, 11 stored mantissa bits:
+ * normals 2^-15 .. 1 - 2^-12, subnormal steps of 2^-26, larger magnitudes
+ * saturate), FP32 collide arithmetic; same traffic as FP16 storage, half
+ * its rounding error. */
+#define MPH_PREC_F16C 6
 
 /* ---- lattice-unit description of one domain ---------------------------- */
 typedef struct {
@@ -259,6 +265,10 @@ int mph_batch_advance_timed(mph_batch* b, int nsteps, float* ms);
 /* The same steps as one single-domain launch per domain per step. */
 int mph_batch_advance_looped_timed(mph_batch* b, int nsteps, float* ms);
 int mph_batch_get_f(mph_batch* b, int domain, double* f);
+/* Replaces one domain's populations (host valid-cell SoA FP64, converted to
+ * the batch's storage), as mph_set_f for a single handle; the next
+ * mph_batch_residual starts a new reference field for every domain. */
+int mph_batch_set_f(mph_batch* b, int domain, const double* f);
 int mph_batch_moments(mph_batch* b, int domain, double* rho, double* u);
 /* Warm start of one batch domain, as mph_init_fields_neq. */
 int mph_batch_init_fields_neq(mph_batch* b, int domain, const double* rho, const double* u);
@@ -272,6 +282,19 @@ int mph_batch_residual(mph_batch* b, double* out);
  * advance), the number of 256-thread chunks per step, and whether the chosen
  * launch is a persistent grid (1) or one block per chunk (0). */
 int mph_batch_info(const mph_batch* b, long long* total_cells, int* cells_per_thread, int* nchunks, int* persistent);
+
+/* ---- memory ceiling of the step ----------------------------------------- */
+/* No counterpart in the reference.  Times the step's memory pattern without
+ * its arithmetic on an nx x ny x nz periodic grid of q populations (q 9 with
+ * nz = 1, or 19 / 27): every cell reads its populations from x - c_n and
+ * writes them to its own slots, reps times (after two untimed passes), on
+ * two buffers it allocates and frees.  elem_bytes 8, 4 or 2; mode 0 = one
+ * cell per thread, 1 = cell pairs with 16-bit loads for x-shifted
+ * populations (the 16-bit step kernel's pattern), 2 = cell pairs with one
+ * aligned 32-bit word per population and warp shuffles for the x shift
+ * (modes 1 and 2: 2-byte elements, nx even).  *ms = mean milliseconds per
+ * pass; a pass moves 2 q elem_bytes bytes per cell. */
+int mph_pull_copy_timed(int elem_bytes, int mode, int q, int nx, int ny, int nz, int reps, float* ms);
 
 /* ---- allocation-free sums ---------------------------------------------- */
 /* No counterpart in the reference.  The FP64 mass and momentum sums of

@@ -29,7 +29,7 @@ MPH_OK = 0
 ERRORS = {1: "MPH_ERR_ARG", 2: "MPH_ERR_CONFIG", 3: "MPH_ERR_CUDA", 4: "MPH_ERR_UNSUPPORTED",
           5: "MPH_ERR_PARSE", 6: "MPH_ERR_NONFINITE", 7: "MPH_ERR_STATE"}
 BC = {"MovingWall": 0, "NoSlip": 1, "Inflow": 2, "Outflow": 3, "PressureOutlet": 4, "Periodic": 5}
-PRECISION = {"f64": 0, "f64_fast": 1, "f32": 2, "f16s": 3, "bf16s": 4, "f64x": 5}
+PRECISION = {"f64": 0, "f64_fast": 1, "f32": 2, "f16s": 3, "bf16s": 4, "f64x": 5, "f16c": 6}
 LATTICE_DQ = {"D2Q9": (2, 9), "D3Q15": (3, 15), "D3Q19": (3, 19), "D3Q27": (3, 27)}
 
 # Exported entry points (the declarations of include/mph.h).
@@ -38,9 +38,9 @@ EXPORTS = [
     "mph_inputs_get", "mph_inputs_derive", "mph_resolve_bc", "mph_create", "mph_destroy", "mph_set_f",
     "mph_get_f", "mph_init_fields", "mph_advance", "mph_update_macroscopic", "mph_reduce", "mph_time",
     "mph_launches_per_step", "mph_advance_timed", "mph_step_host", "mph_pull_collide_fused_arr",
-    "mph_periodic_fill_arr", "mph_bc_fill_arr", "mph_reduce_f64_noalloc", "mph_batch_create",
+    "mph_periodic_fill_arr", "mph_bc_fill_arr", "mph_reduce_f64_noalloc", "mph_pull_copy_timed", "mph_batch_create",
     "mph_batch_destroy", "mph_batch_init_fields", "mph_batch_advance", "mph_batch_advance_timed",
-    "mph_batch_advance_looped_timed", "mph_batch_get_f", "mph_batch_moments", "mph_batch_info",
+    "mph_batch_advance_looped_timed", "mph_batch_get_f", "mph_batch_set_f", "mph_batch_moments", "mph_batch_info",
     "mph_residual", "mph_batch_residual", "mph_lattice", "mph_set_obstacles", "mph_batch_set_obstacles",
     "mph_init_fields_neq", "mph_batch_init_fields_neq", "mph_set_time", "mph_state_bytes", "mph_get_state",
     "mph_set_state", "mph_host_alloc", "mph_host_free", "mph_nn_alloc", "mph_nn_free", "mph_nn_copy", "mph_nn_sync", "mph_nn_gemm", "mph_nn_im2col3", "mph_nn_col2im3",
@@ -132,6 +132,7 @@ def lib():
     L.mph_periodic_fill_arr.argtypes = [C.c_int, C.c_int, ip, ip, ip, C.POINTER(Array4), P]
     L.mph_bc_fill_arr.argtypes = [C.c_int, C.c_int, ip, ip, ip, C.POINTER(ResolvedBC), C.POINTER(Array4), P]
     L.mph_reduce_f64_noalloc.argtypes = [C.c_int, C.c_int, P, C.c_longlong, P, P]
+    L.mph_pull_copy_timed.argtypes = [C.c_int] * 7 + [C.POINTER(C.c_float)]
     L.mph_batch_create.argtypes = [C.c_int, C.POINTER(Desc), C.POINTER(P)]
     L.mph_batch_destroy.argtypes = [P]
     L.mph_batch_init_fields.argtypes = [P, C.c_int, dp, dp]
@@ -139,6 +140,7 @@ def lib():
     L.mph_batch_advance_timed.argtypes = [P, C.c_int, C.POINTER(C.c_float)]
     L.mph_batch_advance_looped_timed.argtypes = [P, C.c_int, C.POINTER(C.c_float)]
     L.mph_batch_get_f.argtypes = [P, C.c_int, dp]
+    L.mph_batch_set_f.argtypes = [P, C.c_int, dp]
     L.mph_batch_moments.argtypes = [P, C.c_int, dp, dp]
     L.mph_batch_info.argtypes = [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                  C.POINTER(C.c_int)]
@@ -185,6 +187,16 @@ class PinnedArray:
             self.close()
         except Exception:
             pass
+
+
+def pull_copy_ms(elem_bytes, mode, q, n, reps=20):
+    """Mean milliseconds of one pull-stencil copy pass (the step's memory
+    pattern without its arithmetic) on an n = (nx, ny[, nz]) periodic grid."""
+    nn = list(n) + [1] * (3 - len(n))
+    ms = C.c_float()
+    check(lib().mph_pull_copy_timed(int(elem_bytes), int(mode), int(q), int(nn[0]), int(nn[1]), int(nn[2]), int(reps),
+                                    C.byref(ms)))
+    return float(ms.value)
 
 
 def make_desc(lattice: str, n, omega: float, faces=None, face_rho=None, face_U=None, force=None,
@@ -429,6 +441,12 @@ class Batch:
         out = np.empty(self.descs[domain].q * self.ncells[domain])
         check(lib().mph_batch_get_f(self._h, int(domain), _dp(out)))
         return out
+
+    def set_f(self, domain, f):
+        """Replaces one domain's populations (FP64, valid-cell SoA)."""
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        assert f.size == self.descs[domain].q * self.ncells[domain]
+        check(lib().mph_batch_set_f(self._h, int(domain), _dp(f)))
 
     def moments(self, domain):
         N, dim = self.ncells[domain], self.descs[domain].dim

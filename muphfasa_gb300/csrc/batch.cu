@@ -53,6 +53,8 @@ cudaError_t launch_batch(int prec, int q, bool forced, int K, bool P, const void
         case MPH_PREC_F16S: return launch_batch_f16s(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
         case MPH_PREC_BF16S:
             return launch_batch_bf16s(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
+        case MPH_PREC_F16C:
+            return launch_batch_f16c(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -64,7 +66,8 @@ size_t elem_of(int prec) {
         case MPH_PREC_F64X: return 8;
         case MPH_PREC_F32: return 4;
         case MPH_PREC_F16S:
-        case MPH_PREC_BF16S: return 2;
+        case MPH_PREC_BF16S:
+        case MPH_PREC_F16C: return 2;
     }
     return 0;
 }
@@ -77,7 +80,7 @@ size_t elem_of(int prec) {
 constexpr int kCells[3] = {1, 2, 4};
 constexpr int kCands = 6;
 
-bool shifted(int prec) { return prec == MPH_PREC_F16S || prec == MPH_PREC_BF16S; }
+bool shifted(int prec) { return prec == MPH_PREC_F16S || prec == MPH_PREC_BF16S || prec == MPH_PREC_F16C; }
 bool candidate_ok(int prec, int cand) {
     if (shifted(prec)) return cand % 3 != 0;
     if (prec == MPH_PREC_F64X) return cand % 3 != 2;
@@ -573,6 +576,7 @@ int mph_batch_advance_looped_timed(mph_batch* b, int nsteps, float* ms) {
                 case MPH_PREC_F32: e = launch_step_fast_f32(b->q, b->forced, (const float*)in, (float*)outp, kp, pg, b->stream); break;
                 case MPH_PREC_F16S: e = launch_step_fast_f16s(b->q, b->forced, in, outp, kp, pg, b->stream); break;
                 case MPH_PREC_BF16S: e = launch_step_fast_bf16s(b->q, b->forced, in, outp, kp, pg, b->stream); break;
+                case MPH_PREC_F16C: e = launch_step_fast_f16c(b->q, b->forced, in, outp, kp, pg, b->stream); break;
                 case MPH_PREC_F64X:
                     e = launch_step_f64x(b->q, b->forced, (const long long*)in, (long long*)outp, kp, b->px_h[d], pg,
                                          b->d_kbb + (size_t)d * 27 * 27, b->d_flag, b->stream);
@@ -606,6 +610,27 @@ int mph_batch_get_f(mph_batch* b, int domain, double* f) {
         }
     }
     MPH_CK(cudaStreamSynchronize(b->stream), "batch get f");
+    return MPH_OK;
+}
+
+int mph_batch_set_f(mph_batch* b, int domain, const double* f) {
+    if (!b || !f || domain < 0 || domain >= b->ndom) return fail(MPH_ERR_ARG, "mph_batch_set_f: bad argument");
+    const KParams& kp = b->params_h[domain];
+    const long long N = kp.ncell;
+    const size_t es = elem_of(b->prec);
+    void* base = static_cast<char*>(b->fa) + es * b->offs_h[domain];
+    if (b->prec == MPH_PREC_F64 || b->prec == MPH_PREC_F64_FAST) {
+        MPH_CK(cudaMemcpyAsync(base, f, sizeof(double) * b->q * N, cudaMemcpyHostToDevice, b->stream), "batch set f");
+    } else {
+        if (!b->d_stage) MPH_CK(cudaMalloc(&b->d_stage, sizeof(double) * b->max_cells), "batch stage");
+        for (int q = 0; q < b->q; ++q) {
+            MPH_CK(cudaMemcpyAsync(b->d_stage, f + (size_t)q * N, sizeof(double) * N, cudaMemcpyHostToDevice,
+                                   b->stream), "batch set f");
+            MPH_CK(launch_convert(b->prec, b->q, true, base, b->d_stage, q, N, b->stream), "batch convert");
+        }
+    }
+    MPH_CK(cudaStreamSynchronize(b->stream), "batch set f");
+    b->has_uprev = false;
     return MPH_OK;
 }
 

@@ -255,6 +255,7 @@ MPH_DECL_BATCH(launch_batch_fast_f64)
 MPH_DECL_BATCH(launch_batch_f32)
 MPH_DECL_BATCH(launch_batch_f16s)
 MPH_DECL_BATCH(launch_batch_bf16s)
+MPH_DECL_BATCH(launch_batch_f16c)
 #undef MPH_DECL_BATCH
 // The fixed-point step (k_f64x_batch.cu): per-domain fixed-point constants
 // dpx, bounce-back tables kbb (27 x 27 per domain) and the range flag.

@@ -159,9 +159,11 @@ struct StBF16S {
     static __device__ __forceinline__ float ldr1(const T* __restrict__ f, unsigned e) {
         return __uint_as_float((unsigned)__ldg(reinterpret_cast<const unsigned short*>(f) + e) << 16);
     }
-    static __device__ __forceinline__ float2 ldr2(const T* __restrict__ f, unsigned e) {
-        const unsigned w = __ldg(reinterpret_cast<const unsigned*>(f + e));
+    static __device__ __forceinline__ float2 dec2(unsigned w) {
         return make_float2(__uint_as_float(w << 16), __uint_as_float(w & 0xffff0000u));
+    }
+    static __device__ __forceinline__ float2 ldr2(const T* __restrict__ f, unsigned e) {
+        return dec2(__ldg(reinterpret_cast<const unsigned*>(f + e)));
     }
     static __device__ __forceinline__ void str1(T* __restrict__ f, unsigned e, float v) { f[e] = __float2bfloat16_rn(v); }
     static __device__ __forceinline__ void str2(T* __restrict__ f, unsigned e, float2 v) {
@@ -181,6 +183,69 @@ struct StBF16S {
     }
     template <int Q> static __device__ __forceinline__ R rt(int n, R v) {
         return __bfloat162float(__float2bfloat16_rn(v - (float)Lat<Q>::w(n))) + (float)Lat<Q>::w(n);
+    }
+};
+
+// Shifted custom 16-bit float (MPH_PREC_F16C): the deviation f_n - w_n in a
+// 1-4-11 format (sign, 4 exponent bits with bias 16, 11 stored mantissa
+// bits), after the custom FP16 formats for lattice-Boltzmann populations of
+// Lehmann et al., Phys. Rev. E 106, 015308 (2022): the deviations stay far
+// below 1, so IEEE FP16's upper exponent range is traded for a 12-bit
+// significand (half the rounding error of FP16).  Normals span 2^-15 up to
+// 1 - 2^-12, subnormals reach down in steps of 2^-26; magnitudes from
+// 1 - 2^-13 up saturate at the largest value.  Conversions are bit
+// arithmetic around one power-of-two FP32
+// multiply (no denormal flushing in these translation units):
+//   decode: the 15 magnitude bits placed at FP32 bit 12 read as an FP32
+//           number 2^(e-127)(1 + m/2^11) (or an FP32 subnormal for e = 0);
+//           times 2^(127-16) rebias it, subnormals included;
+//   encode: times 2^(16-127), then round the FP32 bits to nearest even at
+//           bit 12 (carries run into the exponent as they should).
+namespace f16c {
+__device__ __forceinline__ float decode(unsigned h) {
+    const unsigned u = ((h & 0x8000u) << 16) | ((h & 0x7FFFu) << 12);
+    return __fmul_rn(__uint_as_float(u), 0x1p111f);
+}
+__device__ __forceinline__ unsigned encode(float x) {
+    const unsigned u = __float_as_uint(__fmul_rn(x, 0x1p-111f));
+    const unsigned a = u & 0x7FFFFFFFu;
+    unsigned r = (a + 0x7FFu + ((a >> 12) & 1u)) >> 12;
+    r = r > 0x7FFFu ? 0x7FFFu : r;
+    return ((u >> 16) & 0x8000u) | r;
+}
+}  // namespace f16c
+
+struct StF16C {
+    using T = unsigned short;
+    using R = float;
+    static constexpr bool kShift = true;
+    static __device__ __forceinline__ float ldr1(const T* __restrict__ f, unsigned e) { return f16c::decode(__ldg(f + e)); }
+    static __device__ __forceinline__ float2 dec2(unsigned w) {
+        return make_float2(f16c::decode(w & 0xFFFFu), f16c::decode(w >> 16));
+    }
+    static __device__ __forceinline__ float2 ldr2(const T* __restrict__ f, unsigned e) {
+        return dec2(__ldg(reinterpret_cast<const unsigned*>(f + e)));
+    }
+    static __device__ __forceinline__ void str1(T* __restrict__ f, unsigned e, float v) {
+        f[e] = (unsigned short)f16c::encode(v);
+    }
+    static __device__ __forceinline__ void str2(T* __restrict__ f, unsigned e, float2 v) {
+        *reinterpret_cast<unsigned*>(f + e) = f16c::encode(v.x) | (f16c::encode(v.y) << 16);
+    }
+    template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int n, unsigned e) {
+        return ldr1(f, e) + (float)Lat<Q>::w(n);
+    }
+    template <int Q> static __device__ __forceinline__ void ste(T* __restrict__ f, int n, unsigned e, R v) {
+        str1(f, e, v - (float)Lat<Q>::w(n));
+    }
+    template <int Q> static __device__ __forceinline__ R ld(const T* __restrict__ f, int n, long long i, long long N) {
+        return ldr1(f, (unsigned)(n * N + i)) + (float)Lat<Q>::w(n);
+    }
+    template <int Q> static __device__ __forceinline__ void st(T* __restrict__ f, int n, long long i, long long N, R v) {
+        f[n * N + i] = (unsigned short)f16c::encode(v - (float)Lat<Q>::w(n));
+    }
+    template <int Q> static __device__ __forceinline__ R rt(int n, R v) {
+        return f16c::decode(f16c::encode(v - (float)Lat<Q>::w(n))) + (float)Lat<Q>::w(n);
     }
 };
 
@@ -852,8 +917,11 @@ __global__ void __launch_bounds__(256) k_init(typename St::T* __restrict__ fout,
 }
 
 // Warm start (no counterpart in the reference): f = feq(rho, u) + f_neq with
-// the first-order Chapman-Enskog non-equilibrium part of BGK,
-//   f_neq_n = -(tau w_n rho / cs2) (c_n c_n - cs2 I) : grad u,  cs2 = 1/3,
+// the first-order Chapman-Enskog non-equilibrium part of BGK.  The stored
+// populations are post-collision (the next step's pull streams them), and a
+// BGK collision scales the pre-collision part -(tau w rho / cs2) Q : grad u
+// by (1 - omega), so
+//   f_neq_n = -((tau - 1) w_n rho / cs2) (c_n c_n - cs2 I) : grad u,  cs2 = 1/3,
 // grad u by central differences, one-sided where a neighbour lies beyond a
 // non-periodic face or in an obstacle, zero with no fluid neighbour along an
 // axis.  Obstacle cells get the rest state.  Unforced domains.
@@ -906,7 +974,7 @@ __global__ void __launch_bounds__(256) k_init_neq(typename St::T* __restrict__ f
         double cc = 0.0;
         for (int a = 0; a < L::D; ++a)
             for (int b = 0; b < L::D; ++b) cc += cv[a] * cv[b] * G[a][b];
-        const double neq = -3.0 * tau * L::w(n) * rho * (cc - divu / 3.0);
+        const double neq = -3.0 * (tau - 1.0) * L::w(n) * rho * (cc - divu / 3.0);
         St::template st<Q>(fout, n, c, N, (typename St::R)(feq + neq));
     }
 }

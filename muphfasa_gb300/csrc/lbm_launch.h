@@ -70,6 +70,8 @@ cudaError_t launch_step_fast_f16s(int q, bool forced, const void* fin, void* fou
                                   const KParams* pg, cudaStream_t s);
 cudaError_t launch_step_fast_bf16s(int q, bool forced, const void* fin, void* fout, const KParams& p,
                                    const KParams* pg, cudaStream_t s);
+cudaError_t launch_step_fast_f16c(int q, bool forced, const void* fin, void* fout, const KParams& p,
+                                  const KParams* pg, cudaStream_t s);
 
 // ---- k_f64x.cu (64-bit fixed point on the integer pipes) -----------------
 cudaError_t launch_step_f64x(int q, bool forced, const long long* fin, long long* fout, const KParams& p,

@@ -5,11 +5,12 @@ Cases: lid-driven cavities (MovingWall lid at y = hi, NoSlip elsewhere) and
 channels (Inflow at x = lo, PressureOutlet at x = hi, NoSlip at y = lo, hi),
 n x n cells, Re uniform in [100, 2000] (Re = U n / nu), lid / inflow velocity
 U uniform in [0.02, 0.1], tau = 0.5 + 3 U n / Re, and 0-3 seeded solid boxes
-covering 5-20 % of the domain in total.  FP32 storage.
+covering 5-20 % of the domain in total.
 
-The plain solver (a batch of all cases, one kernel per step) produces the
-steady fields: a case is steady when the relative change of its
-stored-population velocity over 100 steps drops below `tol`.  The surrogate
+The plain solver (a batch of all cases, one kernel per step, FP64-accurate
+fixed-point storage) produces the steady fields: a case is steady when the
+relative change of its stored-population velocity over 100 steps drops
+below `tol` (1e-8).  The surrogate
 (surrogate.UNet) learns (rho, u) from the geometry and parameters; a warm
 start initialises f = feq + f_neq(grad u) from its prediction
 (mph_init_fields_neq), and the same solver iterates to the same residual.
@@ -121,40 +122,118 @@ def fields_from_prediction(c, pred):
     return rho, u
 
 
-def solve(cases, init=None, max_steps=400_000, tol=1e-8, check_every=1000, k=100, log=None, precision="f32"):
-    """Advance all cases together from rest (init None) or from
-    init[i] = (rho, u) (warm start), until each reaches the residual tol over
-    k steps.  Returns (steps per case: -1 not reached, -2 diverged; final
-    (rho, u) per case; seconds; last residual per case)."""
-    set_device(0)
+def _batch(cases, precision):
     b = Batch([case_desc(c, precision) for c in cases])
     for i, c in enumerate(cases):
         b.set_obstacles(i, case_mask(c))
-        if init is None:
-            b.initialize(i)
-        else:
-            b.initialize_neq(i, *init[i])
-    steps = np.full(len(cases), -1, np.int64)
-    last = np.full(len(cases), np.inf)
+    return b
+
+
+def solve(cases, init=None, max_steps=400_000, tol=1e-8, check_every=1000, k=100, log=None, precision="f64x",
+          compact=0.6):
+    """Advance all cases together from rest (init None) or from
+    init[i] = (rho, u) (warm start), until each reaches the residual tol over
+    k steps.  The default storage is the FP64-accurate fixed point (FP32
+    storage stalls near a residual of 1e-6).  Cases that converge or diverge
+    leave the batch: once at most `compact` of a batch's domains still run,
+    the running ones move into a new batch (populations carried over at FP64
+    resolution through mph_batch_set_f), so late cases do not pay for early
+    ones.  Returns (steps per case: -1 not reached, -2 diverged; (rho, u)
+    per case when it stopped; seconds; last residual per case)."""
+    set_device(0)
+    n_all = len(cases)
+    steps = np.full(n_all, -1, np.int64)
+    last = np.full(n_all, np.inf)
+    out = [None] * n_all
     t0 = time.perf_counter()
+    idx = list(range(n_all))  # global index of each batch domain
+    b = _batch(cases, precision)
+    for j, c in enumerate(cases):
+        if init is None:
+            b.initialize(j)
+        else:
+            b.initialize_neq(j, *init[j])
     done = 0
-    while done < max_steps and np.any(steps == -1):
+    while done < max_steps and np.any(steps[idx] == -1):
         b.advance(check_every - k)
         b.residual()
         b.advance(k)
         r, _ = b.residual()
         done += check_every
-        bad = np.isnan(r)
-        last = r
-        newly = (steps < 0) & (r < tol)
-        steps[newly] = done
-        steps[(steps < 0) & bad] = -2  # diverged
+        for j, i in enumerate(idx):
+            if steps[i] != -1:
+                continue
+            last[i] = r[j]
+            if np.isnan(r[j]):
+                steps[i] = -2  # diverged
+                out[i] = b.moments(j)
+            elif r[j] < tol:
+                steps[i] = done
+                out[i] = b.moments(j)
+        running = [j for j, i in enumerate(idx) if steps[i] == -1]
         if log:
-            log(done, int(np.sum(steps > 0)), float(np.nanmedian(r)))
+            log(done, int(np.sum(steps > 0)), float(np.nanmedian(last)), len(idx))
+        if running and len(running) <= compact * len(idx) and done < max_steps:
+            fs = [b.f(j) for j in running]
+            b.close()
+            idx = [idx[j] for j in running]
+            b = _batch([cases[i] for i in idx], precision)
+            for j, f in enumerate(fs):
+                b.set_f(j, f)
+    for j, i in enumerate(idx):
+        if out[i] is None:
+            out[i] = b.moments(j)
     secs = time.perf_counter() - t0
-    out = [b.moments(i) for i in range(len(cases))]
     b.close()
     return steps, out, secs, last
+
+
+def smooth_field(n, rng, modes=3):
+    """A smooth random field on n x n cells: a sum of products of sines with
+    wave numbers 1..modes along each axis and random amplitudes and phases."""
+    t = (np.arange(n) + 0.5) / n
+    f = np.zeros((n, n))
+    for kx in range(1, modes + 1):
+        for ky in range(1, modes + 1):
+            a = rng.standard_normal() / (kx * ky)
+            px, py = rng.uniform(0, 2 * np.pi, 2)
+            f += a * np.sin(np.pi * ky * t + py)[:, None] * np.sin(np.pi * kx * t + px)[None, :]
+    return f
+
+
+def perturbed_fields(c, rho, u, e, rng):
+    """(rho, u) of a converged case with smooth noise of relative L2 amplitude
+    e in u over the fluid cells (and e times the rho - 1 scale in rho);
+    solid cells keep the rest state."""
+    n = c["n"]
+    fluid = case_mask(c).reshape(-1) == 0
+    phi = np.concatenate([smooth_field(n, rng).reshape(-1), smooth_field(n, rng).reshape(-1)])
+    phi[np.tile(~fluid, 2)] = 0.0
+    uf = np.tile(fluid, 2)
+    du = e * np.linalg.norm(u[uf]) / max(np.linalg.norm(phi[uf]), 1e-300) * phi
+    pr = smooth_field(n, rng).reshape(-1)
+    pr[~fluid] = 0.0
+    drho = e * rho_scale(c) * pr / max(np.sqrt(np.mean(pr[fluid] ** 2)), 1e-300)
+    return rho + drho, u + du
+
+
+def perturbation_curve(cases, fields, amps, seed=0, **solve_kw):
+    """Steps to the residual tol from the converged fields of `cases` with
+    smooth noise of each relative amplitude in `amps` (0 = the converged
+    field itself through feq + f_neq), and from rest, all in one batch.
+    Returns {amp: steps per case} with the key 'rest' for the start from rest."""
+    rng = np.random.default_rng(seed)
+    run_cases, inits, keys = [], [], []
+    for c, (rho, u) in zip(cases, fields):
+        for e in amps:
+            run_cases.append(c)
+            inits.append(perturbed_fields(c, rho, u, e, rng))
+            keys.append(e)
+    steps, _, secs, _ = solve(run_cases, inits, **solve_kw)
+    plain, _, secs_rest, _ = solve(cases, None, **solve_kw)
+    table = {e: [int(s) for s, k in zip(steps, keys) if k == e] for e in amps}
+    table["rest"] = [int(s) for s in plain]
+    return table, secs + secs_rest
 
 
 def dataset(cases, fields, limit=20.0):

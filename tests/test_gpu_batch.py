@@ -18,7 +18,7 @@ def _cavity(mph, n, omega, lid, precision, lattice="D2Q9"):
     return mph.make_desc(lattice, n, omega, faces=faces, face_U=U, precision=precision)
 
 
-@pytest.mark.parametrize("precision", ["f64", "f32", "f16s", "f64x"])
+@pytest.mark.parametrize("precision", ["f64", "f32", "f16s", "f64x", "f16c"])
 def test_batch_domains_equal_single_handles(precision, mph):
     descs = [_cavity(mph, (17, 17), 1.2, 0.1, precision), _cavity(mph, (64, 48), 1.7, 0.05, precision),
              _cavity(mph, (100, 100), 0.9, 0.1, precision), _cavity(mph, (33, 65), 1.9, 0.08, precision)]
@@ -42,7 +42,7 @@ def test_batch_domains_equal_single_handles(precision, mph):
     assert total == sum(batch.ncells) and kcells in ((1, 2) if precision == "f64x" else (1, 2, 4)) and nchunks > 0
 
 
-@pytest.mark.parametrize("precision", ["f64", "f16s", "bf16s", "f64x"])
+@pytest.mark.parametrize("precision", ["f64", "f16s", "bf16s", "f64x", "f16c"])
 def test_batch_3d_forced_mixed_boundaries(precision, mph):
     faces_a = ["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic", "Periodic"]
     faces_b = ["Inflow", "PressureOutlet", "NoSlip", "MovingWall", "Periodic", "Periodic"]
@@ -65,7 +65,7 @@ def test_batch_3d_forced_mixed_boundaries(precision, mph):
         assert np.array_equal(batch.f(i), s.f())
 
 
-@pytest.mark.parametrize("precision", ["f32", "f16s", "bf16s", "f64x"])
+@pytest.mark.parametrize("precision", ["f32", "f16s", "bf16s", "f64x", "f16c"])
 def test_looped_launches_equal_batched(precision, mph):
     """Per-domain launches (the single-domain kernels, two cells per thread
     for the 16-bit policies on even sides) against the batched kernel; the
@@ -152,3 +152,30 @@ def test_f64x_batch_range_flag_and_candidate_rejection(mph, monkeypatch):
     with pytest.raises(mph.MphError) as ei:
         c.advance(1)
     assert ei.value.code == 1
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32", "f16s", "f64x"])
+def test_batch_set_f_equals_single_handle_set_f(precision, mph):
+    """mph_batch_set_f converts like mph_set_f: a domain loaded from the same
+    FP64 populations and advanced equals a single handle, and an FP64 batch
+    returns the loaded values unchanged."""
+    descs = [_cavity(mph, (20, 18), 1.3, 0.1, precision), _cavity(mph, (33, 40), 1.7, 0.05, precision)]
+    b = mph.Batch(descs)
+    singles = [mph.Simulation(d) for d in descs]
+    rng = np.random.default_rng(12)
+    for i, s in enumerate(singles):
+        b.initialize(i)
+        s.initialize()
+    b.advance(5)
+    for i, s in enumerate(singles):
+        s.advance(5)
+    f1 = singles[1].f() * (1.0 + 1e-3 * rng.standard_normal(9 * b.ncells[1]))
+    b.set_f(1, f1)
+    singles[1].set_f(f1)
+    if precision == "f64":
+        assert np.array_equal(b.f(1), f1)
+    b.advance(9)
+    for s in singles:
+        s.advance(9)
+    for i, s in enumerate(singles):
+        assert np.array_equal(b.f(i), s.f()), i

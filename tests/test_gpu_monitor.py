@@ -85,7 +85,9 @@ def test_small_cavity_reaches_residual_1e8(mph):
 
 
 def _neq_reference(mph, desc, rho, u, solid, tau):
-    """NumPy restatement of the warm-start initialisation (feq + f_neq)."""
+    """NumPy restatement of the warm-start initialisation: feq + the
+    post-collision first-order non-equilibrium part, -((tau - 1) w rho / cs2)
+    (c c - cs2 I) : grad u."""
     c, w, _ = mph.lattice_tables("D2Q9")
     ny, nx = desc.n[1], desc.n[0]
     per = [desc.face_type[0] == mph.BC["Periodic"], desc.face_type[2] == mph.BC["Periodic"]]
@@ -114,7 +116,7 @@ def _neq_reference(mph, desc, rho, u, solid, tau):
         cu = c[n, 0] * U[0] + c[n, 1] * U[1]
         feq = w[n] * R * (1 + 3 * cu + 4.5 * cu * cu - 1.5 * usq)
         cc = sum(c[n, a] * c[n, b] * G[a, b] for a in range(2) for b in range(2))
-        f[n] = feq - 3.0 * tau * w[n] * R * (cc - div / 3.0)
+        f[n] = feq - 3.0 * (tau - 1.0) * w[n] * R * (cc - div / 3.0)
         f[n][S] = w[n]
     return f.reshape(9, -1)
 
