@@ -270,10 +270,18 @@ def run_ceiling(args):
                          "gbs": round(gbs, 1), "frac": round(gbs / peak, 4),
                          "glups": round(n ** 3 / (best / 1e3) / 1e9, 2)})
             print(json.dumps({"progress": rows[-1]}), file=sys.stderr, flush=True)
+    # arithmetic pipes (mph_pipe_rate): operations per second and per SM per clock
+    sm = ClockSampler(0)
+    with sm:
+        rates = {name: m.pipe_rate(op) for op, name in enumerate(("DFMA", "FFMA", "IMAD32", "UMULHI64+ADD",
+                                                                  "I2F.F64.S64+DADD"))}
+    clk = sm.summary()
+    mhz = clk.get("sm_mhz") or 2070.0
+    pipes = {k: {"gops": round(v / 1e9, 1), "per_sm_per_clk": round(v / 152 / (mhz * 1e6), 2)} for k, v in rates.items()}
     line = {"metric": "pull-stencil copy bandwidth (the step's memory pattern, no arithmetic)", "value": None,
             "unit": "GB/s", "n_gpus": 1, "steps": args.steps, "higher_is_better": True, "data": "synthetic",
             "config": {"workload": f"pull_copy_{n}^3", "best_of": 3, "peak": peak, "peak_kind": kind},
-            "rows": rows}
+            "rows": rows, "pipes": pipes, "pipes_clocks": clk}
     print(json.dumps(line), flush=True)
     return 0
 

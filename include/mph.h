@@ -295,6 +295,12 @@ int mph_batch_info(const mph_batch* b, long long* total_cells, int* cells_per_th
  * (modes 1 and 2: 2-byte elements, nx even).  *ms = mean milliseconds per
  * pass; a pass moves 2 q elem_bytes bytes per cell. */
 int mph_pull_copy_timed(int elem_bytes, int mode, int q, int nx, int ny, int nz, int reps, float* ms);
+/* Instruction throughput of one arithmetic pipe of the current device
+ * (operations per second, one per instruction), the rates that decide
+ * which precision paths are compute-bound: op 0 DFMA, 1 FFMA, 2 32-bit
+ * IMAD, 3 64-bit unsigned high multiply + add, 4 int64 -> FP64 conversion
+ * + FP64 add.  No counterpart in the reference. */
+int mph_pipe_rate(int op, double* ops_per_s);
 
 /* ---- allocation-free sums ---------------------------------------------- */
 /* No counterpart in the reference.  The FP64 mass and momentum sums of

@@ -38,7 +38,7 @@ EXPORTS = [
     "mph_inputs_get", "mph_inputs_derive", "mph_resolve_bc", "mph_create", "mph_destroy", "mph_set_f",
     "mph_get_f", "mph_init_fields", "mph_advance", "mph_update_macroscopic", "mph_reduce", "mph_time",
     "mph_launches_per_step", "mph_advance_timed", "mph_step_host", "mph_pull_collide_fused_arr",
-    "mph_periodic_fill_arr", "mph_bc_fill_arr", "mph_reduce_f64_noalloc", "mph_pull_copy_timed", "mph_batch_create",
+    "mph_periodic_fill_arr", "mph_bc_fill_arr", "mph_reduce_f64_noalloc", "mph_pull_copy_timed", "mph_pipe_rate", "mph_batch_create",
     "mph_batch_destroy", "mph_batch_init_fields", "mph_batch_advance", "mph_batch_advance_timed",
     "mph_batch_advance_looped_timed", "mph_batch_get_f", "mph_batch_set_f", "mph_batch_moments", "mph_batch_info",
     "mph_residual", "mph_batch_residual", "mph_lattice", "mph_set_obstacles", "mph_batch_set_obstacles",
@@ -133,6 +133,7 @@ def lib():
     L.mph_bc_fill_arr.argtypes = [C.c_int, C.c_int, ip, ip, ip, C.POINTER(ResolvedBC), C.POINTER(Array4), P]
     L.mph_reduce_f64_noalloc.argtypes = [C.c_int, C.c_int, P, C.c_longlong, P, P]
     L.mph_pull_copy_timed.argtypes = [C.c_int] * 7 + [C.POINTER(C.c_float)]
+    L.mph_pipe_rate.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.mph_batch_create.argtypes = [C.c_int, C.POINTER(Desc), C.POINTER(P)]
     L.mph_batch_destroy.argtypes = [P]
     L.mph_batch_init_fields.argtypes = [P, C.c_int, dp, dp]
@@ -197,6 +198,14 @@ def pull_copy_ms(elem_bytes, mode, q, n, reps=20):
     check(lib().mph_pull_copy_timed(int(elem_bytes), int(mode), int(q), int(nn[0]), int(nn[1]), int(nn[2]), int(reps),
                                     C.byref(ms)))
     return float(ms.value)
+
+
+def pipe_rate(op):
+    """Operations per second of one arithmetic pipe (mph_pipe_rate): 0 DFMA,
+    1 FFMA, 2 IMAD, 3 64-bit high multiply + add, 4 int64 -> FP64 + add."""
+    r = C.c_double()
+    check(lib().mph_pipe_rate(int(op), C.byref(r)))
+    return float(r.value)
 
 
 def make_desc(lattice: str, n, omega: float, faces=None, face_rho=None, face_U=None, force=None,

@@ -97,6 +97,69 @@ __global__ void __launch_bounds__(256) k_copy_words(const unsigned short* __rest
     }
 }
 
+// Instruction throughput of one pipe: every thread runs kIlp independent
+// dependency chains of `iters` operations (enough independent work to fill
+// the pipe), and the chains are folded into one stored value so nothing is
+// dead code.
+//   op 0 DFMA (FP64 pipe)   1 FFMA (FP32)   2 IMAD 32-bit   3 64-bit unsigned
+//   high multiply + add (the fixed-point step's multiply)   4 int64 -> FP64
+//   conversion + FP64 add (the conversions of fixed-point loads and stores)
+constexpr int kIlp = 8;
+
+template <int OP>
+__global__ void __launch_bounds__(256) k_pipe(double* __restrict__ out, int iters, double a) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    double r = 0.0;
+    if (OP == 0) {
+        double x[kIlp];
+        for (int i = 0; i < kIlp; ++i) x[i] = t * 1e-9 + i;
+        for (int it = 0; it < iters; ++it)
+#pragma unroll
+            for (int i = 0; i < kIlp; ++i) x[i] = fma(x[i], a, 1e-3);
+        for (int i = 0; i < kIlp; ++i) r += x[i];
+    } else if (OP == 1) {
+        float x[kIlp];
+        const float af = (float)a;
+        for (int i = 0; i < kIlp; ++i) x[i] = t * 1e-6f + i;
+        for (int it = 0; it < iters; ++it)
+#pragma unroll
+            for (int i = 0; i < kIlp; ++i) x[i] = fmaf(x[i], af, 1e-3f);
+        for (int i = 0; i < kIlp; ++i) r += x[i];
+    } else if (OP == 2) {
+        unsigned x[kIlp];
+        const unsigned m = (unsigned)(a * 1e6) | 1u;
+        for (int i = 0; i < kIlp; ++i) x[i] = t + i;
+        for (int it = 0; it < iters; ++it)
+#pragma unroll
+            for (int i = 0; i < kIlp; ++i) x[i] = x[i] * m + 7u;
+        unsigned s = 0;
+        for (int i = 0; i < kIlp; ++i) s ^= x[i];
+        r = s;
+    } else if (OP == 3) {
+        unsigned long long x[kIlp];
+        const unsigned long long m = (unsigned long long)(a * 1e15) | 1ull;
+        for (int i = 0; i < kIlp; ++i) x[i] = t * 0x9E3779B97F4A7C15ull + i;
+        for (int it = 0; it < iters; ++it)
+#pragma unroll
+            for (int i = 0; i < kIlp; ++i) x[i] = __umul64hi(x[i], m) + x[i];
+        unsigned long long s = 0;
+        for (int i = 0; i < kIlp; ++i) s ^= x[i];
+        r = (double)(s >> 11);
+    } else {
+        double x[kIlp];
+        long long v[kIlp];
+        for (int i = 0; i < kIlp; ++i) { x[i] = 0.0; v[i] = (long long)t * 3 + i; }
+        for (int it = 0; it < iters; ++it)
+#pragma unroll
+            for (int i = 0; i < kIlp; ++i) {
+                x[i] += (double)v[i];
+                v[i] += it;
+            }
+        for (int i = 0; i < kIlp; ++i) r += x[i];
+    }
+    out[t] = r;
+}
+
 template <class F>
 cudaError_t with_q3(int q, F&& f) {
     switch (q) {
@@ -178,5 +241,42 @@ extern "C" int mph_pull_copy_timed(int elem_bytes, int mode, int q, int nx, int 
     cudaFree(b);
     if (e != cudaSuccess) return fail(MPH_ERR_CUDA, std::string("mph_pull_copy_timed: ") + cudaGetErrorString(e));
     *ms = t / reps;
+    return MPH_OK;
+}
+
+extern "C" int mph_pipe_rate(int op, double* ops_per_s) {
+    using namespace mph;
+    if (!ops_per_s || op < 0 || op > 4) return fail(MPH_ERR_ARG, "mph_pipe_rate: bad argument");
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = 8 * sms, threads = 256, iters = 4096;
+    double* out = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (e == cudaSuccess) e = cudaMalloc(&out, sizeof(double) * blocks * threads);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    auto launch = [&](int it) {
+        switch (op) {
+            case 0: k_pipe<0><<<blocks, threads>>>(out, it, 0.999999); break;
+            case 1: k_pipe<1><<<blocks, threads>>>(out, it, 0.999999); break;
+            case 2: k_pipe<2><<<blocks, threads>>>(out, it, 0.999999); break;
+            case 3: k_pipe<3><<<blocks, threads>>>(out, it, 0.999999); break;
+            default: k_pipe<4><<<blocks, threads>>>(out, it, 0.999999); break;
+        }
+        return cudaGetLastError();
+    };
+    if (e == cudaSuccess) e = launch(iters);  // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(e0);
+    for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = launch(iters);
+    if (e == cudaSuccess) e = cudaEventRecord(e1);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(out);
+    if (e != cudaSuccess) return fail(MPH_ERR_CUDA, std::string("mph_pipe_rate: ") + cudaGetErrorString(e));
+    *ops_per_s = 3.0 * blocks * threads * (double)iters * kIlp / (ms / 1e3);
     return MPH_OK;
 }
