@@ -252,7 +252,8 @@ int mph_bc_fill_arr(int dim, int q, const int dom_lo[3], const int dom_hi[3],
  * omega, boundary faces and force.  Domain d's results equal those of a
  * single handle created from descs[d], bit for bit.  With MPH_PREC_F64X a
  * cell leaving the fixed-point range makes the advance return
- * MPH_ERR_NONFINITE, as for a single handle. */
+ * MPH_ERR_NONFINITE, as for a single handle, and flags its domain
+ * (mph_batch_range_flags). */
 typedef struct mph_batch mph_batch;
 int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out);
 int mph_batch_destroy(mph_batch* b);
@@ -278,6 +279,14 @@ int mph_batch_set_obstacles(mph_batch* b, int domain, const unsigned char* mask)
  * change of domain d's stored-population velocity since the previous call
  * (+inf on the first call after an init), out[2 d + 1] = ||u_d||_2. */
 int mph_batch_residual(mph_batch* b, double* out);
+/* Fixed-point batches (MPH_PREC_F64X): flags[d] = 1 for every domain d
+ * whose populations left the representable range in an advance since the
+ * domain was last initialised or set (mph_batch_advance then returned
+ * MPH_ERR_NONFINITE, and mph_batch_residual reports NaN for it).  The other
+ * domains stepped normally: a caller can drop the flagged ones and go on.
+ * All zero for other precisions.  No counterpart in the reference (its
+ * single domain aborts on a non-finite density). */
+int mph_batch_range_flags(const mph_batch* b, int* flags);
 /* Total cells, cells per thread chosen by the autotuner (0 before the first
  * advance), the number of 256-thread chunks per step, and whether the chosen
  * launch is a persistent grid (1) or one block per chunk (0). */

@@ -41,7 +41,7 @@ EXPORTS = [
     "mph_periodic_fill_arr", "mph_bc_fill_arr", "mph_reduce_f64_noalloc", "mph_pull_copy_timed", "mph_pipe_rate", "mph_batch_create",
     "mph_batch_destroy", "mph_batch_init_fields", "mph_batch_advance", "mph_batch_advance_timed",
     "mph_batch_advance_looped_timed", "mph_batch_get_f", "mph_batch_set_f", "mph_batch_moments", "mph_batch_info",
-    "mph_residual", "mph_batch_residual", "mph_lattice", "mph_set_obstacles", "mph_batch_set_obstacles",
+    "mph_residual", "mph_batch_residual", "mph_batch_range_flags", "mph_lattice", "mph_set_obstacles", "mph_batch_set_obstacles",
     "mph_init_fields_neq", "mph_batch_init_fields_neq", "mph_set_time", "mph_state_bytes", "mph_get_state",
     "mph_set_state", "mph_host_alloc", "mph_host_free", "mph_nn_alloc", "mph_nn_free", "mph_nn_copy", "mph_nn_sync", "mph_nn_gemm", "mph_nn_im2col3", "mph_nn_col2im3",
     "mph_nn_bias_act", "mph_nn_act_bwd", "mph_nn_colsum", "mph_nn_pool", "mph_nn_pool_bwd", "mph_nn_up",
@@ -134,6 +134,7 @@ def lib():
     L.mph_reduce_f64_noalloc.argtypes = [C.c_int, C.c_int, P, C.c_longlong, P, P]
     L.mph_pull_copy_timed.argtypes = [C.c_int] * 7 + [C.POINTER(C.c_float)]
     L.mph_pipe_rate.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    L.mph_batch_range_flags.argtypes = [P, C.POINTER(C.c_int)]
     L.mph_batch_create.argtypes = [C.c_int, C.POINTER(Desc), C.POINTER(P)]
     L.mph_batch_destroy.argtypes = [P]
     L.mph_batch_init_fields.argtypes = [P, C.c_int, dp, dp]
@@ -478,6 +479,13 @@ class Batch:
         out = np.zeros(2 * len(self.descs))
         check(lib().mph_batch_residual(self._h, _dp(out)))
         return out[0::2].copy(), out[1::2].copy()
+
+    def range_flags(self):
+        """Per-domain flags of a fixed-point batch: True where the domain's
+        populations left the representable range (mph_batch_range_flags)."""
+        out = (C.c_int * len(self.descs))()
+        check(lib().mph_batch_range_flags(self._h, out))
+        return np.array(out[:], dtype=bool)
 
     def info(self):
         """(total cells, cells per thread, chunks per step, persistent grid) of

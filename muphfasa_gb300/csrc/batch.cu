@@ -120,11 +120,14 @@ struct mph_batch {
     long long max_cells = 0;
     std::vector<KParams> params_h;
     // fixed-point precision: per-domain constants, bounce-back tables
-    // (27 x 27 per domain) and the range flag of the step kernels
+    // (27 x 27 per domain) and the range flags of the step kernels (one per
+    // domain on the device, cleared after each read; bad_h keeps them on the
+    // host until the domain is initialised or its populations replaced)
     std::vector<KParamsX> px_h;
     KParamsX* d_px = nullptr;
     long long* d_kbb = nullptr;
     int* d_flag = nullptr;
+    std::vector<int> bad_h;
     // cells needing the boundary rules {domain, cell}
     int2* d_walls = nullptr;
     int nwalls = 0;
@@ -304,7 +307,7 @@ int autotune(mph_batch* b) {
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->fa, save, bytes, cudaMemcpyDeviceToDevice, b->stream);
     // only the steps of the caller's advances report the range flag
-    if (e == cudaSuccess && b->d_flag) e = cudaMemsetAsync(b->d_flag, 0, sizeof(int), b->stream);
+    if (e == cudaSuccess && b->d_flag) e = cudaMemsetAsync(b->d_flag, 0, sizeof(int) * b->ndom, b->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     cudaFree(save);
     if (e != cudaSuccess) return cuda_fail(e, "autotune");
@@ -360,16 +363,27 @@ int ensure_graph(mph_batch* b) {
     return MPH_OK;
 }
 
-// Range flag of the fixed-point step (read and cleared after an advance).
+// Range flags of the fixed-point step, one per domain (read and cleared
+// after an advance, kept in bad_h).
 int check_flag(mph_batch* b) {
     if (!b->d_flag) return MPH_OK;
-    int flag = 0;
-    MPH_CK(cudaMemcpyAsync(&flag, b->d_flag, sizeof(int), cudaMemcpyDeviceToHost, b->stream), "read flag");
+    std::vector<int> flag(b->ndom, 0);
+    MPH_CK(cudaMemcpyAsync(flag.data(), b->d_flag, sizeof(int) * b->ndom, cudaMemcpyDeviceToHost, b->stream),
+           "read flag");
     MPH_CK(cudaStreamSynchronize(b->stream), "read flag");
-    if (flag) {
-        MPH_CK(cudaMemsetAsync(b->d_flag, 0, sizeof(int), b->stream), "clear flag");
-        return fail(MPH_ERR_NONFINITE, "fixed-point batch step: a cell left the representable range "
-                                       "(rho outside (1/16, 64) or |J|, |u| >= 4)");
+    int nbad = 0, first = -1;
+    for (int d = 0; d < b->ndom; ++d)
+        if (flag[d]) {
+            b->bad_h[d] = 1;
+            ++nbad;
+            if (first < 0) first = d;
+        }
+    if (nbad) {
+        MPH_CK(cudaMemsetAsync(b->d_flag, 0, sizeof(int) * b->ndom, b->stream), "clear flag");
+        return fail(MPH_ERR_NONFINITE, "fixed-point batch step: a cell of " + std::to_string(nbad) +
+                                           " domain(s) (first: " + std::to_string(first) +
+                                           ") left the representable range (rho outside (1/16, 64) or |J|, "
+                                           "|u| >= 4); mph_batch_range_flags lists them");
     }
     return MPH_OK;
 }
@@ -471,8 +485,9 @@ int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out) {
         if (e == cudaSuccess) e = cudaMalloc(&b->d_kbb, sizeof(long long) * kbb_h.size());
         if (e == cudaSuccess)
             e = cudaMemcpy(b->d_kbb, kbb_h.data(), sizeof(long long) * kbb_h.size(), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = cudaMalloc(&b->d_flag, sizeof(int));
-        if (e == cudaSuccess) e = cudaMemset(b->d_flag, 0, sizeof(int));
+        if (e == cudaSuccess) e = cudaMalloc(&b->d_flag, sizeof(int) * ndomains);
+        if (e == cudaSuccess) e = cudaMemset(b->d_flag, 0, sizeof(int) * ndomains);
+        b->bad_h.assign(ndomains, 0);
     }
     if (e != cudaSuccess) {
         int rc = cuda_fail(e, "mph_batch_create");
@@ -516,6 +531,7 @@ int mph_batch_init_fields(mph_batch* b, int domain, double* rho, double* u) {
     MPH_CK(cudaStreamSynchronize(b->stream), "batch init");
     b->time = 0.0;
     b->has_uprev = false;
+    if (!b->bad_h.empty()) b->bad_h[domain] = 0;
     return MPH_OK;
 }
 
@@ -534,6 +550,7 @@ int mph_batch_init_fields_neq(mph_batch* b, int domain, const double* rho, const
     MPH_CK(cudaStreamSynchronize(b->stream), "batch init");
     b->time = 0.0;
     b->has_uprev = false;
+    if (!b->bad_h.empty()) b->bad_h[domain] = 0;
     return MPH_OK;
 }
 
@@ -579,7 +596,7 @@ int mph_batch_advance_looped_timed(mph_batch* b, int nsteps, float* ms) {
                 case MPH_PREC_F16C: e = launch_step_fast_f16c(b->q, b->forced, in, outp, kp, pg, b->stream); break;
                 case MPH_PREC_F64X:
                     e = launch_step_f64x(b->q, b->forced, (const long long*)in, (long long*)outp, kp, b->px_h[d], pg,
-                                         b->d_kbb + (size_t)d * 27 * 27, b->d_flag, b->stream);
+                                         b->d_kbb + (size_t)d * 27 * 27, b->d_flag + d, b->stream);
                     break;
             }
             if (e != cudaSuccess) return cuda_fail(e, "looped step launch");
@@ -631,6 +648,7 @@ int mph_batch_set_f(mph_batch* b, int domain, const double* f) {
     }
     MPH_CK(cudaStreamSynchronize(b->stream), "batch set f");
     b->has_uprev = false;
+    if (!b->bad_h.empty()) b->bad_h[domain] = 0;
     return MPH_OK;
 }
 
@@ -696,8 +714,17 @@ int mph_batch_residual(mph_batch* b, double* out) {
         const double s0 = sums[2 * d], s1 = sums[2 * d + 1];
         out[2 * d + 1] = std::sqrt(s1);
         out[2 * d] = relative_change(s0, s1, b->has_uprev);
+        // a fixed-point domain that left the representable range holds no
+        // meaningful populations: report it as diverged
+        if (!b->bad_h.empty() && b->bad_h[d]) out[2 * d] = out[2 * d + 1] = std::nan("");
     }
     b->has_uprev = true;
+    return MPH_OK;
+}
+
+int mph_batch_range_flags(const mph_batch* b, int* flags) {
+    if (!b || !flags) return fail(MPH_ERR_ARG, "mph_batch_range_flags: NULL argument");
+    for (int d = 0; d < b->ndom; ++d) flags[d] = b->bad_h.empty() ? 0 : b->bad_h[d];
     return MPH_OK;
 }
 

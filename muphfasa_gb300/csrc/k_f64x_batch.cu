@@ -10,7 +10,8 @@
 // over the chunk kernel's values.  The collide is collide_x of the
 // single-domain kernel with the domain's own fixed-point constants, so every
 // domain's result is bit-identical to a single f64x handle.  A cell leaving
-// the representable range sets the batch's error flag.
+// the representable range sets flag[domain]: the domains are independent,
+// so the host can drop the flagged ones and keep stepping the rest.
 #include "batch_kernel.cuh"
 #include "fx_kernels.cuh"
 
@@ -25,9 +26,9 @@ __global__ void __launch_bounds__(256) k_batch_step_x(const i64* __restrict__ fi
                                                       const KParamsX* __restrict__ dpx,
                                                       const long long* __restrict__ offs, int* __restrict__ flag) {
     using L = Lat<Q>;
-    int bad = 0;
     // One chunk per block, or a persistent grid walking the list.
     for (int ci = blockIdx.x; ci < nchunks; ci += gridDim.x) {
+        int bad = 0;
         const Chunk ch = chunks[ci];
         const KParams& p = dp[ch.dom];
         const long long off = offs[ch.dom];
@@ -59,8 +60,8 @@ __global__ void __launch_bounds__(256) k_batch_step_x(const i64* __restrict__ fi
 #pragma unroll
             for (int n = 0; n < Q; ++n) fout[(unsigned)n * N + (unsigned)cc[k]] = h[k][n];
         }
+        if (bad) atomicOr(flag + ch.dom, 1);
     }
-    if (bad) atomicOr(flag, 1);
 }
 
 // Cells next to a non-periodic face or an obstacle: {domain, linear cell},
@@ -94,7 +95,7 @@ __global__ void __launch_bounds__(256) k_batch_walls_x(const i64* __restrict__ f
     else pull_x<Q, false>(p, &p, kb, fin, x, y, z, c, h);
     int bad = 0;
     collide_x<Q, FORCED>(dpx[w.x], h, bad);
-    if (bad) atomicOr(flag, 1);
+    if (bad) atomicOr(flag + w.x, 1);
 #pragma unroll
     for (int n = 0; n < Q; ++n) fout[(unsigned)n * N + (unsigned)c] = h[n];
 }

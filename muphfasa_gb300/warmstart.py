@@ -22,7 +22,7 @@ import time
 
 import numpy as np
 
-from . import Batch, make_desc, set_device
+from . import Batch, MphError, make_desc, set_device
 
 RE = (100.0, 2000.0)
 U = (0.02, 0.1)
@@ -134,8 +134,10 @@ def solve(cases, init=None, max_steps=400_000, tol=1e-8, check_every=1000, k=100
     """Advance all cases together from rest (init None) or from
     init[i] = (rho, u) (warm start), until each reaches the residual tol over
     k steps.  The default storage is the FP64-accurate fixed point (FP32
-    storage stalls near a residual of 1e-6).  Cases that converge or diverge
-    leave the batch: once at most `compact` of a batch's domains still run,
+    storage stalls near a residual of 1e-6).  A fixed-point case whose
+    populations leave the representable range (an unstable high-Re case)
+    counts as diverged; the other cases step on.  Cases that converge or
+    diverge leave the batch: once at most `compact` of a batch's domains still run,
     the running ones move into a new batch (populations carried over at FP64
     resolution through mph_batch_set_f), so late cases do not pay for early
     ones.  Returns (steps per case: -1 not reached, -2 diverged; (rho, u)
@@ -153,11 +155,18 @@ def solve(cases, init=None, max_steps=400_000, tol=1e-8, check_every=1000, k=100
             b.initialize(j)
         else:
             b.initialize_neq(j, *init[j])
+    def advance(nsteps):
+        try:
+            b.advance(nsteps)
+        except MphError as ex:
+            if ex.code != 6:  # MPH_ERR_NONFINITE: flagged domains report NaN residuals
+                raise
+
     done = 0
     while done < max_steps and np.any(steps[idx] == -1):
-        b.advance(check_every - k)
+        advance(check_every - k)
         b.residual()
-        b.advance(k)
+        advance(k)
         r, _ = b.residual()
         done += check_every
         for j, i in enumerate(idx):

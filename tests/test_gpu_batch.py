@@ -179,3 +179,34 @@ def test_batch_set_f_equals_single_handle_set_f(precision, mph):
         s.advance(9)
     for i, s in enumerate(singles):
         assert np.array_equal(b.f(i), s.f()), i
+
+
+def test_f64x_range_flags_name_the_bad_domain(mph):
+    """Fault injection on the host: one fixed-point domain starts in a
+    near-vacuum state (rho = 1e-3, below the representable range).  The
+    advance reports MPH_ERR_NONFINITE, the range flags name that domain only,
+    its residual is NaN, and the other domains stepped as single handles do,
+    bit for bit.  Re-initialising the flagged domain clears its flag."""
+    descs = [_cavity(mph, (24, 24), 1.2, 0.1, "f64x"), _cavity(mph, (40, 32), 1.5, 0.05, "f64x"),
+             _cavity(mph, (31, 17), 1.7, 0.08, "f64x")]
+    batch = mph.Batch(descs)
+    singles = [mph.Simulation(d) for d in descs]
+    for i in (0, 2):
+        batch.initialize(i)
+        singles[i].initialize()
+    N = batch.ncells[1]
+    batch.initialize(1, np.full(N, 1e-3), np.zeros(2 * N))
+    batch.residual()
+    with pytest.raises(mph.MphError) as e:
+        batch.advance(6)
+    assert e.value.code == 6
+    assert list(batch.range_flags()) == [False, True, False]
+    r, _ = batch.residual()
+    assert np.isnan(r[1]) and np.isfinite(r[0]) and np.isfinite(r[2])
+    for i in (0, 2):
+        singles[i].advance(6)
+        assert np.array_equal(batch.f(i), singles[i].f()), i
+    batch.initialize(1)
+    assert not batch.range_flags().any()
+    batch.advance(2)
+    assert not batch.range_flags().any()
