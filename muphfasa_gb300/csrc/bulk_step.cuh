@@ -1,0 +1,333 @@
+// bulk_step.cuh -- the 16-bit pair step (shifted FP16 / BF16 / 1-4-11
+// storage) with its pull operands staged in shared memory by one-dimensional
+// bulk asynchronous copies.  Included by the k_fast_* translation units of
+// the 16-bit precisions.
+//
+// Why: a 2-byte population gives a warp only 64 bytes per load instruction,
+// so the direct pair kernel (k_step_pair) keeps too few bytes in flight to
+// cover the HBM latency (the measured copy ceiling of that access pattern is
+// 0.87 of the copy peak, and the step reaches 0.70).  Here the unit of work is
+// a chunk of whole rows (y, z) of the launch window.  For every population n
+// the rows its cells pull from are the chunk's rows shifted by (c_y, c_z):
+// one contiguous run of the population's SoA array (the x shift, periodic x
+// wrap included, stays inside a row).  One thread issues Q cp.async.bulk
+// copies of those runs into one stage of a ring of S shared-memory stages,
+// all completing on that stage's mbarrier; a persistent block keeps S - 1
+// chunks in flight while its 256 threads collide the current chunk from
+// shared memory, one cell pair per thread at a time, and store to global
+// memory directly (no registers hold data in flight).
+//
+// Pulls that fall outside the staged runs (rows wrapped by a periodic y or z
+// face) read global memory, and pairs next to a non-periodic face take the
+// boundary rules of the direct kernel: the values and the collide are those
+// of k_step_pair, so the results are equal bit for bit.
+//
+// Alignment: a bulk copy moves a multiple of 16 bytes between 16-byte aligned
+// addresses, so each run is widened to 8-element boundaries and clipped to the
+// last whole 16 bytes of the array (anything past that is read directly).
+// Waits: every mbarrier wait is bounded by %globaltimer; on a timeout the
+// block ORs 2 into *flag, waits (bounded) for its copies still in flight and
+// returns, so the context stays usable and the host reports the error.
+#pragma once
+
+#include "lbm_kernels.cuh"
+
+namespace mph {
+
+// Launch geometry of one window, computed on the host.
+struct BulkGeom {
+    int rows;        // rows per chunk
+    int cpp;         // chunks per plane of the window
+    int nchunks;     // chunks of the window
+    int lpad;        // elements of one staged run slot (a multiple of 8)
+    unsigned total;  // elements of the array, rounded down to a multiple of 8
+};
+
+namespace bulk {
+
+constexpr int kThreads = 256;
+constexpr int kHeader = 1024;  // bytes before the staged data: mbarriers and run table
+constexpr unsigned long long kWaitNs = 200ull * 1000 * 1000;
+constexpr unsigned long long kSpinLimit = 1ull << 26;
+
+struct Run {
+    unsigned base;  // element index of the staged run in the array
+    unsigned len;   // staged elements (0: nothing staged)
+};
+
+__device__ __forceinline__ unsigned sa(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long now_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void bar_init(unsigned long long* b) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(sa(b)) : "memory");
+}
+
+// The one arrival of a phase, announcing `bytes` of copies that complete it.
+__device__ __forceinline__ void bar_expect(unsigned long long* b, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(sa(b)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void copy_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* b) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(sa(dst)),
+        "l"(src), "r"(bytes), "r"(sa(b))
+        : "memory");
+}
+
+// Bounded wait for the phase of parity `parity`; false on timeout.
+__device__ __forceinline__ bool bar_wait(unsigned long long* b, unsigned parity) {
+    const unsigned addr = sa(b);
+    const unsigned long long t0 = now_ns();
+    for (unsigned long long it = 0; it < kSpinLimit; ++it) {
+        unsigned done;
+        asm volatile(
+            "{\n.reg .pred q;\nmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\nselp.u32 %0, 1, 0, q;\n}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((it & 63) == 63 && now_ns() - t0 > kWaitNs) return false;
+    }
+    return false;
+}
+
+}  // namespace bulk
+
+template <int Q, class St, bool FORCED, int S>
+__global__ void __launch_bounds__(bulk::kThreads, 3) k_step_pair_bulk(const typename St::T* __restrict__ fin,
+                                                                   typename St::T* __restrict__ fout, const KParams p,
+                                                                   const KParams* __restrict__ pg, const BulkGeom gm,
+                                                                   int* __restrict__ flag) {
+    using L = Lat<Q>;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem);
+    bulk::Run* runs = reinterpret_cast<bulk::Run*>(smem + 64);  // [S][Q]
+    unsigned short* data = reinterpret_cast<unsigned short*>(smem + bulk::kHeader);  // [S][Q][lpad]
+    const int tid = threadIdx.x;
+    const unsigned N = (unsigned)p.ncell;
+    const int G = gridDim.x;
+    if (tid == 0) {
+        for (int s = 0; s < S; ++s) bulk::bar_init(&bar[s]);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+
+    // Thread 0: the runs of chunk k into stage s, and their copies.
+    auto issue = [&](int k, int s) {
+        const int pz = k / gm.cpp;
+        const int z = p.z0 + pz;
+        const int yb = p.y0 + (k - pz * gm.cpp) * gm.rows;
+        const int r = min(gm.rows, p.y1 - yb);
+        bulk::Run* rs = runs + s * Q;
+        unsigned bytes = 0;
+#pragma unroll 1
+        for (int n = 0; n < Q; ++n) {
+            int zs = z - L::cz(n);
+            bool ok = true;
+            if (zs < 0 || zs >= p.nz) {
+                if (p.periodic[2]) zs = zs < 0 ? zs + p.nz : zs - p.nz;
+                else ok = false;
+            }
+            const int ya = max(yb - L::cy(n), 0), ye = min(yb + r - L::cy(n), p.ny);
+            bulk::Run run{0u, 0u};
+            if (ok && ye > ya) {
+                const unsigned a = (unsigned)n * N + (unsigned)((zs * p.ny + ya) * p.nx);
+                const unsigned b = (unsigned)n * N + (unsigned)((zs * p.ny + ye) * p.nx);
+                unsigned e = (b + 7u) & ~7u;
+                if (e > gm.total) e = gm.total;
+                run.base = a & ~7u;
+                run.len = e > run.base ? e - run.base : 0u;
+            }
+            rs[n] = run;
+            bytes += 2u * run.len;
+        }
+        bulk::bar_expect(&bar[s], bytes);
+#pragma unroll 1
+        for (int n = 0; n < Q; ++n)
+            if (rs[n].len) bulk::copy_g2s(data + (size_t)(s * Q + n) * gm.lpad, fin + rs[n].base, 2u * rs[n].len, &bar[s]);
+    };
+
+    if (tid == 0)
+        for (int i = 0; i < S - 1; ++i) {
+            const int k = blockIdx.x + i * G;
+            if (k < gm.nchunks) issue(k, i);
+        }
+    int it = 0;
+    bool timed_out = false;
+    for (int k = blockIdx.x; k < gm.nchunks; k += G, ++it) {
+        const int s = it % S;
+        // Refill the stage consumed in the previous iteration (every thread
+        // passed that iteration's closing barrier) with the chunk S - 1 ahead.
+        if (tid == 0) {
+            const int kn = k + (S - 1) * G;
+            if (kn < gm.nchunks) issue(kn, (it + S - 1) % S);
+        }
+        const bool got = bulk::bar_wait(&bar[s], (unsigned)(it / S) & 1u);
+        if (__syncthreads_or(!got)) {
+            timed_out = true;
+            break;
+        }
+        const bulk::Run* rs = runs + s * Q;
+        const unsigned short* st = data + (size_t)s * Q * gm.lpad;
+        const int pz = k / gm.cpp;
+        const int z = p.z0 + pz;
+        const int yb = p.y0 + (k - pz * gm.cpp) * gm.rows;
+        const int r = min(gm.rows, p.y1 - yb);
+        const int hx = p.nx >> 1;
+        const int npairs = r * hx;
+        for (int j = tid; j < npairs; j += bulk::kThreads) {
+            const int row = j / hx;
+            const int x = 2 * (j - row * hx);
+            const int y = yb + row;
+            const unsigned ci = (unsigned)(((long long)z * p.ny + y) * p.nx + x);
+            const Nbr oa = neighbours<L::D>(p, x, y, z), ob = neighbours<L::D>(p, x + 1, y, z);
+            float2 g[Q];
+            if (!oa.wall && !ob.wall) {
+#pragma unroll
+                for (int n = 0; n < Q; ++n) {
+                    const bulk::Run rn = rs[n];
+                    const unsigned ea = (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(oa, n));
+                    const unsigned da = ea - rn.base;
+                    const unsigned short* sn = st + (size_t)n * gm.lpad;
+                    if (L::cx(n) == 0) {
+                        // ea is even and run bases are multiples of 8: an aligned word
+                        g[n] = da < rn.len ? St::dec2(*reinterpret_cast<const unsigned*>(sn + da)) : St::ldr2(fin, ea);
+                    } else {
+                        const unsigned eb = (unsigned)n * N + (unsigned)((int)ci + 1 + upstream<Q>(ob, n));
+                        const unsigned db = eb - rn.base;
+                        const float va = da < rn.len ? St::dec1(sn[da]) : St::ldr1(fin, ea);
+                        const float vb = db < rn.len ? St::dec1(sn[db]) : St::ldr1(fin, eb);
+                        g[n] = make_float2(va, vb);
+                    }
+                }
+            } else {
+                float ga[Q], gb[Q];
+                pull_shift<Q, St>(p, pg, fin, x, y, z, ci, ga);
+                pull_shift<Q, St>(p, pg, fin, x + 1, y, z, ci + 1, gb);
+#pragma unroll
+                for (int n = 0; n < Q; ++n) g[n] = make_float2(ga[n], gb[n]);
+            }
+            collide_shift<Q, A2, FORCED>(p, g);
+#pragma unroll
+            for (int n = 0; n < Q; ++n) St::str2(fout, (unsigned)n * N + ci, g[n]);
+        }
+        __syncthreads();
+    }
+    if (timed_out) {
+        if (tid == 0) {
+            atomicOr(flag, 2);
+            // copies still in flight: the chunks of iterations it .. it + S - 1
+            for (int i = 0; i < S; ++i) {
+                const int j = it + i;
+                if (blockIdx.x + j * G < gm.nchunks) bulk::bar_wait(&bar[j % S], (unsigned)(j / S) & 1u);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Shared-memory bytes of a launch with `stages` stages of Q runs of lpad elements.
+inline size_t bulk_smem_bytes(int q, int stages, int lpad) {
+    return (size_t)bulk::kHeader + (size_t)stages * q * lpad * 2;
+}
+
+// Geometry of the window of p with chunks of about `cells` cells (whole rows;
+// at least one row).  Returns false when the launch does not apply: odd nx,
+// obstacles, a run slot too large for shared memory, or more elements than
+// the 32-bit element indices cover.
+constexpr int kBulkMaxSmem = 227 * 1024;
+
+inline bool bulk_geometry(const KParams& p, int q, int stages, int cells, long long total_elems, BulkGeom& gm) {
+    if (p.nx % 2 != 0 || p.cls || stages < 2 || stages > 4) return false;
+    if (total_elems >= (1LL << 32) - 64) return false;
+    int rows = cells / p.nx;
+    if (rows < 1) rows = 1;
+    const int wy = p.y1 - p.y0;
+    if (rows > wy) rows = wy;
+    if (rows < 1) return false;
+    gm.rows = rows;
+    gm.cpp = (wy + rows - 1) / rows;
+    const long long nch = (long long)gm.cpp * (p.z1 - p.z0);
+    if (nch <= 0 || nch > 0x7fffffffLL) return false;
+    gm.nchunks = (int)nch;
+    gm.lpad = ((rows * p.nx + 14) + 7) & ~7;
+    gm.total = (unsigned)(total_elems & ~7LL);
+    return bulk_smem_bytes(q, stages, gm.lpad) <= (size_t)kBulkMaxSmem;
+}
+
+// Resident blocks of the kernel with `smem` dynamic shared memory times the
+// SM count (host-side queries only, so a launch under stream capture may
+// call it); 0 on error.
+template <class Kern>
+int bulk_grid(Kern k, size_t smem) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, bulk::kThreads, smem) != cudaSuccess) return 0;
+    return per_sm * sms;
+}
+
+// mode 0: raise the dynamic shared-memory limit of the kernels of (q,
+// forced, stages) to the largest block allowance (once per handle, before
+// any launch or capture); mode 1: launch one step.  cudaErrorNotSupported
+// when the launch does not apply to this window (the caller steps it with
+// the direct kernel).
+template <class St>
+cudaError_t launch_step_bulk_t(int mode, int q, bool forced, const void* fin, void* fout, const KParams& p,
+                               const KParams* pg, long long total_elems, int cells, int stages, int* flag,
+                               cudaStream_t s) {
+    BulkGeom gm;
+    size_t smem = 0;
+    if (mode == 1) {
+        if (!bulk_geometry(p, q, stages, cells, total_elems, gm)) return cudaErrorNotSupported;
+        if ((reinterpret_cast<unsigned long long>(fin) | reinterpret_cast<unsigned long long>(fout)) & 15)
+            return cudaErrorNotSupported;
+        smem = bulk_smem_bytes(q, stages, gm.lpad);
+    }
+    auto in = static_cast<const typename St::T*>(fin);
+    auto out = static_cast<typename St::T*>(fout);
+    cudaError_t err = cudaErrorInvalidValue;
+    auto go = [&](auto kern) {
+        if (mode == 0) {
+            err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kBulkMaxSmem);
+            return;
+        }
+        int grid = bulk_grid(kern, smem);
+        if (grid <= 0) {
+            err = cudaGetLastError();
+            if (err == cudaSuccess) err = cudaErrorInvalidConfiguration;
+            return;
+        }
+        if (grid > gm.nchunks) grid = gm.nchunks;
+        kern<<<grid, bulk::kThreads, smem, s>>>(in, out, p, pg, gm, flag);
+        err = cudaGetLastError();
+    };
+#define MPH_BULK_S(QQ, SS)                                      \
+    if (stages == SS) {                                         \
+        if (forced) go(k_step_pair_bulk<QQ, St, true, SS>);     \
+        else go(k_step_pair_bulk<QQ, St, false, SS>);           \
+        return err;                                             \
+    }
+#define MPH_BULK_Q(QQ)    \
+    case QQ:              \
+        MPH_BULK_S(QQ, 2) \
+        MPH_BULK_S(QQ, 3) \
+        MPH_BULK_S(QQ, 4) \
+        return cudaErrorNotSupported;
+    switch (q) {
+        MPH_BULK_Q(9)
+        MPH_BULK_Q(15)
+        MPH_BULK_Q(19)
+        MPH_BULK_Q(27)
+    }
+#undef MPH_BULK_Q
+#undef MPH_BULK_S
+    return cudaErrorNotSupported;
+}
+
+}  // namespace mph

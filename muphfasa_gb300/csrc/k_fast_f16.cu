@@ -1,12 +1,18 @@
 // k_fast_f16.cu -- shifted FP16 storage (f - w), FP32 arithmetic (single
 // domain and batch).
 #include "batch_kernel.cuh"
+#include "bulk_step.cuh"
 #include "k_fast_common.cuh"
 
 namespace mph {
 cudaError_t launch_step_fast_f16s(int q, bool forced, const void* fin, void* fout, const KParams& p,
                                   const KParams* pg, cudaStream_t s) {
     return launch_step_fast<StF16S>(q, forced, fin, fout, p, pg, s);
+}
+cudaError_t launch_step_bulk_f16s(int mode, int q, bool forced, const void* fin, void* fout, const KParams& p,
+                                  const KParams* pg, long long total_elems, int cells, int stages, int* flag,
+                                  cudaStream_t s) {
+    return launch_step_bulk_t<StF16S>(mode, q, forced, fin, fout, p, pg, total_elems, cells, stages, flag, s);
 }
 cudaError_t launch_batch_f16s(int q, bool forced, int K, bool persistent, const void* fin, void* fout, const Chunk* chunks, int nchunks,
                        const int2* walls, int nwalls, const KParams* dp, const long long* offs, cudaStream_t s) {

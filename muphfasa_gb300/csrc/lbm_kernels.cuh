@@ -131,6 +131,12 @@ struct StF16S {
     static __device__ __forceinline__ float2 ldr2(const T* __restrict__ f, unsigned e) {
         return __half22float2(*reinterpret_cast<const __half2*>(f + e));
     }
+    // the same conversions from raw bits (values staged in shared memory)
+    static __device__ __forceinline__ float dec1(unsigned h) { return __half2float(__ushort_as_half((unsigned short)h)); }
+    static __device__ __forceinline__ float2 dec2(unsigned w) {
+        return __half22float2(__halves2half2(__ushort_as_half((unsigned short)(w & 0xFFFFu)),
+                                             __ushort_as_half((unsigned short)(w >> 16))));
+    }
     static __device__ __forceinline__ void str1(T* __restrict__ f, unsigned e, float v) { f[e] = __float2half_rn(v); }
     static __device__ __forceinline__ void str2(T* __restrict__ f, unsigned e, float2 v) {
         *reinterpret_cast<__half2*>(f + e) = __floats2half2_rn(v.x, v.y);
@@ -159,6 +165,7 @@ struct StBF16S {
     static __device__ __forceinline__ float ldr1(const T* __restrict__ f, unsigned e) {
         return __uint_as_float((unsigned)__ldg(reinterpret_cast<const unsigned short*>(f) + e) << 16);
     }
+    static __device__ __forceinline__ float dec1(unsigned h) { return __uint_as_float(h << 16); }
     static __device__ __forceinline__ float2 dec2(unsigned w) {
         return make_float2(__uint_as_float(w << 16), __uint_as_float(w & 0xffff0000u));
     }
@@ -220,6 +227,7 @@ struct StF16C {
     using R = float;
     static constexpr bool kShift = true;
     static __device__ __forceinline__ float ldr1(const T* __restrict__ f, unsigned e) { return f16c::decode(__ldg(f + e)); }
+    static __device__ __forceinline__ float dec1(unsigned h) { return f16c::decode(h); }
     static __device__ __forceinline__ float2 dec2(unsigned w) {
         return make_float2(f16c::decode(w & 0xFFFFu), f16c::decode(w >> 16));
     }

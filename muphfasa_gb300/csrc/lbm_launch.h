@@ -72,6 +72,22 @@ cudaError_t launch_step_fast_bf16s(int q, bool forced, const void* fin, void* fo
                                    const KParams* pg, cudaStream_t s);
 cudaError_t launch_step_fast_f16c(int q, bool forced, const void* fin, void* fout, const KParams& p,
                                   const KParams* pg, cudaStream_t s);
+// The 16-bit pair step with bulk-copy staging (bulk_step.cuh): chunks of
+// about `cells` cells of whole rows, `stages` shared-memory stages (2..4),
+// total_elems = elements of the population array, flag |= 2 on a wait
+// timeout.  mode 0 prepares the kernels (once per handle, before any launch
+// or stream capture), mode 1 launches.  cudaErrorNotSupported when the launch
+// does not apply (odd nx, obstacles, rows too long for shared memory): use
+// the direct step then.
+cudaError_t launch_step_bulk_f16s(int mode, int q, bool forced, const void* fin, void* fout, const KParams& p,
+                                  const KParams* pg, long long total_elems, int cells, int stages, int* flag,
+                                  cudaStream_t s);
+cudaError_t launch_step_bulk_bf16s(int mode, int q, bool forced, const void* fin, void* fout, const KParams& p,
+                                   const KParams* pg, long long total_elems, int cells, int stages, int* flag,
+                                   cudaStream_t s);
+cudaError_t launch_step_bulk_f16c(int mode, int q, bool forced, const void* fin, void* fout, const KParams& p,
+                                  const KParams* pg, long long total_elems, int cells, int stages, int* flag,
+                                  cudaStream_t s);
 
 // ---- k_f64x.cu (64-bit fixed point on the integer pipes) -----------------
 cudaError_t launch_step_f64x(int q, bool forced, const long long* fin, long long* fout, const KParams& p,

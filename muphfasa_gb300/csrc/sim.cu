@@ -22,8 +22,10 @@ struct mph_sim {
     KParamsX kpx;             // fixed-point constants (MPH_PREC_F64X)
     KParams* d_kp = nullptr;  // global copy for the boundary path
     long long* d_kbb = nullptr;  // fixed-point bounce-back constants [27][27]
-    int* d_flag = nullptr;       // range / validity flag of the fixed-point step
+    int* d_flag = nullptr;       // range flag of the fixed-point step (1), wait timeout of a staged step (2)
     int pipe_ctas = 0;           // resident CTAs of the pipelined fixed-point kernel (0: direct kernel)
+    int bulk_stages = 0;         // 16-bit storage: shared-memory stages of the bulk-copy step (0: direct kernel)
+    int bulk_cells = 512;        // cells per chunk of the bulk-copy step
     size_t elem = 8;          // bytes per stored population value
     void* fa = nullptr;       // current populations (m_fin)
     void* fb = nullptr;       // next populations (m_fout)
@@ -307,6 +309,23 @@ int ensure_stage(mph_sim* s) {
 
 bool is_f64(const mph_sim* s) { return s->d.precision == MPH_PREC_F64 || s->d.precision == MPH_PREC_F64_FAST; }
 
+// The bulk-copy staged step of the 16-bit storages (mode 0: prepare the
+// kernel once, mode 1: one step fa -> fb over the window of kp).
+cudaError_t launch_bulk(mph_sim* s, int mode, const KParams& kp) {
+    const long long total = (long long)s->d.q * s->kp.ncell;
+    const int q = s->d.q, st = s->bulk_stages, cells = s->bulk_cells;
+    const bool forced = s->d.forced != 0;
+    switch (s->d.precision) {
+        case MPH_PREC_F16S:
+            return launch_step_bulk_f16s(mode, q, forced, s->fa, s->fb, kp, s->d_kp, total, cells, st, s->d_flag, s->stream);
+        case MPH_PREC_BF16S:
+            return launch_step_bulk_bf16s(mode, q, forced, s->fa, s->fb, kp, s->d_kp, total, cells, st, s->d_flag, s->stream);
+        case MPH_PREC_F16C:
+            return launch_step_bulk_f16c(mode, q, forced, s->fa, s->fb, kp, s->d_kp, total, cells, st, s->d_flag, s->stream);
+    }
+    return cudaErrorNotSupported;
+}
+
 // One step fa -> fb over the window of kp (the whole domain, or a slab of
 // planes for the host-copy pipeline; slabs take the direct fixed-point kernel).
 cudaError_t launch_step_window(mph_sim* s, const KParams& kp, bool whole) {
@@ -320,11 +339,18 @@ cudaError_t launch_step_window(mph_sim* s, const KParams& kp, bool whole) {
         case MPH_PREC_F32:
             return launch_step_fast_f32(q, forced, (const float*)s->fa, (float*)s->fb, kp, s->d_kp, s->stream);
         case MPH_PREC_F16S:
-            return launch_step_fast_f16s(q, forced, s->fa, s->fb, kp, s->d_kp, s->stream);
         case MPH_PREC_BF16S:
-            return launch_step_fast_bf16s(q, forced, s->fa, s->fb, kp, s->d_kp, s->stream);
-        case MPH_PREC_F16C:
+        case MPH_PREC_F16C: {
+            if (s->bulk_stages > 0) {
+                const cudaError_t e = launch_bulk(s, 1, kp);
+                if (e != cudaErrorNotSupported) return e;
+            }
+            if (s->d.precision == MPH_PREC_F16S)
+                return launch_step_fast_f16s(q, forced, s->fa, s->fb, kp, s->d_kp, s->stream);
+            if (s->d.precision == MPH_PREC_BF16S)
+                return launch_step_fast_bf16s(q, forced, s->fa, s->fb, kp, s->d_kp, s->stream);
             return launch_step_fast_f16c(q, forced, s->fa, s->fb, kp, s->d_kp, s->stream);
+        }
         case MPH_PREC_F64X:
             if (whole && s->pipe_ctas > 0)
                 return launch_step_f64x_pipe(q, forced, (const long long*)s->fa, (long long*)s->fb, kp, s->kpx,
@@ -339,10 +365,15 @@ cudaError_t launch_one_step(mph_sim* s) { return launch_step_window(s, s->kp, tr
 
 // Range flag of the fixed-point step: a cell left the representable range.
 int check_flag(mph_sim* s) {
-    if (s->d.precision != MPH_PREC_F64X) return MPH_OK;
+    if (s->d.precision != MPH_PREC_F64X && s->bulk_stages == 0) return MPH_OK;
     int flag = 0;
     MPH_CK(cudaMemcpyAsync(&flag, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "read flag");
     MPH_CK(cudaStreamSynchronize(s->stream), "read flag");
+    if (flag & 2) {
+        MPH_CK(cudaMemsetAsync(s->d_flag, 0, sizeof(int), s->stream), "clear flag");
+        return fail(MPH_ERR_CUDA, "staged 16-bit step: a wait for bulk-copied operands exceeded its time limit "
+                                  "(the step's results are incomplete)");
+    }
     if (flag) return fail(MPH_ERR_NONFINITE, "fixed-point step: a cell left the representable range "
                                                "(rho outside (1/16, 64) or |J|, |u| >= 4)");
     return MPH_OK;
@@ -735,6 +766,26 @@ int mph_create(const mph_desc* desc, mph_sim** out) {
                 e = cudaGetLastError();
                 if (e == cudaSuccess) e = cudaErrorInvalidConfiguration;
             }
+        }
+    }
+    // 16-bit storages: the pair step with bulk-copy staging of its pull
+    // operands (MPH_PAIR_KERNEL=bulk, stages MPH_BULK_STAGES 2..4, chunk
+    // cells MPH_BULK_CELLS) or the direct pair kernel (MPH_PAIR_KERNEL=direct).
+    const bool p16 = d.precision == MPH_PREC_F16S || d.precision == MPH_PREC_BF16S || d.precision == MPH_PREC_F16C;
+    if (e == cudaSuccess && p16) {
+        const char* kv = std::getenv("MPH_PAIR_KERNEL");
+        if (kv && std::strcmp(kv, "bulk") == 0) {
+            s->bulk_stages = 3;
+            if (const char* v = std::getenv("MPH_BULK_STAGES")) s->bulk_stages = std::atoi(v);
+            if (const char* v = std::getenv("MPH_BULK_CELLS")) s->bulk_cells = std::atoi(v);
+            if (s->bulk_stages < 2 || s->bulk_stages > 4 || s->bulk_cells < 2) {
+                free_all(s);
+                delete s;
+                return fail(MPH_ERR_ARG, "mph_create: MPH_BULK_STAGES must be 2..4 and MPH_BULK_CELLS >= 2");
+            }
+            e = cudaMalloc(&s->d_flag, sizeof(int));
+            if (e == cudaSuccess) e = cudaMemset(s->d_flag, 0, sizeof(int));
+            if (e == cudaSuccess) e = launch_bulk(s, 0, s->kp);
         }
     }
     // Domains of up to 2^22 cells (a step of at most a few tens of
