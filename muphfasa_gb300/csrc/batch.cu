@@ -76,12 +76,17 @@ size_t elem_of(int prec) {
 // chunk is 256 K cells), cand / 3 a persistent grid; the shifted 16-bit
 // policies take cells in pairs, so K = 1 is skipped for them, and the
 // fixed-point step holds at most two cells of int64 populations per thread,
-// so K = 4 is skipped for it.
+// so K = 4 is skipped for it.  Candidate 6 (16-bit storages only) is the
+// persistent kernel with bulk-copy staging over chunks of whole rows.
 constexpr int kCells[3] = {1, 2, 4};
-constexpr int kCands = 6;
+constexpr int kCands = 7;
+constexpr int kBulkCand = 6;
+constexpr int kBulkCells = 512;  // cells per row chunk of the staged kernel
+constexpr int kBulkStages = 3;
 
 bool shifted(int prec) { return prec == MPH_PREC_F16S || prec == MPH_PREC_BF16S || prec == MPH_PREC_F16C; }
 bool candidate_ok(int prec, int cand) {
+    if (cand == kBulkCand) return shifted(prec);
     if (shifted(prec)) return cand % 3 != 0;
     if (prec == MPH_PREC_F64X) return cand % 3 != 2;
     return true;
@@ -147,6 +152,11 @@ struct mph_batch {
     double* d_rout = nullptr;
     bool has_uprev = false;
     int k_idx = -1;  // candidate chosen by the autotuner
+    // 16-bit storages: row chunks of the bulk-copy staged kernel (candidate
+    // 6), its run slot length and whether it fits in shared memory
+    RowChunk* d_rchunks = nullptr;
+    int nrchunks = 0, bulk_lpad = 0;
+    bool bulk_ok = false;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // two steps from graph_in[i] back to it
@@ -182,6 +192,7 @@ void free_batch(mph_batch* b) {
     cudaFree(b->d_rout);
     cudaFree(b->d_walls);
     cudaFree(b->d_cls);
+    cudaFree(b->d_rchunks);
     cudaFree(b->d_px);
     cudaFree(b->d_kbb);
     cudaFree(b->d_flag);
@@ -249,7 +260,61 @@ int build_walls(mph_batch* b) {
     return MPH_OK;
 }
 
+cudaError_t launch_bulk(mph_batch* b, int mode) {
+    switch (b->prec) {
+        case MPH_PREC_F16S:
+            return launch_batch_bulk_f16s(mode, b->q, b->forced, kBulkStages, b->bulk_lpad, b->fa, b->fb, b->d_rchunks,
+                                          b->nrchunks, b->d_walls, b->nwalls, b->d_params, b->d_offs, b->d_flag,
+                                          b->stream);
+        case MPH_PREC_BF16S:
+            return launch_batch_bulk_bf16s(mode, b->q, b->forced, kBulkStages, b->bulk_lpad, b->fa, b->fb, b->d_rchunks,
+                                           b->nrchunks, b->d_walls, b->nwalls, b->d_params, b->d_offs, b->d_flag,
+                                           b->stream);
+        case MPH_PREC_F16C:
+            return launch_batch_bulk_f16c(mode, b->q, b->forced, kBulkStages, b->bulk_lpad, b->fa, b->fb, b->d_rchunks,
+                                          b->nrchunks, b->d_walls, b->nwalls, b->d_params, b->d_offs, b->d_flag,
+                                          b->stream);
+    }
+    return cudaErrorNotSupported;
+}
+
+// Row chunks of the staged kernel (about kBulkCells cells of whole rows per
+// chunk), the longest run slot, and the kernel's shared-memory setting.
+int build_row_chunks(mph_batch* b) {
+    std::vector<RowChunk> rc;
+    long long lpad = 0;
+    for (int d = 0; d < b->ndom; ++d) {
+        const mph_desc& ds = b->descs[d];
+        const int nx = ds.n[0], ny = ds.n[1], nz = ds.dim == 3 ? ds.n[2] : 1;
+        int rows = kBulkCells / nx;
+        if (rows < 1) rows = 1;
+        if (rows > ny) rows = ny;
+        lpad = std::max(lpad, ((long long)rows * nx + 14 + 7) & ~7LL);
+        for (int z = 0; z < nz; ++z)
+            for (int y = 0; y < ny; y += rows) rc.push_back(RowChunk{d, z, y, std::min(rows, ny - y)});
+    }
+    if (rc.size() > 0x7fffffffu || lpad > (1 << 20)) return MPH_OK;  // the staged kernel does not apply
+    b->bulk_lpad = (int)lpad;
+    MPH_CK(cudaMalloc(&b->d_rchunks, sizeof(RowChunk) * rc.size()), "batch row chunks");
+    MPH_CK(cudaMemcpy(b->d_rchunks, rc.data(), sizeof(RowChunk) * rc.size(), cudaMemcpyHostToDevice), "batch row chunks");
+    b->nrchunks = (int)rc.size();
+    if (!b->d_flag) {
+        MPH_CK(cudaMalloc(&b->d_flag, sizeof(int)), "batch flag");
+        MPH_CK(cudaMemset(b->d_flag, 0, sizeof(int)), "batch flag");
+    }
+    const cudaError_t e = launch_bulk(b, 0);
+    if (e == cudaErrorNotSupported) return MPH_OK;  // runs too long for shared memory
+    MPH_CK(e, "batch staged kernel setup");
+    b->bulk_ok = true;
+    return MPH_OK;
+}
+
 int step_once(mph_batch* b, int cand) {
+    if (cand == kBulkCand) {
+        MPH_CK(launch_bulk(b, 1), "batch staged step launch");
+        std::swap(b->fa, b->fb);
+        return MPH_OK;
+    }
     const int ki = cand % 3;
     MPH_CK(launch_batch(b->prec, b->q, b->forced, kCells[ki], cand >= 3, b->fa, b->fb, b->d_chunks[ki], b->nchunks[ki],
                         b->d_walls, b->nwalls, b->d_params, b->d_offs, b->d_px, b->d_kbb, b->d_flag, b->stream),
@@ -267,9 +332,9 @@ int autotune(mph_batch* b) {
     // MPH_BATCH_CANDIDATE=c (0..5) fixes the launch instead of timing.
     if (const char* env = std::getenv("MPH_BATCH_CANDIDATE")) {
         const int c = std::atoi(env);
-        if (c < 0 || c >= kCands || !candidate_ok(b->prec, c))
-            return fail(MPH_ERR_ARG, "MPH_BATCH_CANDIDATE must be 0..5 (1, 2, 4, 5 for 16-bit storage; "
-                                     "0, 1, 3, 4 for fixed point)");
+        if (c < 0 || c >= kCands || !candidate_ok(b->prec, c) || (c == kBulkCand && !b->bulk_ok))
+            return fail(MPH_ERR_ARG, "MPH_BATCH_CANDIDATE must be 0..6 (1, 2, 4, 5 and 6 for 16-bit storage; "
+                                     "0, 1, 3, 4 for fixed point; 0..5 otherwise)");
         b->k_idx = c;
         return ensure_chunks(b, c % 3);
     }
@@ -290,7 +355,7 @@ int autotune(mph_batch* b) {
     float best = 1e30f;
     int besti = shifted(b->prec) ? 1 : 0;
     for (int wi = 0; wi < kCands && e == cudaSuccess; ++wi) {
-        if (!candidate_ok(b->prec, wi)) continue;
+        if (!candidate_ok(b->prec, wi) || (wi == kBulkCand && !b->bulk_ok)) continue;
         int rc = ensure_chunks(b, wi % 3);
         if (rc) { cudaFree(save); return rc; }
         rc = step_once(b, wi);
@@ -307,7 +372,8 @@ int autotune(mph_batch* b) {
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->fa, save, bytes, cudaMemcpyDeviceToDevice, b->stream);
     // only the steps of the caller's advances report the range flag
-    if (e == cudaSuccess && b->d_flag) e = cudaMemsetAsync(b->d_flag, 0, sizeof(int) * b->ndom, b->stream);
+    if (e == cudaSuccess && b->d_flag)
+        e = cudaMemsetAsync(b->d_flag, 0, sizeof(int) * (b->prec == MPH_PREC_F64X ? b->ndom : 1), b->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     cudaFree(save);
     if (e != cudaSuccess) return cuda_fail(e, "autotune");
@@ -367,6 +433,15 @@ int ensure_graph(mph_batch* b) {
 // after an advance, kept in bad_h).
 int check_flag(mph_batch* b) {
     if (!b->d_flag) return MPH_OK;
+    if (b->prec != MPH_PREC_F64X) {  // the staged 16-bit kernel: 2 = a wait timed out
+        int f = 0;
+        MPH_CK(cudaMemcpyAsync(&f, b->d_flag, sizeof(int), cudaMemcpyDeviceToHost, b->stream), "read flag");
+        MPH_CK(cudaStreamSynchronize(b->stream), "read flag");
+        if (!f) return MPH_OK;
+        MPH_CK(cudaMemsetAsync(b->d_flag, 0, sizeof(int), b->stream), "clear flag");
+        return fail(MPH_ERR_CUDA, "staged 16-bit batch step: a wait for bulk-copied operands exceeded its time limit "
+                                  "(the step's results are incomplete)");
+    }
     std::vector<int> flag(b->ndom, 0);
     MPH_CK(cudaMemcpyAsync(flag.data(), b->d_flag, sizeof(int) * b->ndom, cudaMemcpyDeviceToHost, b->stream),
            "read flag");
@@ -496,6 +571,7 @@ int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out) {
         return rc;
     }
     int rc = build_walls(b);
+    if (!rc && shifted(b->prec)) rc = build_row_chunks(b);
     if (rc) {
         free_batch(b);
         delete b;
@@ -731,8 +807,9 @@ int mph_batch_range_flags(const mph_batch* b, int* flags) {
 int mph_batch_info(const mph_batch* b, long long* total_cells, int* cells_per_thread, int* nchunks, int* persistent) {
     if (!b) return fail(MPH_ERR_ARG, "mph_batch_info: NULL batch");
     if (total_cells) *total_cells = b->total_cells;
-    if (cells_per_thread) *cells_per_thread = b->k_idx >= 0 ? kCells[b->k_idx % 3] : 0;
-    if (nchunks) *nchunks = b->k_idx >= 0 ? b->nchunks[b->k_idx % 3] : 0;
+    const bool staged = b->k_idx == kBulkCand;
+    if (cells_per_thread) *cells_per_thread = b->k_idx >= 0 ? (staged ? 2 : kCells[b->k_idx % 3]) : 0;
+    if (nchunks) *nchunks = b->k_idx >= 0 ? (staged ? b->nrchunks : b->nchunks[b->k_idx % 3]) : 0;
     if (persistent) *persistent = b->k_idx >= 3 ? 1 : 0;
     return MPH_OK;
 }

@@ -29,6 +29,12 @@ struct Chunk {
     int yz;
 };
 
+// A chunk of whole rows of one domain, rows [yb, yb + r) of plane z (the
+// bulk-copy staged kernel of the 16-bit storages, bulk_step.cuh).
+struct RowChunk {
+    int dom, z, yb, r;
+};
+
 namespace {
 
 // Coordinates of cell c0 + l of the chunk's domain.  v / n by a float
@@ -257,6 +263,19 @@ MPH_DECL_BATCH(launch_batch_f16s)
 MPH_DECL_BATCH(launch_batch_bf16s)
 MPH_DECL_BATCH(launch_batch_f16c)
 #undef MPH_DECL_BATCH
+// The 16-bit storages' batch step with bulk-copy staging of the pull
+// operands (bulk_step.cuh): `stages` 2 or 3, lpad = elements of one staged
+// run slot; mode 0 prepares the kernel (once, before any launch or capture),
+// mode 1 launches the chunk kernel and the wall cells.  cudaErrorNotSupported
+// when the shared memory of one block would exceed its limit.
+#define MPH_DECL_BATCH_BULK(NAME)                                                                              \
+    cudaError_t NAME(int mode, int q, bool forced, int stages, int lpad, const void* fin, void* fout,         \
+                     const RowChunk* chunks, int nchunks, const int2* walls, int nwalls, const KParams* dp,     \
+                     const long long* offs, int* flag, cudaStream_t s);
+MPH_DECL_BATCH_BULK(launch_batch_bulk_f16s)
+MPH_DECL_BATCH_BULK(launch_batch_bulk_bf16s)
+MPH_DECL_BATCH_BULK(launch_batch_bulk_f16c)
+#undef MPH_DECL_BATCH_BULK
 // The fixed-point step (k_f64x_batch.cu): per-domain fixed-point constants
 // dpx, bounce-back tables kbb (27 x 27 per domain) and the range flag.
 cudaError_t launch_batch_f64x(int q, bool forced, int K, bool persistent, const void* fin, void* fout,

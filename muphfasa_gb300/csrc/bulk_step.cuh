@@ -30,6 +30,7 @@
 // returns, so the context stays usable and the host reports the error.
 #pragma once
 
+#include "batch_kernel.cuh"
 #include "lbm_kernels.cuh"
 
 namespace mph {
@@ -328,6 +329,195 @@ cudaError_t launch_step_bulk_t(int mode, int q, bool forced, const void* fin, vo
 #undef MPH_BULK_Q
 #undef MPH_BULK_S
     return cudaErrorNotSupported;
+}
+
+// ---- batches ------------------------------------------------------------
+// The same staging over a batch of domains of any sizes (the batch's chunk
+// kernel: every cell pulls through the wrapped neighbour offsets, and the
+// cells next to non-periodic faces or obstacles are recomputed afterwards by
+// k_batch_walls from the wall list, so pairs whose two cells are both on a
+// face are skipped here).  Pairs are consecutive cells of the chunk (they may
+// straddle two rows when nx is odd); every value is read as 16 bits, from the
+// staged runs or, outside them, from global memory.  Domains start on
+// 128-element boundaries and their runs are clipped to the domain's
+// allocation, rounded up to 8 elements.
+template <int Q, class St, bool FORCED, int S>
+__global__ void __launch_bounds__(bulk::kThreads, 3) k_batch_pair_bulk(const typename St::T* __restrict__ fin_base,
+                                                                    typename St::T* __restrict__ fout_base,
+                                                                    const RowChunk* __restrict__ chunks, int nchunks,
+                                                                    const KParams* __restrict__ dp,
+                                                                    const long long* __restrict__ offs, int lpad,
+                                                                    int* __restrict__ flag) {
+    using L = Lat<Q>;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem);
+    bulk::Run* runs = reinterpret_cast<bulk::Run*>(smem + 64);
+    unsigned short* data = reinterpret_cast<unsigned short*>(smem + bulk::kHeader);
+    const int tid = threadIdx.x;
+    const int G = gridDim.x;
+    if (tid == 0) {
+        for (int s = 0; s < S; ++s) bulk::bar_init(&bar[s]);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+
+    auto issue = [&](int k, int s) {
+        const RowChunk ch = chunks[k];
+        const KParams& p = dp[ch.dom];
+        const typename St::T* fin = fin_base + offs[ch.dom];
+        const unsigned N = (unsigned)p.ncell;
+        const unsigned total = ((unsigned)Q * N + 7u) & ~7u;
+        bulk::Run* rs = runs + s * Q;
+        unsigned bytes = 0;
+#pragma unroll 1
+        for (int n = 0; n < Q; ++n) {
+            int zs = ch.z - L::cz(n);
+            bool ok = true;
+            if (zs < 0 || zs >= p.nz) {
+                if (p.periodic[2]) zs = zs < 0 ? zs + p.nz : zs - p.nz;
+                else ok = false;
+            }
+            const int ya = max(ch.yb - L::cy(n), 0), ye = min(ch.yb + ch.r - L::cy(n), p.ny);
+            bulk::Run run{0u, 0u};
+            if (ok && ye > ya) {
+                const unsigned a = (unsigned)n * N + (unsigned)((zs * p.ny + ya) * p.nx);
+                const unsigned b = (unsigned)n * N + (unsigned)((zs * p.ny + ye) * p.nx);
+                unsigned e = (b + 7u) & ~7u;
+                if (e > total) e = total;
+                run.base = a & ~7u;
+                run.len = e > run.base ? e - run.base : 0u;
+            }
+            rs[n] = run;
+            bytes += 2u * run.len;
+        }
+        bulk::bar_expect(&bar[s], bytes);
+#pragma unroll 1
+        for (int n = 0; n < Q; ++n)
+            if (rs[n].len) bulk::copy_g2s(data + (size_t)(s * Q + n) * lpad, fin + rs[n].base, 2u * rs[n].len, &bar[s]);
+    };
+
+    if (tid == 0)
+        for (int i = 0; i < S - 1; ++i) {
+            const int k = blockIdx.x + i * G;
+            if (k < nchunks) issue(k, i);
+        }
+    int it = 0;
+    bool timed_out = false;
+    for (int k = blockIdx.x; k < nchunks; k += G, ++it) {
+        const int s = it % S;
+        if (tid == 0) {
+            const int kn = k + (S - 1) * G;
+            if (kn < nchunks) issue(kn, (it + S - 1) % S);
+        }
+        const bool got = bulk::bar_wait(&bar[s], (unsigned)(it / S) & 1u);
+        if (__syncthreads_or(!got)) {
+            timed_out = true;
+            break;
+        }
+        const RowChunk ch = chunks[k];
+        const KParams& p = dp[ch.dom];
+        const long long off = offs[ch.dom];
+        const typename St::T* fin = fin_base + off;
+        typename St::T* fout = fout_base + off;
+        const unsigned N = (unsigned)p.ncell;
+        const bulk::Run* rs = runs + s * Q;
+        const unsigned short* st = data + (size_t)s * Q * lpad;
+        const int ncells = ch.r * p.nx;
+        const unsigned c0 = (unsigned)((ch.z * p.ny + ch.yb) * p.nx);
+        for (int j = tid; 2 * j < ncells; j += bulk::kThreads) {
+            const int la = 2 * j;
+            const bool okb = la + 1 < ncells;
+            const int ra = la / p.nx, xa = la - ra * p.nx;
+            const int lb = okb ? la + 1 : la;
+            const int rb = lb / p.nx, xb = lb - rb * p.nx;
+            const Nbr oa = neighbours<L::D>(p, xa, ch.yb + ra, ch.z);
+            const Nbr ob = neighbours<L::D>(p, xb, ch.yb + rb, ch.z);
+            if (oa.wall && ob.wall) continue;  // both recomputed by the wall-list kernel
+            const unsigned ca = c0 + (unsigned)la, cb = c0 + (unsigned)lb;
+            float2 g[Q];
+#pragma unroll
+            for (int n = 0; n < Q; ++n) {
+                const bulk::Run rn = rs[n];
+                const unsigned short* sn = st + (size_t)n * lpad;
+                const unsigned ea = (unsigned)n * N + (unsigned)((int)ca + upstream<Q>(oa, n));
+                const unsigned eb = (unsigned)n * N + (unsigned)((int)cb + upstream<Q>(ob, n));
+                const unsigned da = ea - rn.base, db = eb - rn.base;
+                const float va = da < rn.len ? St::dec1(sn[da]) : St::ldr1(fin, ea);
+                const float vb = db < rn.len ? St::dec1(sn[db]) : St::ldr1(fin, eb);
+                g[n] = make_float2(va, vb);
+            }
+            collide_shift<Q, A2, FORCED>(p, g);
+#pragma unroll
+            for (int n = 0; n < Q; ++n) {
+                const unsigned e = (unsigned)n * N + ca;
+                if (okb && (e & 1u) == 0) {
+                    St::str2(fout, e, g[n]);
+                } else {
+                    St::str1(fout, e, g[n].x);
+                    if (okb) St::str1(fout, e + 1, g[n].y);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (timed_out) {
+        if (tid == 0) {
+            atomicOr(flag, 2);
+            for (int i = 0; i < S; ++i) {
+                const int j = it + i;
+                if (blockIdx.x + j * G < nchunks) bulk::bar_wait(&bar[j % S], (unsigned)(j / S) & 1u);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// mode 0: raise the dynamic shared-memory limit (once per batch, before any
+// launch or capture); mode 1: one batch step (the staged chunk kernel, then
+// the wall cells).
+template <class St>
+cudaError_t launch_batch_bulk_t(int mode, int q, bool forced, int stages, int lpad, const void* fin, void* fout,
+                                const RowChunk* chunks, int nchunks, const int2* walls, int nwalls,
+                                const KParams* dp, const long long* offs, int* flag, cudaStream_t s) {
+    const size_t smem = bulk_smem_bytes(q, stages, lpad);
+    if (smem > (size_t)kBulkMaxSmem) return cudaErrorNotSupported;
+    auto in = static_cast<const typename St::T*>(fin);
+    auto out = static_cast<typename St::T*>(fout);
+    cudaError_t err = cudaErrorNotSupported;
+    auto go = [&](auto kern) {
+        if (mode == 0) {
+            err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kBulkMaxSmem);
+            return;
+        }
+        int grid = bulk_grid(kern, smem);
+        if (grid <= 0) {
+            err = cudaGetLastError();
+            if (err == cudaSuccess) err = cudaErrorInvalidConfiguration;
+            return;
+        }
+        if (grid > nchunks) grid = nchunks;
+        kern<<<grid, bulk::kThreads, smem, s>>>(in, out, chunks, nchunks, dp, offs, lpad, flag);
+        err = cudaGetLastError();
+    };
+    return batch_with_q(q, [&](auto qc) {
+        constexpr int Q = decltype(qc)::value;
+        if (stages == 2) {
+            if (forced) go(k_batch_pair_bulk<Q, St, true, 2>);
+            else go(k_batch_pair_bulk<Q, St, false, 2>);
+        } else if (stages == 3) {
+            if (forced) go(k_batch_pair_bulk<Q, St, true, 3>);
+            else go(k_batch_pair_bulk<Q, St, false, 3>);
+        } else {
+            return cudaErrorNotSupported;
+        }
+        if (err != cudaSuccess || mode == 0) return err;
+        if (nwalls > 0) {
+            const int nb = (nwalls + 255) / 256;
+            if (forced) k_batch_walls<Q, St, kFast, true><<<nb, 256, 0, s>>>(in, out, walls, nwalls, dp, offs);
+            else k_batch_walls<Q, St, kFast, false><<<nb, 256, 0, s>>>(in, out, walls, nwalls, dp, offs);
+        }
+        return cudaGetLastError();
+    });
 }
 
 }  // namespace mph

@@ -18,4 +18,10 @@ cudaError_t launch_batch_f16c(int q, bool forced, int K, bool persistent, const 
                        const int2* walls, int nwalls, const KParams* dp, const long long* offs, cudaStream_t s) {
     return launch_batch_t<StF16C, kFast>(q, forced, K, persistent, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
 }
+cudaError_t launch_batch_bulk_f16c(int mode, int q, bool forced, int stages, int lpad, const void* fin, void* fout,
+                                   const RowChunk* chunks, int nchunks, const int2* walls, int nwalls,
+                                   const KParams* dp, const long long* offs, int* flag, cudaStream_t s) {
+    return launch_batch_bulk_t<StF16C>(mode, q, forced, stages, lpad, fin, fout, chunks, nchunks, walls, nwalls, dp, offs,
+                                     flag, s);
+}
 }  // namespace mph

@@ -210,3 +210,70 @@ def test_f64x_range_flags_name_the_bad_domain(mph):
     assert not batch.range_flags().any()
     batch.advance(2)
     assert not batch.range_flags().any()
+
+
+def _advance_with_candidate(batch, cand, nsteps):
+    """Advance with the autotuner's choice fixed to candidate `cand` (the
+    choice is made at the first advance and kept)."""
+    import os
+    old = os.environ.get("MPH_BATCH_CANDIDATE")
+    os.environ["MPH_BATCH_CANDIDATE"] = str(cand)
+    try:
+        batch.advance(nsteps)
+    finally:
+        if old is None:
+            os.environ.pop("MPH_BATCH_CANDIDATE", None)
+        else:
+            os.environ["MPH_BATCH_CANDIDATE"] = old
+
+
+@pytest.mark.parametrize("precision", ["f16s", "bf16s", "f16c"])
+def test_staged_batch_kernel_equals_single_handles(precision, mph):
+    """Candidate 6, the bulk-copy staged kernel over chunks of whole rows:
+    odd and even sides (pairs straddling rows), sides longer than a chunk's
+    512 cells, obstacles, and a forced periodic domain, all bit for bit equal
+    to single handles."""
+    descs = [_cavity(mph, (17, 17), 1.2, 0.1, precision), _cavity(mph, (64, 48), 1.7, 0.05, precision),
+             _cavity(mph, (600, 20), 0.9, 0.1, precision), _cavity(mph, (33, 65), 1.9, 0.08, precision),
+             _cavity(mph, (130, 7), 1.4, 0.06, precision)]
+    batch = mph.Batch(descs)
+    singles = [mph.Simulation(d) for d in descs]
+    rng = np.random.default_rng(9)
+    mask = np.zeros((65, 33), np.uint8)
+    mask[20:30, 10:16] = 1
+    batch.set_obstacles(3, mask)
+    singles[3].set_obstacles(mask)
+    for i, d in enumerate(descs):
+        N = batch.ncells[i]
+        rho, u = 1 + 0.01 * rng.standard_normal(N), 0.02 * rng.standard_normal(2 * N)
+        batch.initialize(i, rho, u)
+        singles[i].initialize(rho, u)
+    _advance_with_candidate(batch, 6, 37)
+    assert batch.info()[1] == 2 and batch.info()[3]
+    for s in singles:
+        s.advance(37)
+    for i, s in enumerate(singles):
+        assert np.array_equal(batch.f(i), s.f()), i
+
+
+@pytest.mark.parametrize("precision", ["f16s", "f16c"])
+def test_staged_batch_kernel_3d_forced_mixed_boundaries(precision, mph):
+    faces_a = ["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic", "Periodic"]
+    faces_b = ["Inflow", "PressureOutlet", "NoSlip", "MovingWall", "Periodic", "Periodic"]
+    Ub = [[0.0] * 3 for _ in range(6)]
+    Ub[0][0] = 0.02
+    Ub[3][0] = 0.05
+    descs = [mph.make_desc("D3Q19", (20, 12, 9), 1.3, faces=faces_a, force=(1e-5, 0, 0), precision=precision),
+             mph.make_desc("D3Q19", (7, 16, 11), 1.6, faces=faces_b, face_U=Ub, face_rho=[1, 1.01, 1, 1, 1, 1],
+                           force=(2e-5, 1e-6, 0), precision=precision),
+             mph.make_desc("D3Q19", (40, 8, 6), 1.1, faces=faces_b, face_U=Ub, face_rho=[1, 1.01, 1, 1, 1, 1],
+                           force=(1e-5, 0, 2e-6), precision=precision)]
+    batch = mph.Batch(descs)
+    singles = [mph.Simulation(d) for d in descs]
+    for i in range(len(descs)):
+        batch.initialize(i)
+        singles[i].initialize()
+    _advance_with_candidate(batch, 6, 31)
+    for i, s in enumerate(singles):
+        s.advance(31)
+        assert np.array_equal(batch.f(i), s.f())
