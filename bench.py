@@ -299,6 +299,45 @@ def tgv2d_fields(N, u0):
     return rho.ravel(), np.concatenate([ux.ravel(), uy.ravel()])
 
 
+def run_surrogate(args):
+    """Training throughput of the warm-start U-Net: Adam iterations (forward,
+    masked loss, backward, gradient clipping, update) on seeded synthetic
+    fields of the warm-start shape (batch 8, ws_n^2 cells, 8 input and 3
+    output channels), timed end to end including the host-side input upload
+    and loss download of every iteration."""
+    import muphfasa_gb300 as m
+    from muphfasa_gb300 import surrogate as sg
+    from muphfasa_gb300.surrogate import Trainer, UNet
+    m.set_device(0)
+    sync = lambda: m.check(sg._lib().mph_nn_sync(None))
+    n, B = args.ws_n, 8
+    rng = np.random.default_rng(5)
+    X = rng.standard_normal((B, n, n, 8)).astype(np.float32)
+    Y = rng.standard_normal((B, n, n, 3)).astype(np.float32)
+    M = (rng.random((B, n, n)) < 0.9).astype(np.float32)
+    net = UNet(seed=1)
+    tr = Trainer(net, B, n, n)
+    for _ in range(args.warmup):
+        tr.train_step(X, Y, M, 1e-4)
+    sync()
+    sm = ClockSampler(0)
+    with sm:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            loss = tr.train_step(X, Y, M, 1e-4)
+        sync()
+        dt = time.perf_counter() - t0
+    line = {"metric": "surrogate training iterations per second", "value": round(args.steps / dt, 2),
+            "unit": "iterations/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * dt / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 operands / f32 accumulate", "data": "synthetic",
+            "config": {"workload": f"unet_train_{n}^2_batch{B}", "params": net.n_params(),
+                       "gemm": "tcgen05 BF16 (mma.sync below 128 rows)"},
+            "loss": round(float(loss), 6), "clocks": sm.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_tgv2d(args):
     """The CPU-runnable configuration: 2-D Taylor-Green vortex, D2Q9, periodic
     256^2, tau 0.8, u0 0.05, 5000 steps.  MLUPS per precision with the
@@ -574,7 +613,8 @@ def main():
     ap.add_argument("--secondary-steps", type=int, default=40,
                     help="steps of the 512-cavity batch record added to the channel line (0: skip)")
     ap.add_argument("--domains", type=int, default=512, help="domains of the batch512 workload")
-    ap.add_argument("--workload", default="channel", choices=["channel", "batch512", "tgv3d", "warmstart", "tgv2d", "ceiling"],
+    ap.add_argument("--workload", default="channel", choices=["channel", "batch512", "tgv3d", "warmstart", "tgv2d", "ceiling",
+                                                  "surrogate"],
                     help="channel: the D3Q19 channel (headline); batch512: 512 uneven D2Q9 cavities; "
                          "tgv3d: the D3Q27 precision study (use --n 384)")
     ap.add_argument("--tgv-steps", type=int, default=10000, help="tgv3d: total steps")
@@ -602,6 +642,8 @@ def main():
         return run_ceiling(args)
     if args.workload == "warmstart":
         return run_warmstart(args)
+    if args.workload == "surrogate":
+        return run_surrogate(args)
     if args.workload == "batch512":
         return run_batch(args)
 

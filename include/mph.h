@@ -389,6 +389,12 @@ int mph_nn_sumsq(const float* x, long long n, float* part, int nblocks, void* st
 /* kind 0 float -> BF16, 1 BF16 -> float. */
 int mph_nn_cast(int kind, const void* x, long long n, void* y, void* stream);
 int mph_nn_fill(float* x, long long n, float v, void* stream);
+/* y[c][r] = x[r][c] for a rows x cols BF16 matrix (the K-contiguous layout
+ * of a weight gradient's operands). */
+int mph_nn_transpose(const void* x, long long rows, int cols, void* y, void* stream);
+/* w2[ci][t cout + co] = wt[co][(8 - t) cin + ci] (BF16): the weights of a 3 x 3
+ * convolution's data gradient as a convolution of dY with mirrored taps. */
+int mph_nn_wflip(const void* wt, int cout, int cin, void* w2, void* stream);
 
 #ifdef __cplusplus
 }

@@ -717,6 +717,45 @@ __global__ void k_cast(const T* __restrict__ x, long long n, U* __restrict__ y) 
         y[i] = (U)(float)x[i];
 }
 
+// Y[c][r] = X[r][c] for a rows x cols BF16 matrix, through 32 x 32 tiles in
+// shared memory (coalesced reads along c and writes along r).  Puts the
+// pixel-major operands of a weight gradient (dY [P][Cout], Xcol [P][9 Cin])
+// into the K-contiguous layout of the tensor-core GEMM's asynchronous copies.
+__global__ void __launch_bounds__(256) k_transpose_bf16(const unsigned short* __restrict__ X, long long rows, int cols,
+                                                        unsigned short* __restrict__ Y) {
+    __shared__ unsigned short t[32][33];
+    const long long r0 = (long long)blockIdx.x * 32;
+    const int c0 = blockIdx.y * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+#pragma unroll
+    for (int i = 0; i < 32; i += 8) {
+        const long long r = r0 + ty + i;
+        const int c = c0 + tx;
+        if (r < rows && c < cols) t[ty + i][tx] = X[r * cols + c];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 32; i += 8) {
+        const int c = c0 + ty + i;
+        const long long r = r0 + tx;
+        if (r < rows && c < cols) Y[(long long)c * rows + r] = t[tx][ty + i];
+    }
+}
+
+// W2[ci][t Cout + co] = Wt[co][(8 - t) Cin + ci]: the weights of the data
+// gradient of a 3 x 3 convolution written as a convolution of dY with the
+// taps mirrored (t' = 8 - t) and the channel roles exchanged.
+__global__ void k_wflip(const unsigned short* __restrict__ Wt, int cout, int cin, unsigned short* __restrict__ W2) {
+    const long long n = 9LL * cout * cin;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int co = (int)(i % cout);
+        const long long r = i / cout;
+        const int t = (int)(r % 9);
+        const int ci = (int)(r / 9);
+        W2[i] = Wt[(long long)co * 9 * cin + (long long)(8 - t) * cin + ci];
+    }
+}
+
 // Block sums of x^2 into part[blockIdx.x].
 __global__ void k_sumsq(const float* __restrict__ x, long long n, float* __restrict__ part) {
     float s = 0.f;
@@ -813,7 +852,10 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     auto a = static_cast<const bf16*>(A);
     auto b = static_cast<const bf16*>(B);
-    const bool tc = g_gemm_mode >= 2 || (g_gemm_mode == 0 && M >= TC_BM && N >= 16);
+    // tcgen05 tiles are 128 rows: below that the mma.sync kernel, unless K
+    // is long (a weight gradient, K = pixels), where the idle rows cost less
+    // than the slower kernel.
+    const bool tc = g_gemm_mode >= 2 || (g_gemm_mode == 0 && (M >= TC_BM || K >= 16 * TC_BK) && N >= 16);
     const int tm = tc ? TC_BM : BM, tn = tc ? TC_BN : BN;
     const long long gx = (N + tn - 1) / tn, gy = (M + tm - 1) / tm;
     if (gy > 65535) return mph::fail(MPH_ERR_ARG, "mph_nn_gemm: M too large for one launch");
@@ -961,6 +1003,23 @@ int mph_nn_cast(int kind, const void* x, long long n, void* y, void* stream) {
     if (kind == 0) k_cast<float, bf16><<<grid_for(n), 256, 0, s>>>(static_cast<const float*>(x), n, static_cast<bf16*>(y));
     else k_cast<bf16, float><<<grid_for(n), 256, 0, s>>>(static_cast<const bf16*>(x), n, static_cast<float*>(y));
     return ck("cast");
+}
+
+int mph_nn_transpose(const void* x, long long rows, int cols, void* y, void* stream) {
+    if (!x || !y || rows <= 0 || cols <= 0 || (rows + 31) / 32 > 0x7fffffffLL || (cols + 31) / 32 > 65535)
+        return mph::fail(MPH_ERR_ARG, "mph_nn_transpose: bad argument");
+    const dim3 grid((unsigned)((rows + 31) / 32), (unsigned)((cols + 31) / 32));
+    k_transpose_bf16<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const unsigned short*>(x), rows,
+                                                                          cols, static_cast<unsigned short*>(y));
+    return ck("transpose");
+}
+
+int mph_nn_wflip(const void* wt, int cout, int cin, void* w2, void* stream) {
+    if (!wt || !w2 || cout <= 0 || cin <= 0) return mph::fail(MPH_ERR_ARG, "mph_nn_wflip: bad argument");
+    const long long n = 9LL * cout * cin;
+    k_wflip<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const unsigned short*>(wt), cout, cin,
+                                                                        static_cast<unsigned short*>(w2));
+    return ck("wflip");
 }
 
 int mph_nn_fill(float* x, long long n, float v, void* stream) {

@@ -97,6 +97,8 @@ def _lib():
         L.mph_nn_sumsq.argtypes = [fp, LL, fp, I, P]
         L.mph_nn_cast.argtypes = [I, P, LL, P, P]
         L.mph_nn_fill.argtypes = [fp, LL, F, P]
+        L.mph_nn_transpose.argtypes = [P, LL, I, P, P]
+        L.mph_nn_wflip.argtypes = [P, I, I, P, P]
         L.mph_nn_sync.argtypes = [P]
         L.mph_nn_gemm_mode.argtypes = [I]
         L.mph_nn_status.argtypes = [C.POINTER(C.c_int), I]
@@ -105,7 +107,17 @@ def _lib():
 
 
 class Conv:
-    """3 x 3 (pad 1) or 1 x 1 convolution with bias and optional leaky ReLU."""
+    """3 x 3 (pad 1) or 1 x 1 convolution with bias and optional leaky ReLU.
+
+    Every GEMM reads both operands K-contiguous (the tensor-core kernel's
+    16-byte asynchronous copies):
+      forward          Y [P][Cout]    = Xcol [P][9 Cin] . Wt^T
+      weight gradient  gW [Cout][9 Cin] = dY^T [Cout][P] . Xcol^T [9 Cin][P]
+                       (both operands transposed once per step)
+      data gradient    dX [P][Cin]    = dYcol [P][9 Cout] . W2^T, with dYcol the
+                       im2col of dY and W2 the weights with mirrored taps, so the
+                       gradient is a 3 x 3 convolution of dY (no 9 x expanded
+                       FP32 column gradient and no col2im)."""
 
     def __init__(self, cin, cout, rng, k3=True, act=True):
         self.cin, self.cout, self.k3, self.act = cin, cout, k3, act
@@ -118,6 +130,7 @@ class Conv:
         self.wt.upload(w)
         self.b.upload(np.zeros(cout, np.float32))
         self.wt_bf = _bf(self.n)
+        self.w2 = _bf(self.n) if k3 else None
         self.gw, self.gb = _f32(self.n), _f32(cout)
         self.mw, self.vw, self.mb, self.vb = _f32(self.n), _f32(self.n), _f32(cout), _f32(cout)
         L = _lib()
@@ -136,9 +149,10 @@ class Conv:
         self.y = _f32(P * self.cout)
         self.out = _bf(P * self.cout)
         self.dpre, self.dpre_bf = _f32(P * self.cout), _bf(P * self.cout)
+        self.dpre_t, self.xcol_t = _bf(P * self.cout), _bf(P * self.K)
         self.dx = _f32(P * self.cin)
         if self.k3:
-            self.xcol, self.dxcol = _bf(P * self.K), _f32(P * self.K)
+            self.xcol, self.dycol = _bf(P * self.K), _bf(P * 9 * self.cout)
 
     def forward(self, x: Dev, Bn, H, W, out_f32: Dev | None = None):
         L, P = _lib(), Bn * H * W
@@ -164,14 +178,17 @@ class Conv:
         check(L.mph_nn_colsum(self.dpre.ptr, P, self.cout, self.gb.ptr, None))
         check(L.mph_nn_cast(0, self.dpre.ptr, P * self.cout, self.dpre_bf.ptr, None))
         B = self.xcol if self.k3 else self.x
-        check(L.mph_nn_gemm(self.cout, self.K, P, self.dpre_bf.ptr, self.cout, 1, B.ptr, self.K, 1, self.gw.ptr,
+        check(L.mph_nn_transpose(self.dpre_bf.ptr, P, self.cout, self.dpre_t.ptr, None))
+        check(L.mph_nn_transpose(B.ptr, P, self.K, self.xcol_t.ptr, None))
+        check(L.mph_nn_gemm(self.cout, self.K, P, self.dpre_t.ptr, P, 0, self.xcol_t.ptr, P, 0, self.gw.ptr,
                             self.K, 0, None))
         if not need_dx:
             return None
         if self.k3:
-            check(L.mph_nn_gemm(P, self.K, self.cout, self.dpre_bf.ptr, self.cout, 0, self.wt_bf.ptr, self.K, 1,
-                                self.dxcol.ptr, self.K, 0, None))
-            check(L.mph_nn_col2im3(self.dxcol.ptr, Bn, H, W, self.cin, self.dx.ptr, None))
+            check(L.mph_nn_im2col3(self.dpre_bf.ptr, Bn, H, W, self.cout, self.dycol.ptr, None))
+            check(L.mph_nn_wflip(self.wt_bf.ptr, self.cout, self.cin, self.w2.ptr, None))
+            check(L.mph_nn_gemm(P, self.cin, 9 * self.cout, self.dycol.ptr, 9 * self.cout, 0, self.w2.ptr,
+                                9 * self.cout, 0, self.dx.ptr, self.cin, 0, None))
         else:
             check(L.mph_nn_gemm(P, self.K, self.cout, self.dpre_bf.ptr, self.cout, 0, self.wt_bf.ptr, self.K, 1,
                                 self.dx.ptr, self.K, 0, None))
@@ -185,12 +202,13 @@ class Conv:
                             gscale, None))
         self.refresh()
 
-    def grad_sumsq(self, part: Dev, nblk: int) -> float:
+    def grad_sumsq(self, part: Dev, nblk: int, off: int = 0):
+        """Block sums of the squared weight and bias gradients into
+        part[off : off + 2 nblk] (no host synchronisation)."""
         L = _lib()
-        check(L.mph_nn_sumsq(self.gw.ptr, self.n, part.ptr, nblk, None))
-        s = float(part.download(nblk).astype(np.float64).sum())
-        check(L.mph_nn_sumsq(self.gb.ptr, self.cout, part.ptr, nblk, None))
-        return s + float(part.download(nblk).astype(np.float64).sum())
+        base = part.ptr.value + 4 * off
+        check(L.mph_nn_sumsq(self.gw.ptr, self.n, C.c_void_p(base), nblk, None))
+        check(L.mph_nn_sumsq(self.gb.ptr, self.cout, C.c_void_p(base + 4 * nblk), nblk, None))
 
     def get(self):
         return self.wt.download(self.n).reshape(self.cout, self.K), self.b.download(self.cout)
@@ -301,9 +319,13 @@ class UNet:
         l["e1a"].backward(d, need_dx=False)
 
     def grad_norm(self) -> float:
+        """Global L2 norm of all gradients, with one download."""
+        nblk, nl = 64, len(self.layers)
         if not hasattr(self, "_part"):
-            self._part = _f32(64)
-        return float(np.sqrt(sum(l.grad_sumsq(self._part, 64) for l in self.layers.values())))
+            self._part = _f32(2 * nblk * nl)
+        for i, layer in enumerate(self.layers.values()):
+            layer.grad_sumsq(self._part, nblk, 2 * nblk * i)
+        return float(np.sqrt(self._part.download(2 * nblk * nl).astype(np.float64).sum()))
 
     def step(self, lr, wd=0.0, clip=None):
         """Adam step; with clip, gradients are scaled so their global L2 norm

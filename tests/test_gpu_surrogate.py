@@ -78,6 +78,45 @@ def test_tcgen05_gemm_matches_mma_sync_and_numpy(ta, tb, shape, S):
         assert np.all(np.abs(out[mode] - out[1]) <= 2e-5 * scale + 2e-6), mode
 
 
+def _download_bf16(S, dev, n):
+    f = S._f32(n)
+    S.check(S._lib().mph_nn_cast(1, dev.ptr, n, f.ptr, None))
+    return f.download(n)
+
+
+@pytest.mark.parametrize("rows,cols", [(1, 1), (37, 5), (4096, 288), (1000, 33)])
+def test_transpose_bf16(rows, cols, S):
+    rng = np.random.default_rng(rows + cols)
+    x = NO.to_bf16(rng.standard_normal((rows, cols)).astype(np.float32))
+    dx, dy = _bf16_dev(S, x), S._bf(x.size)
+    S.check(S._lib().mph_nn_transpose(dx.ptr, rows, cols, dy.ptr, None))
+    assert np.array_equal(_download_bf16(S, dy, x.size).reshape(cols, rows), x.T)
+
+
+@pytest.mark.parametrize("cin,cout", [(5, 3), (32, 64), (96, 32)])
+def test_data_gradient_as_mirrored_convolution(cin, cout, S):
+    """dX of a 3 x 3 convolution computed as the convolution of dY with the
+    mirrored, channel-exchanged weights (mph_nn_wflip + im2col of dY + one
+    GEMM) equals col2im of the column gradient dY . Wt within FP32 rounding."""
+    rng = np.random.default_rng(cin * cout)
+    Bn, H, W = 2, 8, 16
+    P = Bn * H * W
+    wt = NO.to_bf16(rng.standard_normal((cout, 9 * cin)).astype(np.float32))
+    dy = NO.to_bf16(rng.standard_normal((P, cout)).astype(np.float32))
+    L = S._lib()
+    dwt, ddy = _bf16_dev(S, wt), _bf16_dev(S, dy)
+    w2, dycol, dx = S._bf(wt.size), S._bf(P * 9 * cout), S._f32(P * cin)
+    S.check(L.mph_nn_wflip(dwt.ptr, cout, cin, w2.ptr, None))
+    w2h = _download_bf16(S, w2, wt.size).reshape(cin, 9, cout)
+    assert np.array_equal(w2h, wt.reshape(cout, 9, cin)[:, ::-1, :].transpose(2, 1, 0))
+    S.check(L.mph_nn_im2col3(ddy.ptr, Bn, H, W, cout, dycol.ptr, None))
+    S.check(L.mph_nn_gemm(P, cin, 9 * cout, dycol.ptr, 9 * cout, 0, w2.ptr, 9 * cout, 0, dx.ptr, cin, 0, None))
+    got = dx.download(P * cin).reshape(Bn, H, W, cin)
+    ref = NO.Net.col2im(dy.astype(np.float64) @ wt.astype(np.float64), (Bn, H, W, cin))
+    scale = NO.Net.col2im(np.abs(dy).astype(np.float64) @ np.abs(wt).astype(np.float64), (Bn, H, W, cin))
+    assert np.all(np.abs(got - ref) <= 1e-5 * scale + 1e-6)
+
+
 def test_im2col_col2im_adjoint(S):
     rng = np.random.default_rng(3)
     Bn, H, W, Cc = 2, 8, 16, 5
