@@ -97,6 +97,60 @@ __device__ __forceinline__ bool bar_wait(unsigned long long* b, unsigned parity)
     return false;
 }
 
+// (c_y, c_z) of population n for a runtime n, by compile-time selects (an
+// indexed lattice table would live in local memory).
+template <int Q>
+__device__ __forceinline__ void lane_c(int n, int& cy, int& cz) {
+    cy = 0;
+    cz = 0;
+#pragma unroll
+    for (int m = 0; m < Q; ++m)
+        if (m == n) {
+            cy = Lat<Q>::cy(m);
+            cz = Lat<Q>::cz(m);
+        }
+}
+
+// Warp 0, lane n < Q: the staged run of population n for rows [yb, yb + r) of
+// plane z (in the array's element indices, widened to 8-element boundaries
+// and clipped at `total`); lane 0 announces the stage's bytes on its mbarrier
+// and every lane with a run issues its copy.
+template <int Q, class T>
+__device__ __forceinline__ void issue_runs(const KParams& p, const T* __restrict__ fin, int z, int yb, int r,
+                                           unsigned total, Run* rs, unsigned short* dst, int lpad,
+                                           unsigned long long* b) {
+    const int lane = threadIdx.x & 31;
+    const unsigned N = (unsigned)p.ncell;
+    Run run{0u, 0u};
+    if (lane < Q) {
+        int cy, cz;
+        lane_c<Q>(lane, cy, cz);
+        int zs = z - cz;
+        bool ok = true;
+        if (zs < 0 || zs >= p.nz) {
+            if (p.periodic[2]) zs = zs < 0 ? zs + p.nz : zs - p.nz;
+            else ok = false;
+        }
+        const int ya = max(yb - cy, 0), ye = min(yb + r - cy, p.ny);
+        if (ok && ye > ya) {
+            const unsigned a = (unsigned)lane * N + (unsigned)((zs * p.ny + ya) * p.nx);
+            const unsigned e0 = (unsigned)lane * N + (unsigned)((zs * p.ny + ye) * p.nx);
+            unsigned e = (e0 + 7u) & ~7u;
+            if (e > total) e = total;
+            run.base = a & ~7u;
+            run.len = e > run.base ? e - run.base : 0u;
+        }
+        rs[lane] = run;
+    }
+    unsigned bytes = 2u * run.len;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
+    __syncwarp();
+    if (lane == 0) bar_expect(b, bytes);
+    __syncwarp();
+    if (lane < Q && run.len) copy_g2s(dst + (size_t)lane * lpad, fin + run.base, 2u * run.len, b);
+}
+
 }  // namespace bulk
 
 template <int Q, class St, bool FORCED, int S>
@@ -118,42 +172,15 @@ __global__ void __launch_bounds__(bulk::kThreads, 3) k_step_pair_bulk(const type
     }
     __syncthreads();
 
-    // Thread 0: the runs of chunk k into stage s, and their copies.
+    // Warp 0: the runs of chunk k into stage s, and their copies.
     auto issue = [&](int k, int s) {
         const int pz = k / gm.cpp;
-        const int z = p.z0 + pz;
         const int yb = p.y0 + (k - pz * gm.cpp) * gm.rows;
-        const int r = min(gm.rows, p.y1 - yb);
-        bulk::Run* rs = runs + s * Q;
-        unsigned bytes = 0;
-#pragma unroll 1
-        for (int n = 0; n < Q; ++n) {
-            int zs = z - L::cz(n);
-            bool ok = true;
-            if (zs < 0 || zs >= p.nz) {
-                if (p.periodic[2]) zs = zs < 0 ? zs + p.nz : zs - p.nz;
-                else ok = false;
-            }
-            const int ya = max(yb - L::cy(n), 0), ye = min(yb + r - L::cy(n), p.ny);
-            bulk::Run run{0u, 0u};
-            if (ok && ye > ya) {
-                const unsigned a = (unsigned)n * N + (unsigned)((zs * p.ny + ya) * p.nx);
-                const unsigned b = (unsigned)n * N + (unsigned)((zs * p.ny + ye) * p.nx);
-                unsigned e = (b + 7u) & ~7u;
-                if (e > gm.total) e = gm.total;
-                run.base = a & ~7u;
-                run.len = e > run.base ? e - run.base : 0u;
-            }
-            rs[n] = run;
-            bytes += 2u * run.len;
-        }
-        bulk::bar_expect(&bar[s], bytes);
-#pragma unroll 1
-        for (int n = 0; n < Q; ++n)
-            if (rs[n].len) bulk::copy_g2s(data + (size_t)(s * Q + n) * gm.lpad, fin + rs[n].base, 2u * rs[n].len, &bar[s]);
+        bulk::issue_runs<Q>(p, fin, p.z0 + pz, yb, min(gm.rows, p.y1 - yb), gm.total, runs + s * Q,
+                            data + (size_t)s * Q * gm.lpad, gm.lpad, &bar[s]);
     };
 
-    if (tid == 0)
+    if (tid < 32)
         for (int i = 0; i < S - 1; ++i) {
             const int k = blockIdx.x + i * G;
             if (k < gm.nchunks) issue(k, i);
@@ -162,16 +189,17 @@ __global__ void __launch_bounds__(bulk::kThreads, 3) k_step_pair_bulk(const type
     bool timed_out = false;
     for (int k = blockIdx.x; k < gm.nchunks; k += G, ++it) {
         const int s = it % S;
-        // Refill the stage consumed in the previous iteration (every thread
-        // passed that iteration's closing barrier) with the chunk S - 1 ahead.
-        if (tid == 0) {
-            const int kn = k + (S - 1) * G;
-            if (kn < gm.nchunks) issue(kn, (it + S - 1) % S);
-        }
         const bool got = bulk::bar_wait(&bar[s], (unsigned)(it / S) & 1u);
         if (__syncthreads_or(!got)) {
             timed_out = true;
             break;
+        }
+        // Warp 0 refills the stage consumed in the previous iteration (every
+        // thread passed that iteration's closing barrier) with the chunk S - 1
+        // ahead, while the other warps start on this chunk.
+        if (tid < 32) {
+            const int kn = k + (S - 1) * G;
+            if (kn < gm.nchunks) issue(kn, (it + S - 1) % S);
         }
         const bulk::Run* rs = runs + s * Q;
         const unsigned short* st = data + (size_t)s * Q * gm.lpad;
@@ -181,6 +209,7 @@ __global__ void __launch_bounds__(bulk::kThreads, 3) k_step_pair_bulk(const type
         const int r = min(gm.rows, p.y1 - yb);
         const int hx = p.nx >> 1;
         const int npairs = r * hx;
+#pragma unroll 1
         for (int j = tid; j < npairs; j += bulk::kThreads) {
             const int row = j / hx;
             const int x = 2 * (j - row * hx);
@@ -222,8 +251,8 @@ __global__ void __launch_bounds__(bulk::kThreads, 3) k_step_pair_bulk(const type
     if (timed_out) {
         if (tid == 0) {
             atomicOr(flag, 2);
-            // copies still in flight: the chunks of iterations it .. it + S - 1
-            for (int i = 0; i < S; ++i) {
+            // copies still in flight: the chunks of iterations it .. it + S - 2
+            for (int i = 0; i < S - 1; ++i) {
                 const int j = it + i;
                 if (blockIdx.x + j * G < gm.nchunks) bulk::bar_wait(&bar[j % S], (unsigned)(j / S) & 1u);
             }
@@ -361,42 +390,15 @@ __global__ void __launch_bounds__(bulk::kThreads, 3) k_batch_pair_bulk(const typ
     }
     __syncthreads();
 
-    auto issue = [&](int k, int s) {
+    auto issue = [&](int k, int s) {  // warp 0
         const RowChunk ch = chunks[k];
         const KParams& p = dp[ch.dom];
-        const typename St::T* fin = fin_base + offs[ch.dom];
-        const unsigned N = (unsigned)p.ncell;
-        const unsigned total = ((unsigned)Q * N + 7u) & ~7u;
-        bulk::Run* rs = runs + s * Q;
-        unsigned bytes = 0;
-#pragma unroll 1
-        for (int n = 0; n < Q; ++n) {
-            int zs = ch.z - L::cz(n);
-            bool ok = true;
-            if (zs < 0 || zs >= p.nz) {
-                if (p.periodic[2]) zs = zs < 0 ? zs + p.nz : zs - p.nz;
-                else ok = false;
-            }
-            const int ya = max(ch.yb - L::cy(n), 0), ye = min(ch.yb + ch.r - L::cy(n), p.ny);
-            bulk::Run run{0u, 0u};
-            if (ok && ye > ya) {
-                const unsigned a = (unsigned)n * N + (unsigned)((zs * p.ny + ya) * p.nx);
-                const unsigned b = (unsigned)n * N + (unsigned)((zs * p.ny + ye) * p.nx);
-                unsigned e = (b + 7u) & ~7u;
-                if (e > total) e = total;
-                run.base = a & ~7u;
-                run.len = e > run.base ? e - run.base : 0u;
-            }
-            rs[n] = run;
-            bytes += 2u * run.len;
-        }
-        bulk::bar_expect(&bar[s], bytes);
-#pragma unroll 1
-        for (int n = 0; n < Q; ++n)
-            if (rs[n].len) bulk::copy_g2s(data + (size_t)(s * Q + n) * lpad, fin + rs[n].base, 2u * rs[n].len, &bar[s]);
+        const unsigned total = ((unsigned)Q * (unsigned)p.ncell + 7u) & ~7u;
+        bulk::issue_runs<Q>(p, fin_base + offs[ch.dom], ch.z, ch.yb, ch.r, total, runs + s * Q,
+                            data + (size_t)s * Q * lpad, lpad, &bar[s]);
     };
 
-    if (tid == 0)
+    if (tid < 32)
         for (int i = 0; i < S - 1; ++i) {
             const int k = blockIdx.x + i * G;
             if (k < nchunks) issue(k, i);
@@ -405,14 +407,14 @@ __global__ void __launch_bounds__(bulk::kThreads, 3) k_batch_pair_bulk(const typ
     bool timed_out = false;
     for (int k = blockIdx.x; k < nchunks; k += G, ++it) {
         const int s = it % S;
-        if (tid == 0) {
-            const int kn = k + (S - 1) * G;
-            if (kn < nchunks) issue(kn, (it + S - 1) % S);
-        }
         const bool got = bulk::bar_wait(&bar[s], (unsigned)(it / S) & 1u);
         if (__syncthreads_or(!got)) {
             timed_out = true;
             break;
+        }
+        if (tid < 32) {
+            const int kn = k + (S - 1) * G;
+            if (kn < nchunks) issue(kn, (it + S - 1) % S);
         }
         const RowChunk ch = chunks[k];
         const KParams& p = dp[ch.dom];
@@ -424,6 +426,7 @@ __global__ void __launch_bounds__(bulk::kThreads, 3) k_batch_pair_bulk(const typ
         const unsigned short* st = data + (size_t)s * Q * lpad;
         const int ncells = ch.r * p.nx;
         const unsigned c0 = (unsigned)((ch.z * p.ny + ch.yb) * p.nx);
+#pragma unroll 1
         for (int j = tid; 2 * j < ncells; j += bulk::kThreads) {
             const int la = 2 * j;
             const bool okb = la + 1 < ncells;
@@ -463,7 +466,7 @@ __global__ void __launch_bounds__(bulk::kThreads, 3) k_batch_pair_bulk(const typ
     if (timed_out) {
         if (tid == 0) {
             atomicOr(flag, 2);
-            for (int i = 0; i < S; ++i) {
+            for (int i = 0; i < S - 1; ++i) {
                 const int j = it + i;
                 if (blockIdx.x + j * G < nchunks) bulk::bar_wait(&bar[j % S], (unsigned)(j / S) & 1u);
             }
