@@ -76,8 +76,11 @@ size_t elem_of(int prec) {
 // chunk is 256 K cells), cand / 3 a persistent grid; the shifted 16-bit
 // policies take cells in pairs, so K = 1 is skipped for them, and the
 // fixed-point step holds at most two cells of int64 populations per thread,
-// so K = 4 is skipped for it.  Candidate 6 (16-bit storages only) is the
-// persistent kernel with bulk-copy staging over chunks of whole rows.
+// so K = 4 is skipped for it.  Candidate 6 (16-bit storages only, chosen
+// only through MPH_BATCH_CANDIDATE=6) is the persistent kernel with
+// bulk-copy staging over chunks of whole rows: bit-identical, but measured
+// slower than the direct kernels (the 16-bit step is bound by instruction
+// issue, and staging adds instructions), so the autotuner does not time it.
 constexpr int kCells[3] = {1, 2, 4};
 constexpr int kCands = 7;
 constexpr int kBulkCand = 6;
@@ -355,7 +358,7 @@ int autotune(mph_batch* b) {
     float best = 1e30f;
     int besti = shifted(b->prec) ? 1 : 0;
     for (int wi = 0; wi < kCands && e == cudaSuccess; ++wi) {
-        if (!candidate_ok(b->prec, wi) || (wi == kBulkCand && !b->bulk_ok)) continue;
+        if (!candidate_ok(b->prec, wi) || wi == kBulkCand) continue;
         int rc = ensure_chunks(b, wi % 3);
         if (rc) { cudaFree(save); return rc; }
         rc = step_once(b, wi);

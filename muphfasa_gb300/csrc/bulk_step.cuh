@@ -3,10 +3,16 @@
 // bulk asynchronous copies.  Included by the k_fast_* translation units of
 // the 16-bit precisions.
 //
-// Why: a 2-byte population gives a warp only 64 bytes per load instruction,
-// so the direct pair kernel (k_step_pair) keeps too few bytes in flight to
-// cover the HBM latency (the measured copy ceiling of that access pattern is
-// 0.87 of the copy peak, and the step reaches 0.70).  Here the unit of work is
+// Why it exists: a 2-byte population gives a warp only 64 bytes per load
+// instruction, so a direct pull keeps few bytes in flight (the measured copy
+// ceiling of the pair pattern is 0.87-0.89 of the copy peak, the direct step
+// reaches 0.72).  Measured on the 512^3 D3Q19 channel (FP16): 44 GLUPS (0.50)
+// against the direct kernel's 63 (0.72).  An ncu capture at 256^3 shows why:
+// the direct step is already close to issue-bound (357 instructions per cell,
+// issue slots 56 % busy) and staging adds 46 % instructions (shared-memory
+// loads, run bounds checks) plus block-barrier stalls.  The kernel is kept as
+// an opt-in (MPH_PAIR_KERNEL=bulk; batches: MPH_BATCH_CANDIDATE=6), bit-
+// identical to the direct one.  Here the unit of work is
 // a chunk of whole rows (y, z) of the launch window.  For every population n
 // the rows its cells pull from are the chunk's rows shifted by (c_y, c_z):
 // one contiguous run of the population's SoA array (the x shift, periodic x
@@ -273,7 +279,7 @@ inline size_t bulk_smem_bytes(int q, int stages, int lpad) {
 constexpr int kBulkMaxSmem = 227 * 1024;
 
 inline bool bulk_geometry(const KParams& p, int q, int stages, int cells, long long total_elems, BulkGeom& gm) {
-    if (p.nx % 2 != 0 || p.cls || stages < 2 || stages > 4) return false;
+    if (p.nx % 2 != 0 || p.cls || stages < 2 || stages > 3) return false;
     if (total_elems >= (1LL << 32) - 64) return false;
     int rows = cells / p.nx;
     if (rows < 1) rows = 1;
@@ -347,7 +353,6 @@ cudaError_t launch_step_bulk_t(int mode, int q, bool forced, const void* fin, vo
     case QQ:              \
         MPH_BULK_S(QQ, 2) \
         MPH_BULK_S(QQ, 3) \
-        MPH_BULK_S(QQ, 4) \
         return cudaErrorNotSupported;
     switch (q) {
         MPH_BULK_Q(9)

@@ -73,7 +73,7 @@ cudaError_t launch_step_fast_bf16s(int q, bool forced, const void* fin, void* fo
 cudaError_t launch_step_fast_f16c(int q, bool forced, const void* fin, void* fout, const KParams& p,
                                   const KParams* pg, cudaStream_t s);
 // The 16-bit pair step with bulk-copy staging (bulk_step.cuh): chunks of
-// about `cells` cells of whole rows, `stages` shared-memory stages (2..4),
+// about `cells` cells of whole rows, `stages` shared-memory stages (2 or 3),
 // total_elems = elements of the population array, flag |= 2 on a wait
 // timeout.  mode 0 prepares the kernels (once per handle, before any launch
 // or stream capture), mode 1 launches.  cudaErrorNotSupported when the launch

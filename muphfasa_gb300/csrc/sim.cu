@@ -769,7 +769,7 @@ int mph_create(const mph_desc* desc, mph_sim** out) {
         }
     }
     // 16-bit storages: the pair step with bulk-copy staging of its pull
-    // operands (MPH_PAIR_KERNEL=bulk, stages MPH_BULK_STAGES 2..4, chunk
+    // operands (MPH_PAIR_KERNEL=bulk, stages MPH_BULK_STAGES 2 or 3, chunk
     // cells MPH_BULK_CELLS) or the direct pair kernel (MPH_PAIR_KERNEL=direct).
     const bool p16 = d.precision == MPH_PREC_F16S || d.precision == MPH_PREC_BF16S || d.precision == MPH_PREC_F16C;
     if (e == cudaSuccess && p16) {
@@ -778,10 +778,10 @@ int mph_create(const mph_desc* desc, mph_sim** out) {
             s->bulk_stages = 3;
             if (const char* v = std::getenv("MPH_BULK_STAGES")) s->bulk_stages = std::atoi(v);
             if (const char* v = std::getenv("MPH_BULK_CELLS")) s->bulk_cells = std::atoi(v);
-            if (s->bulk_stages < 2 || s->bulk_stages > 4 || s->bulk_cells < 2) {
+            if (s->bulk_stages < 2 || s->bulk_stages > 3 || s->bulk_cells < 2) {
                 free_all(s);
                 delete s;
-                return fail(MPH_ERR_ARG, "mph_create: MPH_BULK_STAGES must be 2..4 and MPH_BULK_CELLS >= 2");
+                return fail(MPH_ERR_ARG, "mph_create: MPH_BULK_STAGES must be 2 or 3 and MPH_BULK_CELLS >= 2");
             }
             e = cudaMalloc(&s->d_flag, sizeof(int));
             if (e == cudaSuccess) e = cudaMemset(s->d_flag, 0, sizeof(int));

@@ -72,7 +72,7 @@ def test_bulk_step_equals_direct_pair_step(case, prec, mph):
     assert np.array_equal(a.f(), b.f())
 
 
-@pytest.mark.parametrize("stages,cells", [(2, 2), (3, 100), (4, 512), (2, 4096)])
+@pytest.mark.parametrize("stages,cells", [(2, 2), (3, 100), (3, 512), (2, 4096)])
 def test_bulk_step_every_stage_count_and_chunk_size(stages, cells, mph):
     case = CASES[2]
     d = _desc(mph, case, "f16s")
@@ -106,5 +106,5 @@ def test_bulk_step_large_channel_and_host_slabs(mph):
 def test_bulk_step_rejects_bad_settings(mph):
     d = _desc(mph, CASES[0], "f16s")
     with pytest.raises(mph.MphError) as e:
-        _sim(mph, d, True, stages=5)
+        _sim(mph, d, True, stages=4)
     assert e.value.code == 1
