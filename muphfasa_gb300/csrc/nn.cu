@@ -514,6 +514,24 @@ __global__ void k_splitk_reduce(const float* __restrict__ W, int S, int M, int N
 }
 
 // ---- convolution data movement --------------------------------------------
+// im2col with 16-byte moves (C a multiple of 8, 32-bit index math): one
+// thread per (pixel, tap, 8-channel group); consecutive threads read and
+// write consecutive 16-byte groups.
+__global__ void __launch_bounds__(256) k_im2col3_v8(const uint4* __restrict__ X, int Bn, int H, int W, int G,
+                                                    uint4* __restrict__ Xcol) {
+    const unsigned total = (unsigned)Bn * H * W * 9u * G;
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const unsigned g = i % G, r = i / G;
+    const unsigned tap = r % 9u, p = r / 9u;
+    const unsigned x = p % W, q = p / W;
+    const unsigned y = q % H, b = q / H;
+    const int sy = (int)y + (int)(tap / 3u) - 1, sx = (int)x + (int)(tap % 3u) - 1;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (sy >= 0 && sy < H && sx >= 0 && sx < W) v = X[((b * H + sy) * (unsigned)W + sx) * G + g];
+    Xcol[i] = v;
+}
+
 // Xcol[p][(dy * 3 + dx) * C + c] = X[b][y + dy - 1][x + dx - 1][c] (0 outside).
 __global__ void k_im2col3(const bf16* __restrict__ X, int Bn, int H, int W, int C, bf16* __restrict__ Xcol) {
     const long long total = (long long)Bn * H * W * 9 * C;
@@ -559,8 +577,10 @@ __global__ void k_bias_act(const float* __restrict__ Y, const float* __restrict_
     const long long total = P * C;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
          i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long long p = i / C;
+        // 32-bit division while the index fits (a 64-bit one costs several times more)
+        const bool small = total < (1LL << 32);
+        const int c = small ? (int)((unsigned)i % (unsigned)C) : (int)(i % C);
+        const long long p = small ? (long long)((unsigned)i / (unsigned)C) : i / C;
         float v = Y[i] + bias[c];
         if (act && v < 0.f) v *= 0.1f;
         if (out_bf) out_bf[p * ld_out + c_off + c] = __float2bfloat16(v);
@@ -574,12 +594,42 @@ __global__ void k_act_bwd(const float* __restrict__ dOut, int ld_dout, int c_off
     const long long total = P * C;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
          i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long long p = i / C;
+        const bool small = total < (1LL << 32);
+        const int c = small ? (int)((unsigned)i % (unsigned)C) : (int)(i % C);
+        const long long p = small ? (long long)((unsigned)i / (unsigned)C) : i / C;
         float d = dOut[p * ld_dout + c_off + c];
         if (act && __bfloat162float(act_out[p * ld_act + act_off + c]) < 0.f) d *= 0.1f;
         dPre[i] = d;
     }
+}
+
+// Column sums in two fixed-order passes, for C dividing 256: block b sums the
+// rows of its slice (each thread keeps one column, t mod C, since 256 is a
+// multiple of C), then part[b][c]; k_colsum_final adds the blocks in order.
+__global__ void __launch_bounds__(256) k_colsum_part(const float* __restrict__ X, long long P, int C, long long rows,
+                                                     float* __restrict__ part) {
+    const long long r0 = (long long)blockIdx.x * rows;
+    const long long r1 = min(P, r0 + rows);
+    const float* x = X + r0 * C;
+    const long long n = (r1 > r0 ? r1 - r0 : 0) * C;
+    float s = 0.f;
+    for (long long j = threadIdx.x; j < n; j += 256) s += x[j];
+    __shared__ float sh[256];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x < C) {
+        float t = 0.f;
+        for (int k = threadIdx.x; k < 256; k += C) t += sh[k];
+        part[(long long)blockIdx.x * C + threadIdx.x] = t;
+    }
+}
+
+__global__ void k_colsum_final(const float* __restrict__ part, int nb, int C, float* __restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    float t = 0.f;
+    for (int b = 0; b < nb; ++b) t += part[(long long)b * C + c];
+    out[c] = t;
 }
 
 // db[c] = sum_p dPre[p][c]: one block per channel group, fixed order.
@@ -906,6 +956,13 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
 
 int mph_nn_im2col3(const void* X, int Bn, int H, int W, int C, void* Xcol, void* stream) {
     const long long n = (long long)Bn * H * W * 9 * C;
+    const bool aligned = ((reinterpret_cast<unsigned long long>(X) | reinterpret_cast<unsigned long long>(Xcol)) & 15) == 0;
+    if (C % 8 == 0 && aligned && n / 8 < 0xffffffffLL) {
+        const long long nv = n / 8;
+        k_im2col3_v8<<<(unsigned)((nv + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            static_cast<const uint4*>(X), Bn, H, W, C / 8, static_cast<uint4*>(Xcol));
+        return ck("im2col");
+    }
     k_im2col3<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const bf16*>(X), Bn, H, W, C,
                                                                            static_cast<bf16*>(Xcol));
     return ck("im2col");
@@ -932,8 +989,25 @@ int mph_nn_act_bwd(const float* dOut, int ld_dout, int c_off, const void* act_ou
     return ck("act_bwd");
 }
 
+// [blocks][C] partial column sums, shared by every call: calls on different
+// streams must not overlap (the surrogate issues all its kernels on one stream).
+static float* g_colsum_ws = nullptr;
+static constexpr int kColsumBlocks = 608;
+
 int mph_nn_colsum(const float* X, long long P, int C, float* out, void* stream) {
-    k_colsum<<<C, 256, 0, static_cast<cudaStream_t>(stream)>>>(X, P, C, out);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (C > 0 && C <= 256 && 256 % C == 0 && P >= 256) {
+        if (!g_colsum_ws) {
+            const cudaError_t e = cudaMalloc(&g_colsum_ws, sizeof(float) * kColsumBlocks * 256);
+            if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string("mph_nn_colsum: ") + cudaGetErrorString(e));
+        }
+        const long long rows = (P + kColsumBlocks - 1) / kColsumBlocks;
+        const int nb = (int)((P + rows - 1) / rows);
+        k_colsum_part<<<nb, 256, 0, s>>>(X, P, C, rows, g_colsum_ws);
+        k_colsum_final<<<(C + 255) / 256, 256, 0, s>>>(g_colsum_ws, nb, C, out);
+        return ck("colsum");
+    }
+    k_colsum<<<C, 256, 0, s>>>(X, P, C, out);
     return ck("colsum");
 }
 

@@ -117,6 +117,29 @@ def test_data_gradient_as_mirrored_convolution(cin, cout, S):
     assert np.all(np.abs(got - ref) <= 1e-5 * scale + 1e-6)
 
 
+@pytest.mark.parametrize("Cc", [8, 16, 96])
+def test_im2col_16_byte_path(Cc, S):
+    """im2col with C a multiple of 8 (16-byte moves) against the restatement."""
+    rng = np.random.default_rng(Cc)
+    Bn, H, W = 2, 8, 16
+    x = NO.to_bf16(rng.standard_normal((Bn, H, W, Cc)).astype(np.float32))
+    dx_, col = _bf16_dev(S, x), S._bf(Bn * H * W * 9 * Cc)
+    S.check(S._lib().mph_nn_im2col3(dx_.ptr, Bn, H, W, Cc, col.ptr, None))
+    got = _download_bf16(S, col, Bn * H * W * 9 * Cc).reshape(Bn * H * W, 9 * Cc)
+    assert np.array_equal(got, NO.Net.im2col(x))
+
+
+@pytest.mark.parametrize("P,Cc", [(131072, 32), (2048, 256), (300, 64), (4096, 3), (100, 8)])
+def test_colsum(P, Cc, S):
+    rng = np.random.default_rng(P + Cc)
+    x = rng.standard_normal((P, Cc)).astype(np.float32)
+    dx_, out = S._f32(x.size), S._f32(Cc)
+    dx_.upload(x.reshape(-1))
+    S.check(S._lib().mph_nn_colsum(dx_.ptr, P, Cc, out.ptr, None))
+    ref = x.astype(np.float64).sum(axis=0)
+    assert np.allclose(out.download(Cc), ref, rtol=1e-5, atol=1e-5 * np.sqrt(P))
+
+
 def test_im2col_col2im_adjoint(S):
     rng = np.random.default_rng(3)
     Bn, H, W, Cc = 2, 8, 16, 5
