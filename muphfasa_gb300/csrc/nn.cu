@@ -15,6 +15,8 @@
 //
 // Shapes: activations [P][C] with P = batch x H x W pixels (NHWC), weights of
 // a 3 x 3 conv as Wt [Cout][9 Cin] (k = (dy * 3 + dx) * Cin + ci contiguous).
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -499,6 +501,166 @@ __global__ void __launch_bounds__(128) k_gemm_tc05p(int M, int N, int K, const b
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_BN));
 }
 
+// ---- TMA-fed tcgen05 GEMM (both operands K-contiguous) --------------------
+// Same contract as k_gemm_tc05p for ta = tb = 0.  A 128 x BN tile of C per CTA
+// of 128 threads; K in slices of 64 through a ring of TM_STAGES stages:
+//   thread 0 (producer): waits for the stage to be empty, announces the bytes
+//     on its `full` mbarrier and issues two tiled TMA copies
+//     (cp.async.bulk.tensor.2d, 128-byte swizzle: the A slice is 128 rows x
+//     128 B, the B slice BN rows x 128 B; rows / columns past M, N or K read as
+//     zeros);
+//   thread 32 (MMA issuer): waits for the stage to be full and issues four
+//     tcgen05.mma (M 128, N BN, K 16) on 128-byte-swizzled K-major shared-memory
+//     descriptors (8-row atoms 1024 B apart, the K step advances the start
+//     address by 32 B inside the atom), then tcgen05.commit to the stage's
+//     `empty` mbarrier, and after the last slice to `done`;
+//   all warps: wait for `done`, read the FP32 accumulator from TMEM in 32-column
+//     pieces (tcgen05.ld.32x32b.x32), transpose it through shared memory (the
+//     stage buffers, free by then) and write C rows with consecutive lanes on
+//     consecutive columns.
+// Every wait is bounded (mbar_wait); the outcome is combined over the block
+// before the warp-collective TMEM reads, and a timeout sets g_nn_timeout.
+constexpr int TM_BK = 64, TM_STAGES = 4;
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// K-major shared-memory matrix descriptor, 128-byte swizzle: rows of 128 B,
+// atoms of 8 rows 1024 B apart (stride byte offset), leading byte offset
+// unused (1), descriptor version 1 (bits 46-47), layout type 2 (bits 61-63).
+__device__ __forceinline__ unsigned long long smem_desc_sw128(unsigned addr) {
+    return (unsigned long long)((addr >> 4) & 0x3FFF) | (1ull << 16) | ((unsigned long long)(1024 >> 4) << 32) |
+           (1ull << 46) | (2ull << 61);
+}
+
+template <int BN>
+__global__ void __launch_bounds__(128) k_gemm_tma(int M, int N, const __grid_constant__ CUtensorMap tmA,
+                                                  const __grid_constant__ CUtensorMap tmB, float* __restrict__ C,
+                                                  long long ldc, int accumulate, int K, int kchunk) {
+    constexpr int A_BYTES = 128 * TM_BK * 2, B_BYTES = BN * TM_BK * 2;
+    extern __shared__ unsigned char tm_dyn[];
+    __shared__ __align__(8) unsigned long long full[TM_STAGES], empty[TM_STAGES], done;
+    __shared__ unsigned tmem_base;
+    // stage buffers on a 1024-byte boundary (the swizzle atom)
+    unsigned char* base = tm_dyn + ((1024u - (smem_u32(tm_dyn) & 1023u)) & 1023u);
+    unsigned char* sA = base;
+    unsigned char* sB = base + TM_STAGES * A_BYTES;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.y * 128, n0 = blockIdx.x * BN;
+    const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+    const int nk = (ke - kb + TM_BK - 1) / TM_BK;
+    C += (long long)blockIdx.z * M * ldc;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
+                     "r"(BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    if (tid == 0) {
+        for (int s = 0; s < TM_STAGES; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&full[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&empty[s])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&done)));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<unsigned long long>(&tmA)) : "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<unsigned long long>(&tmB)) : "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    const unsigned tmem = tmem_base;
+    bool ok = true;
+    if (tid == 0) {  // producer
+        for (int kt = 0; kt < nk; ++kt) {
+            const int s = kt % TM_STAGES, u = kt / TM_STAGES;
+            if (u > 0 && !mbar_wait(smem_u32(&empty[s]), (unsigned)(u - 1) & 1u)) {
+                ok = false;
+                break;
+            }
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(&full[s])),
+                         "r"(A_BYTES + B_BYTES)
+                         : "memory");
+            tma_load_2d(sA + s * A_BYTES, &tmA, kb + kt * TM_BK, m0, &full[s]);
+            tma_load_2d(sB + s * B_BYTES, &tmB, kb + kt * TM_BK, n0, &full[s]);
+        }
+    } else if (tid == 32) {  // MMA issuer
+        const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(BN >> 3) << 17) | ((unsigned)(128 >> 4) << 24);
+        for (int kt = 0; kt < nk; ++kt) {
+            const int s = kt % TM_STAGES, u = kt / TM_STAGES;
+            if (!mbar_wait(smem_u32(&full[s]), (unsigned)u & 1u)) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+#pragma unroll
+            for (int kk = 0; kk < TM_BK / 16; ++kk) {
+                const unsigned long long ad = smem_desc_sw128(smem_u32(sA + s * A_BYTES) + kk * 32);
+                const unsigned long long bd = smem_desc_sw128(smem_u32(sB + s * B_BYTES) + kk * 32);
+                const unsigned acc = (kt > 0 || kk > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                smem_u32(&empty[s])));
+        }
+        if (ok)
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                smem_u32(&done)));
+    }
+    __syncwarp();
+    const bool got = ok && mbar_wait(smem_u32(&done), 0u);
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    ok = __syncthreads_and(got) != 0;
+    if (!ok && tid == 0) atomicExch(&g_nn_timeout, 1);
+    if (ok) {
+        // TMEM -> registers -> shared memory tile [128][BN + 1] -> coalesced rows of C
+        float* tile = reinterpret_cast<float*>(base);
+        constexpr int LD = BN + 1;
+        const int row = 32 * warp + lane;
+#pragma unroll
+        for (int c0 = 0; c0 < BN; c0 += 32) {
+            unsigned r[32];
+            const unsigned taddr = tmem + ((unsigned)(32 * warp) << 16) + (unsigned)c0;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,"
+                "%28,%29,%30,%31}, [%32];\n"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+                  "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+                  "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+            for (int j = 0; j < 32; ++j) tile[row * LD + c0 + j] = __uint_as_float(r[j]);
+        }
+        __syncwarp();
+        for (int rr = 0; rr < 32; ++rr) {
+            const int trow = 32 * warp + rr;
+            const int gm = m0 + trow;
+            if (gm >= M) break;
+            float* crow = C + (long long)gm * ldc + n0;
+            for (int c = lane; c < BN; c += 32)
+                if (n0 + c < N) crow[c] = accumulate ? crow[c] + tile[trow * LD + c] : tile[trow * LD + c];
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(BN));
+}
+
+template <int BN>
+constexpr size_t tma_smem_bytes() {
+    return 1024 + (size_t)TM_STAGES * (128 + BN) * TM_BK * 2;
+}
+
 // C[m][n] (+)= sum over splits z of W[z][m][n] (W rows of width N), in split order.
 __global__ void k_splitk_reduce(const float* __restrict__ W, int S, int M, int N, float* __restrict__ C, long long ldc,
                                 int accumulate) {
@@ -841,6 +1003,51 @@ int ck(const char* what) {
 
 }  // namespace
 
+// cuTensorMapEncodeTiled from the driver (through the runtime's entry-point
+// query, so the library does not link libcuda); null when unavailable.
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+static bool g_encode_tried = false;
+
+static bool tma_available() {
+    if (!g_encode_tried) {
+        g_encode_tried = true;
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess && fn)
+            g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        else
+            cudaGetLastError();
+    }
+    return g_encode != nullptr;
+}
+
+// Map of a row-major BF16 matrix [rows][cols] (row stride ld elements) read
+// in boxes of 64 columns (128 B, the swizzle span) x box_rows rows.
+static bool tma_map(CUtensorMap* m, const void* ptr, long long rows, long long cols, long long ld, int box_rows) {
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {64u, (cuuint32_t)box_rows};
+    const cuuint32_t es[2] = {1u, 1u};
+    return g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN>
+static cudaError_t launch_tma(const dim3& g, int M, int N, const CUtensorMap& ta, const CUtensorMap& tb, float* out,
+                              long long ldo, int acc, int K, int kchunk, cudaStream_t s) {
+    static bool attr = false;
+    constexpr size_t smem = tma_smem_bytes<BN>();
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(k_gemm_tma<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    k_gemm_tma<BN><<<g, 128, smem, s>>>(M, N, ta, tb, out, ldo, acc, K, kchunk);
+    return cudaGetLastError();
+}
+
 extern "C" {
 
 int mph_nn_alloc(long long bytes, void** out) {
@@ -870,11 +1077,15 @@ int mph_nn_sync(void* stream) {
     return MPH_OK;
 }
 
-static int g_gemm_mode = 0;  // 0 auto, 1 mma.sync, 2 tcgen05 pipelined, 3 tcgen05 single-buffered
+// 0 auto, 1 mma.sync, 2 tcgen05 pipelined (cp.async), 3 tcgen05 single-
+// buffered, 4 tcgen05 fed by TMA (where both operands are K-contiguous and
+// 16-byte aligned; the pipelined kernel otherwise)
+static int g_gemm_mode = 0;
 
 int mph_nn_gemm_mode(int mode) {
-    if (mode < 0 || mode > 3)
-        return mph::fail(MPH_ERR_ARG, "mph_nn_gemm_mode: 0 auto, 1 mma.sync, 2 tcgen05, 3 tcgen05 single-buffered");
+    if (mode < 0 || mode > 4)
+        return mph::fail(MPH_ERR_ARG, "mph_nn_gemm_mode: 0 auto, 1 mma.sync, 2 tcgen05, 3 tcgen05 single-buffered, "
+                                      "4 tcgen05 with TMA");
     g_gemm_mode = mode;
     return MPH_OK;
 }
@@ -906,7 +1117,12 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
     // is long (a weight gradient, K = pixels), where the idle rows cost less
     // than the slower kernel.
     const bool tc = g_gemm_mode >= 2 || (g_gemm_mode == 0 && (M >= TC_BM || K >= 16 * TC_BK) && N >= 16);
-    const int tm = tc ? TC_BM : BM, tn = tc ? TC_BN : BN;
+    // TMA operands: K-contiguous, 16-byte aligned bases and row strides
+    const bool tma = tc && (g_gemm_mode == 0 || g_gemm_mode == 4) && !ta && !tb &&
+                     ((reinterpret_cast<unsigned long long>(A) | reinterpret_cast<unsigned long long>(B)) & 15) == 0 &&
+                     lda % 8 == 0 && ldb % 8 == 0 && tma_available();
+    const int tma_bn = N <= 32 ? 32 : (N <= 64 ? 64 : 128);
+    const int tm = tc ? TC_BM : BM, tn = tma ? tma_bn : (tc ? TC_BN : BN);
     const long long gx = (N + tn - 1) / tn, gy = (M + tm - 1) / tm;
     if (gy > 65535) return mph::fail(MPH_ERR_ARG, "mph_nn_gemm: M too large for one launch");
     // Enough blocks for the 152 SMs: split K when the output tiles are few.
@@ -937,6 +1153,17 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
         acc = 0;
     }
     const dim3 g((unsigned)gx, (unsigned)gy, (unsigned)S);
+    if (tma) {
+        CUtensorMap tA, tB;
+        if (!tma_map(&tA, A, M, K, lda, 128) || !tma_map(&tB, B, N, K, ldb, tma_bn))
+            return mph::fail(MPH_ERR_CUDA, "mph_nn_gemm: cuTensorMapEncodeTiled failed");
+        cudaError_t e = tma_bn == 32 ? launch_tma<32>(g, M, N, tA, tB, out, ldo, acc, K, kchunk, s)
+                      : tma_bn == 64 ? launch_tma<64>(g, M, N, tA, tB, out, ldo, acc, K, kchunk, s)
+                                     : launch_tma<128>(g, M, N, tA, tB, out, ldo, acc, K, kchunk, s);
+        if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string("mph_nn_gemm (TMA): ") + cudaGetErrorString(e));
+        if (S > 1) k_splitk_reduce<<<grid_for((long long)M * N), 256, 0, s>>>(g_ws, S, M, N, C, ldc, accumulate);
+        return ck("gemm (tcgen05, TMA)");
+    }
 #define MPH_GEMM_LAUNCH(KERN)                                                                                  \
     if (!ta && !tb) KERN<false, false><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, out, ldo, acc, kchunk);      \
     else if (!ta && tb) KERN<false, true><<<g, 128, 0, s>>>(M, N, K, a, lda, b, ldb, out, ldo, acc, kchunk);   \

@@ -51,8 +51,9 @@ def test_gemm_layouts(ta, tb, S):
 @pytest.mark.parametrize("shape", [(200, 70, 100), (1024, 256, 576), (128, 64, 64), (130, 70, 32), (300, 64, 4096)])
 @pytest.mark.parametrize("ta,tb", [(0, 0), (0, 1), (1, 0), (1, 1)])
 def test_tcgen05_gemm_matches_mma_sync_and_numpy(ta, tb, shape, S):
-    """The tensor-memory GEMMs (tcgen05.mma, 128 x 64 tiles; pipelined and
-    single-buffered) against NumPy and against the mma.sync kernel."""
+    """The tensor-memory GEMMs (tcgen05.mma: cp.async pipelined, single-
+    buffered, and TMA-fed where the operands are K-contiguous and aligned)
+    against NumPy and against the mma.sync kernel."""
     rng = np.random.default_rng(10 + ta * 2 + tb)
     M, N, K = shape
     A = NO.to_bf16(rng.standard_normal((M, K)).astype(np.float32))
@@ -61,7 +62,7 @@ def test_tcgen05_gemm_matches_mma_sync_and_numpy(ta, tb, shape, S):
     L = S._lib()
     out = {}
     try:
-        for mode in (1, 2, 3):
+        for mode in (1, 2, 3, 4):
             S.check(L.mph_nn_gemm_mode(mode))
             c = S._f32(M * N)
             S.check(L.mph_nn_gemm(M, N, K, da.ptr, M if ta else K, ta, db.ptr, N if tb else K, tb, c.ptr, N, 0, None))
@@ -73,7 +74,7 @@ def test_tcgen05_gemm_matches_mma_sync_and_numpy(ta, tb, shape, S):
     assert flag.value == 0
     ref = A.astype(np.float64) @ B.astype(np.float64)
     scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64)
-    for mode in (2, 3):
+    for mode in (2, 3, 4):
         assert np.all(np.abs(out[mode] - ref) <= 1e-5 * scale + 1e-6), mode
         assert np.all(np.abs(out[mode] - out[1]) <= 2e-5 * scale + 2e-6), mode
 
@@ -138,6 +139,36 @@ def test_colsum(P, Cc, S):
     S.check(S._lib().mph_nn_colsum(dx_.ptr, P, Cc, out.ptr, None))
     ref = x.astype(np.float64).sum(axis=0)
     assert np.allclose(out.download(Cc), ref, rtol=1e-5, atol=1e-5 * np.sqrt(P))
+
+
+@pytest.mark.parametrize("shape", [(4096, 32, 288), (1000, 96, 864), (64, 288, 8192), (256, 3, 64), (131, 200, 72)])
+def test_tma_gemm_shapes_of_the_network(shape, S):
+    """The TMA-fed tcgen05 GEMM (K-contiguous operands) on the network's
+    shapes: a forward convolution (N = 32), a partial last row tile and a
+    128-wide column tile, a weight gradient (K = pixels, split K, M < 128), a
+    3-column output and a K that is not a multiple of the 64-wide slices."""
+    rng = np.random.default_rng(sum(shape))
+    M, N, K = shape
+    A = NO.to_bf16(rng.standard_normal((M, K)).astype(np.float32))
+    B = NO.to_bf16(rng.standard_normal((K, N)).astype(np.float32))
+    da, db = _bf16_dev(S, A), _bf16_dev(S, B.T)
+    L = S._lib()
+    c = S._f32(M * N)
+    try:
+        S.check(L.mph_nn_gemm_mode(4))
+        S.check(L.mph_nn_gemm(M, N, K, da.ptr, K, 0, db.ptr, K, 0, c.ptr, N, 0, None))
+        got = c.download(M * N).reshape(M, N)
+        S.check(L.mph_nn_gemm(M, N, K, da.ptr, K, 0, db.ptr, K, 0, c.ptr, N, 1, None))
+        got2 = c.download(M * N).reshape(M, N)
+    finally:
+        S.check(L.mph_nn_gemm_mode(0))
+    flag = C.c_int(-1)
+    S.check(L.mph_nn_status(C.byref(flag), 1))
+    assert flag.value == 0
+    ref = A.astype(np.float64) @ B.astype(np.float64)
+    scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64)
+    assert np.all(np.abs(got - ref) <= 1e-5 * scale + 1e-6)
+    assert np.all(np.abs(got2 - 2 * ref) <= 2e-5 * scale + 2e-6)
 
 
 def test_im2col_col2im_adjoint(S):
