@@ -299,6 +299,33 @@ def tgv2d_fields(N, u0):
     return rho.ravel(), np.concatenate([ux.ravel(), uy.ravel()])
 
 
+def surrogate_measure(n, steps, warmup):
+    """Training iterations of the warm-start U-Net (batch 8, n^2 cells):
+    (seconds, last loss, parameters, clock summary)."""
+    import muphfasa_gb300 as m
+    from muphfasa_gb300 import surrogate as sg
+    from muphfasa_gb300.surrogate import Trainer, UNet
+    sync = lambda: m.check(sg._lib().mph_nn_sync(None))
+    B = 8
+    rng = np.random.default_rng(5)
+    X = rng.standard_normal((B, n, n, 8)).astype(np.float32)
+    Y = rng.standard_normal((B, n, n, 3)).astype(np.float32)
+    M = (rng.random((B, n, n)) < 0.9).astype(np.float32)
+    net = UNet(seed=1)
+    tr = Trainer(net, B, n, n)
+    for _ in range(warmup):
+        tr.train_step(X, Y, M, 1e-4)
+    sync()
+    sm = ClockSampler(0)
+    with sm:
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            loss = tr.train_step(X, Y, M, 1e-4)
+        sync()
+        dt = time.perf_counter() - t0
+    return dt, float(loss), net.n_params(), sm.summary()
+
+
 def run_surrogate(args):
     """Training throughput of the warm-start U-Net: Adam iterations (forward,
     masked loss, backward, gradient clipping, update) on seeded synthetic
@@ -306,34 +333,17 @@ def run_surrogate(args):
     output channels), timed end to end including the host-side input upload
     and loss download of every iteration."""
     import muphfasa_gb300 as m
-    from muphfasa_gb300 import surrogate as sg
-    from muphfasa_gb300.surrogate import Trainer, UNet
     m.set_device(0)
-    sync = lambda: m.check(sg._lib().mph_nn_sync(None))
-    n, B = args.ws_n, 8
-    rng = np.random.default_rng(5)
-    X = rng.standard_normal((B, n, n, 8)).astype(np.float32)
-    Y = rng.standard_normal((B, n, n, 3)).astype(np.float32)
-    M = (rng.random((B, n, n)) < 0.9).astype(np.float32)
-    net = UNet(seed=1)
-    tr = Trainer(net, B, n, n)
-    for _ in range(args.warmup):
-        tr.train_step(X, Y, M, 1e-4)
-    sync()
-    sm = ClockSampler(0)
-    with sm:
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            loss = tr.train_step(X, Y, M, 1e-4)
-        sync()
-        dt = time.perf_counter() - t0
+    n = args.ws_n
+    dt, loss, nparams, clk = surrogate_measure(n, args.steps, args.warmup)
+    B = 8
     line = {"metric": "surrogate training iterations per second", "value": round(args.steps / dt, 2),
             "unit": "iterations/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1e3 * dt / args.steps, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16 operands / f32 accumulate", "data": "synthetic",
-            "config": {"workload": f"unet_train_{n}^2_batch{B}", "params": net.n_params(),
-                       "gemm": "tcgen05 BF16 (mma.sync below 128 rows)"},
-            "loss": round(float(loss), 6), "clocks": sm.summary()}
+            "config": {"workload": f"unet_train_{n}^2_batch{B}", "params": nparams,
+                       "gemm": "tcgen05 BF16 (TMA-fed where operands are K-contiguous; mma.sync below 128 rows)"},
+            "loss": round(loss, 6), "clocks": clk}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -736,6 +746,16 @@ def main():
             secondary = {"batch512": rec}
         except Exception as ex:  # report, do not hide
             secondary = {"batch512": {"error": str(ex)[:200]}}
+        # the warm-start surrogate's training throughput (128^2, batch 8)
+        try:
+            its = 50
+            dt, _, nparams, sclk = surrogate_measure(128, its, 3)
+            secondary["surrogate_train"] = {"metric": "U-Net training iterations per second (128^2, batch 8)",
+                                            "value": round(its / dt, 2), "unit": "iterations/s",
+                                            "ms_per_step": round(1e3 * dt / its, 3), "steps": its, "params": nparams,
+                                            "clocks": sclk}
+        except Exception as ex:
+            secondary["surrogate_train"] = {"error": str(ex)[:200]}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

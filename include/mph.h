@@ -354,8 +354,12 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
                 float* C, long long ldc, int accumulate, void* stream);
 /* GEMM kernel choice for later calls: 1 = mma.sync (m16n8k16) tiles, 2 =
  * tcgen05.mma with the accumulator in tensor memory (128 x 64 tiles, three
- * cp.async stages), 3 = the same single-buffered, 0 = mode 2 for M >= 128 and
- * N >= 16, else mma.sync.  Not thread-safe (process-wide setting). */
+ * cp.async stages), 3 = the same single-buffered, 4 = tcgen05.mma fed by TMA
+ * tensor copies (128 x 32/64/128 tiles, 64-wide K slices in 128-byte swizzled
+ * layout, four stages; for ta = tb = 0 with 16-byte aligned bases and row
+ * strides, mode 2 otherwise), 0 = automatic: mode 4 where it applies, else
+ * mode 2, for M >= 128 or K >= 1024 with N >= 16, else mma.sync.  Not
+ * thread-safe (process-wide setting). */
 int mph_nn_gemm_mode(int mode);
 /* Reads (and with reset != 0 clears) the flag the tcgen05 GEMM sets when a
  * bounded wait for its tensor-core work runs out. */
