@@ -7,8 +7,11 @@
 //   mph_batch_run <inputs file> [<inputs file> ...] [key=value ...]
 //
 // Every key=value override applies to every domain.  Extra keys:
-//   mph.precision  f64 | f64_fast | f32 | f16s | bf16s (default f64, the
-//                  reference's arithmetic; one precision for the batch)
+//   mph.precision  f64 | f64_fast | f64x | f32 | f16s | bf16s | f16c (default
+//                  f64, the reference's arithmetic; one precision for the
+//                  batch).  With f64x a domain whose populations leave the
+//                  fixed-point range stops there and is reported "diverged";
+//                  the others go on.
 //   mph.device     CUDA device (default 0)
 //   mph.tol        > 0: a domain also stops once the steady-state residual
 //                  (relative change of its velocity over mph.check_every
@@ -46,6 +49,7 @@ struct Domain {
     int last = 0;         // last loop step (max_step, or the stop-time bound)
     int done_step = -1;   // loop step at which the domain stopped (-1: running)
     double residual = NAN;
+    bool diverged = false;  // left the fixed-point range (f64x)
     std::string dir, plot_prefix;
 };
 
@@ -85,8 +89,7 @@ int main(int argc, char** argv) {
         if (i == 0) {
             prec_name = get(in, "mph.precision", "f64");
             prec = precision_code(prec_name);
-            if (prec < 0 || prec == MPH_PREC_F64X)
-                die("mph.precision must be one of f64 f64_fast f32 f16s bf16s for a batch");
+            if (prec < 0) die("mph.precision must be one of f64 f64_fast f64x f32 f16s bf16s f16c");
             device = std::atoi(get(in, "mph.device", "0").c_str());
             tol = std::atof(get(in, "mph.tol", "0").c_str());
             check_every = std::atoi(get(in, "mph.check_every", "100").c_str());
@@ -140,7 +143,19 @@ int main(int argc, char** argv) {
             if (tol > 0) next = std::min(next, (step + 1 + check_every) / check_every * check_every - 1);
         }
         if (next == INT_MAX) break;
-        ck(mph_batch_advance(b, next - step), "advance");
+        const int rc = mph_batch_advance(b, next - step);
+        if (rc == MPH_ERR_NONFINITE && prec == MPH_PREC_F64X) {
+            // domains that left the fixed-point range stop where they are
+            std::vector<int> flags(dom.size(), 0);
+            ck(mph_batch_range_flags(b, flags.data()), "range flags");
+            for (size_t i = 0; i < dom.size(); ++i)
+                if (flags[i] && dom[i].done_step < 0) {
+                    dom[i].done_step = next;
+                    dom[i].diverged = true;
+                }
+        } else {
+            ck(rc, "advance");
+        }
         step = next;
         if (tol > 0 && (step + 1) % check_every == 0) ck(mph_batch_residual(b, res.data()), "residual");
         for (size_t i = 0; i < dom.size(); ++i) {
@@ -162,6 +177,11 @@ int main(int argc, char** argv) {
     }
     for (size_t i = 0; i < dom.size(); ++i) {
         const Domain& m = dom[i];
+        if (m.diverged) {
+            std::cout << "domain " << i << " " << m.inputs << ": diverged (left the fixed-point range) by step "
+                      << m.done_step + 1 << "\n";
+            continue;
+        }
         std::cout << "domain " << i << " " << m.inputs << ": steps " << m.done_step + 1 << " residual "
                   << std::setprecision(6) << m.residual << (tol > 0 && m.residual < tol ? " converged" : "")
                   << " -> " << m.dir << "/final\n";

@@ -1,5 +1,5 @@
 """Argument handling of the host drivers (mph_batch_run, mph_run) that needs
-no GPU: usage, precisions they cannot take, missing inputs files."""
+no GPU: usage, an unknown precision, missing inputs files."""
 import os
 import subprocess
 
@@ -12,7 +12,7 @@ def test_usage_and_precision_errors(mph, tmp_path):
     assert os.access(exe, os.X_OK)
     r = subprocess.run([exe], capture_output=True, text=True)
     assert r.returncode == 2 and "usage" in r.stderr
-    r = subprocess.run([exe, INPUTS, "mph.precision=f64x"], cwd=tmp_path, capture_output=True, text=True)
+    r = subprocess.run([exe, INPUTS, "mph.precision=f128"], cwd=tmp_path, capture_output=True, text=True)
     assert r.returncode == 1 and "mph.precision" in r.stderr
     r = subprocess.run([exe, str(tmp_path / "missing.inputs")], cwd=tmp_path, capture_output=True, text=True)
     assert r.returncode == 1 and r.stderr.startswith("mph_batch_run:")

@@ -137,3 +137,30 @@ def test_batch_runner_stops_converged_domains(mph, tmp_path):
         rho, _ = s.update_macroscopic()
         got = np.load(tmp_path / "out" / f"domain{i:04d}" / "final" / "density.npy").reshape(-1)
         assert np.array_equal(got, rho * info.ref_density)
+
+
+def test_batch_runner_fixed_point_converges_and_drops_a_diverging_domain(mph, tmp_path):
+    """mph_batch_run in the FP64-accurate fixed point: a stable cavity stops at
+    its first residual check below 1e-8 with the fields of a single f64x
+    handle advanced as many steps, bit for bit, while a cavity at Re = 10^6
+    (tau within 1e-5 of 1/2, unstable) leaves the fixed-point range, is
+    reported as diverged and does not stop the run."""
+    exe = os.path.join(os.path.dirname(mph.__file__), "_build", "mph_batch_run")
+    files = [_inputs_variant(tmp_path / "a.inputs", **{"grid.ncells": "16 16", "units.Re": 10.0}),
+             _inputs_variant(tmp_path / "b.inputs", **{"grid.ncells": "24 24", "units.Re": 1.0e6})]
+    r = subprocess.run([exe, *files, f"mph.out={tmp_path / 'out'}", "mph.tol=1e-8", "mph.check_every=500",
+                        "sim.max_step=400000", "amr.plot_int=0", "mph.precision=f64x"], cwd=tmp_path,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lines = {int(ln.split()[1]): ln for ln in r.stdout.splitlines() if ln.startswith("domain ")}
+    assert "diverged" in lines[1], r.stdout
+    ln = lines[0].split()
+    steps = int(ln[ln.index("steps") + 1])
+    assert "converged" in ln and steps % 500 == 0 and float(ln[ln.index("residual") + 1]) < 1e-8
+    d, info = mph.InputParser(files[0], overrides=["sim.max_step=400000"]).derive("f64x")
+    s = mph.Simulation(d, info)
+    s.initialize()
+    s.advance(steps)
+    rho, _ = s.update_macroscopic()
+    got = np.load(tmp_path / "out" / "domain0000" / "final" / "density.npy").reshape(-1)
+    assert np.array_equal(got, rho * info.ref_density)
