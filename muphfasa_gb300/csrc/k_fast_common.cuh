@@ -30,18 +30,10 @@ cudaError_t launch_step_fast(int q, bool forced, const void* fin, void* fout, co
                 if (t == 64 || t == 128 || t == 256) threads = t;
             }
             step_shape(half, g, b, threads);  // one thread per cell pair
-            // MPH_PAIR_MINBLOCKS=4: the 64-register build (more warps, some spilling)
-            const char* mb = std::getenv("MPH_PAIR_MINBLOCKS");
-            const bool four = mb && std::atoi(mb) == 4;
-#define MPH_PAIR_CASE(QQ)                                                                       \
-    case QQ:                                                                                    \
-        if (four) {                                                                             \
-            if (forced) k_step_pair<QQ, St, true, 4><<<g, b, 0, s>>>(in, out, p, pg);           \
-            else k_step_pair<QQ, St, false, 4><<<g, b, 0, s>>>(in, out, p, pg);                 \
-        } else {                                                                                \
-            if (forced) k_step_pair<QQ, St, true><<<g, b, 0, s>>>(in, out, p, pg);              \
-            else k_step_pair<QQ, St, false><<<g, b, 0, s>>>(in, out, p, pg);                    \
-        }                                                                                       \
+#define MPH_PAIR_CASE(QQ)                                                              \
+    case QQ:                                                                           \
+        if (forced) k_step_pair<QQ, St, true><<<g, b, 0, s>>>(in, out, p, pg);         \
+        else k_step_pair<QQ, St, false><<<g, b, 0, s>>>(in, out, p, pg);               \
         return cudaGetLastError();
             switch (q) {
                 MPH_PAIR_CASE(9)

@@ -823,10 +823,10 @@ __global__ void __launch_bounds__(256) k_step(const typename St::T* __restrict__
 // (x, x+1), x even, with packed FP32x2 arithmetic.  Populations with c_x = 0
 // come from an aligned pair and are read as one 32-bit word; all stores are
 // 32-bit words.  (nx even makes every row, plane and population offset even.)
-// MINB: resident 256-thread blocks the registers are sized for (3: 80
-// registers, 24 warps per SM; 4: 64 registers with some spilling, 32 warps).
-template <int Q, class St, bool FORCED, int MINB = 3>
-__global__ void __launch_bounds__(256, MINB) k_step_pair(const typename St::T* __restrict__ fin,
+// Registers sized for 3 blocks of 256 threads (80: 24 warps per SM); a
+// 64-register build (32 warps, some spilling) measured 2 % slower.
+template <int Q, class St, bool FORCED>
+__global__ void __launch_bounds__(256, 3) k_step_pair(const typename St::T* __restrict__ fin,
                                                    typename St::T* __restrict__ fout, const KParams p,
                                                    const KParams* __restrict__ pg) {
     using L = Lat<Q>;

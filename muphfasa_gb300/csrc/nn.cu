@@ -786,12 +786,17 @@ __global__ void __launch_bounds__(256) k_colsum_part(const float* __restrict__ X
     }
 }
 
+// One warp per column: lane l adds the partials l, l + 32, ... in order, then
+// a fixed shuffle tree adds the lanes (the same order on every call).
 __global__ void k_colsum_final(const float* __restrict__ part, int nb, int C, float* __restrict__ out) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
     if (c >= C) return;
     float t = 0.f;
-    for (int b = 0; b < nb; ++b) t += part[(long long)b * C + c];
-    out[c] = t;
+    for (int b = lane; b < nb; b += 32) t += part[(long long)b * C + c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) out[c] = t;
 }
 
 // db[c] = sum_p dPre[p][c]: one block per channel group, fixed order.
@@ -1231,7 +1236,7 @@ int mph_nn_colsum(const float* X, long long P, int C, float* out, void* stream) 
         const long long rows = (P + kColsumBlocks - 1) / kColsumBlocks;
         const int nb = (int)((P + rows - 1) / rows);
         k_colsum_part<<<nb, 256, 0, s>>>(X, P, C, rows, g_colsum_ws);
-        k_colsum_final<<<(C + 255) / 256, 256, 0, s>>>(g_colsum_ws, nb, C, out);
+        k_colsum_final<<<(C + 7) / 8, 256, 0, s>>>(g_colsum_ws, nb, C, out);
         return ck("colsum");
     }
     k_colsum<<<C, 256, 0, s>>>(X, P, C, out);
