@@ -662,16 +662,26 @@ constexpr size_t tma_smem_bytes() {
 }
 
 // C[m][n] (+)= sum over splits z of W[z][m][n] (W rows of width N), in split order.
-__global__ void k_splitk_reduce(const float* __restrict__ W, int S, int M, int N, float* __restrict__ C, long long ldc,
-                                int accumulate) {
+// Blocks of 256 threads: 64 elements x 4 groups of consecutive splits; each
+// group adds its splits in order, then the four group sums are added in
+// group order (a fixed order: the result is the same on every call).
+__global__ void __launch_bounds__(256) k_splitk_reduce(const float* __restrict__ W, int S, int M, int N,
+                                                       float* __restrict__ C, long long ldc, int accumulate) {
+    __shared__ float part[4][64];
     const long long total = (long long)M * N;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        float s = 0.f;
-        for (int z = 0; z < S; ++z) s += W[(long long)z * total + i];
-        const long long m = i / N, n = i % N;
+    const int e = threadIdx.x & 63, grp = threadIdx.x >> 6;
+    const long long i = (long long)blockIdx.x * 64 + e;
+    const int per = (S + 3) / 4, z0 = grp * per, z1 = min(S, z0 + per);
+    float t = 0.f;
+    if (i < total)
+        for (int z = z0; z < z1; ++z) t += W[(long long)z * total + i];
+    part[grp][e] = t;
+    __syncthreads();
+    if (grp == 0 && i < total) {
+        const float sum = ((part[0][e] + part[1][e]) + part[2][e]) + part[3][e];
+        const long long m = i / N, n = i - m * N;
         float* p = C + m * ldc + n;
-        *p = accumulate ? *p + s : s;
+        *p = accumulate ? *p + sum : sum;
     }
 }
 
@@ -959,6 +969,37 @@ __global__ void __launch_bounds__(256) k_transpose_bf16(const unsigned short* __
     }
 }
 
+// The same for even rows and cols through 64 x 64 tiles moved as 32-bit words
+// (two BF16 values): a warp reads 128 B of an input row and writes 128 B of an
+// output row.  The tile is kept as 16-bit values with rows padded to an odd
+// number of words.
+__global__ void __launch_bounds__(256) k_transpose_bf16_w(const unsigned* __restrict__ X, long long rows, int cols,
+                                                          unsigned* __restrict__ Y) {
+    __shared__ unsigned short t[64][66];
+    const long long r0 = (long long)blockIdx.x * 64;
+    const int c0 = blockIdx.y * 64;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;  // 8 warps
+    const int hc = cols >> 1;                                     // words per input row
+    const long long hr = rows >> 1;                               // words per output row
+#pragma unroll
+    for (int i = 0; i < 64; i += 8) {
+        const long long r = r0 + warp + i;
+        const int wc = (c0 >> 1) + lane;
+        unsigned v = 0u;
+        if (r < rows && wc < hc) v = X[r * hc + wc];
+        t[warp + i][2 * lane] = (unsigned short)(v & 0xFFFFu);
+        t[warp + i][2 * lane + 1] = (unsigned short)(v >> 16);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 64; i += 8) {
+        const int c = c0 + warp + i;
+        const long long wr = (r0 >> 1) + lane;
+        if (c < cols && wr < hr)
+            Y[(long long)c * hr + wr] = (unsigned)t[2 * lane][warp + i] | ((unsigned)t[2 * lane + 1][warp + i] << 16);
+    }
+}
+
 // W2[ci][t Cout + co] = Wt[co][(8 - t) Cin + ci]: the weights of the data
 // gradient of a 3 x 3 convolution written as a convolution of dY with the
 // taps mirrored (t' = 8 - t) and the channel roles exchanged.
@@ -1166,7 +1207,7 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
                       : tma_bn == 64 ? launch_tma<64>(g, M, N, tA, tB, out, ldo, acc, K, kchunk, s)
                                      : launch_tma<128>(g, M, N, tA, tB, out, ldo, acc, K, kchunk, s);
         if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string("mph_nn_gemm (TMA): ") + cudaGetErrorString(e));
-        if (S > 1) k_splitk_reduce<<<grid_for((long long)M * N), 256, 0, s>>>(g_ws, S, M, N, C, ldc, accumulate);
+        if (S > 1) k_splitk_reduce<<<(unsigned)(((long long)M * N + 63) / 64), 256, 0, s>>>(g_ws, S, M, N, C, ldc, accumulate);
         return ck("gemm (tcgen05, TMA)");
     }
 #define MPH_GEMM_LAUNCH(KERN)                                                                                  \
@@ -1182,7 +1223,7 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
         MPH_GEMM_LAUNCH(k_gemm_bf16)
     }
 #undef MPH_GEMM_LAUNCH
-    if (S > 1) k_splitk_reduce<<<grid_for((long long)M * N), 256, 0, s>>>(g_ws, S, M, N, C, ldc, accumulate);
+    if (S > 1) k_splitk_reduce<<<(unsigned)(((long long)M * N + 63) / 64), 256, 0, s>>>(g_ws, S, M, N, C, ldc, accumulate);
     return ck(tc ? "gemm (tcgen05)" : "gemm (mma.sync)");
 }
 
@@ -1314,6 +1355,14 @@ int mph_nn_cast(int kind, const void* x, long long n, void* y, void* stream) {
 int mph_nn_transpose(const void* x, long long rows, int cols, void* y, void* stream) {
     if (!x || !y || rows <= 0 || cols <= 0 || (rows + 31) / 32 > 0x7fffffffLL || (cols + 31) / 32 > 65535)
         return mph::fail(MPH_ERR_ARG, "mph_nn_transpose: bad argument");
+    const bool words = rows % 2 == 0 && cols % 2 == 0 &&
+                       ((reinterpret_cast<unsigned long long>(x) | reinterpret_cast<unsigned long long>(y)) & 3) == 0;
+    if (words && (rows + 63) / 64 <= 0x7fffffffLL && (cols + 63) / 64 <= 65535) {
+        const dim3 grid((unsigned)((rows + 63) / 64), (unsigned)((cols + 63) / 64));
+        k_transpose_bf16_w<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const unsigned*>(x), rows,
+                                                                                cols, static_cast<unsigned*>(y));
+        return ck("transpose");
+    }
     const dim3 grid((unsigned)((rows + 31) / 32), (unsigned)((cols + 31) / 32));
     k_transpose_bf16<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const unsigned short*>(x), rows,
                                                                           cols, static_cast<unsigned short*>(y));

@@ -85,7 +85,7 @@ def _download_bf16(S, dev, n):
     return f.download(n)
 
 
-@pytest.mark.parametrize("rows,cols", [(1, 1), (37, 5), (4096, 288), (1000, 33)])
+@pytest.mark.parametrize("rows,cols", [(1, 1), (37, 5), (4096, 288), (1000, 33), (130, 70), (2, 2), (64, 4096)])
 def test_transpose_bf16(rows, cols, S):
     rng = np.random.default_rng(rows + cols)
     x = NO.to_bf16(rng.standard_normal((rows, cols)).astype(np.float32))
