@@ -142,12 +142,14 @@ def test_batch_runner_stops_converged_domains(mph, tmp_path):
 def test_batch_runner_fixed_point_converges_and_drops_a_diverging_domain(mph, tmp_path):
     """mph_batch_run in the FP64-accurate fixed point: a stable cavity stops at
     its first residual check below 1e-8 with the fields of a single f64x
-    handle advanced as many steps, bit for bit, while a cavity at Re = 10^6
-    (tau within 1e-5 of 1/2, unstable) leaves the fixed-point range, is
-    reported as diverged and does not stop the run."""
+    handle advanced as many steps, bit for bit, while a cavity with tau =
+    0.5001 at Re = 72 000 (lid at 0.1 in lattice units, a grid Reynolds number
+    of 3000: unstable) leaves the fixed-point range, is reported as diverged
+    and does not stop the run."""
     exe = os.path.join(os.path.dirname(mph.__file__), "_build", "mph_batch_run")
     files = [_inputs_variant(tmp_path / "a.inputs", **{"grid.ncells": "16 16", "units.Re": 10.0}),
-             _inputs_variant(tmp_path / "b.inputs", **{"grid.ncells": "24 24", "units.Re": 1.0e6})]
+             _inputs_variant(tmp_path / "b.inputs", **{"grid.ncells": "24 24", "lbm.tau": 0.5001,
+                                                       "units.Re": 72000.0})]
     r = subprocess.run([exe, *files, f"mph.out={tmp_path / 'out'}", "mph.tol=1e-8", "mph.check_every=500",
                         "sim.max_step=400000", "amr.plot_int=0", "mph.precision=f64x"], cwd=tmp_path,
                        capture_output=True, text=True)
