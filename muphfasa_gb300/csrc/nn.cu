@@ -662,10 +662,25 @@ constexpr size_t tma_smem_bytes() {
 }
 
 // C[m][n] (+)= sum over splits z of W[z][m][n] (W rows of width N), in split order.
-// Blocks of 256 threads: 64 elements x 4 groups of consecutive splits; each
-// group adds its splits in order, then the four group sums are added in
-// group order (a fixed order: the result is the same on every call).
-__global__ void __launch_bounds__(256) k_splitk_reduce(const float* __restrict__ W, int S, int M, int N,
+// C[m][n] (+)= sum over splits z of W[z][m][n], in split order (few splits).
+__global__ void k_splitk_reduce(const float* __restrict__ W, int S, int M, int N, float* __restrict__ C, long long ldc,
+                                int accumulate) {
+    const long long total = (long long)M * N;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int z = 0; z < S; ++z) s += W[(long long)z * total + i];
+        const long long m = i / N, n = i % N;
+        float* p = C + m * ldc + n;
+        *p = accumulate ? *p + s : s;
+    }
+}
+
+// Many splits (the weight gradients, K = pixels): blocks of 256 threads, 64
+// elements x 4 groups of consecutive splits; each group adds its splits in
+// order, then the four group sums are added in group order (a fixed order:
+// the result is the same on every call).
+__global__ void __launch_bounds__(256) k_splitk_reduce4(const float* __restrict__ W, int S, int M, int N,
                                                        float* __restrict__ C, long long ldc, int accumulate) {
     __shared__ float part[4][64];
     const long long total = (long long)M * N;
@@ -775,23 +790,26 @@ __global__ void k_act_bwd(const float* __restrict__ dOut, int ld_dout, int c_off
     }
 }
 
-// Column sums in two fixed-order passes, for C dividing 256: block b sums the
-// rows of its slice (each thread keeps one column, t mod C, since 256 is a
-// multiple of C), then part[b][c]; k_colsum_final adds the blocks in order.
+// Column sums in two fixed-order passes, for C <= 256: block b sums the rows
+// of its slice with T = floor(256 / C) C threads, each keeping one column
+// (t mod C, since the stride T is a multiple of C), then part[b][c];
+// k_colsum_final adds the blocks in order.
 __global__ void __launch_bounds__(256) k_colsum_part(const float* __restrict__ X, long long P, int C, long long rows,
                                                      float* __restrict__ part) {
+    const int T = (256 / C) * C;
     const long long r0 = (long long)blockIdx.x * rows;
     const long long r1 = min(P, r0 + rows);
     const float* x = X + r0 * C;
     const long long n = (r1 > r0 ? r1 - r0 : 0) * C;
     float s = 0.f;
-    for (long long j = threadIdx.x; j < n; j += 256) s += x[j];
+    if ((int)threadIdx.x < T)
+        for (long long j = threadIdx.x; j < n; j += T) s += x[j];
     __shared__ float sh[256];
     sh[threadIdx.x] = s;
     __syncthreads();
-    if (threadIdx.x < C) {
+    if ((int)threadIdx.x < C) {
         float t = 0.f;
-        for (int k = threadIdx.x; k < 256; k += C) t += sh[k];
+        for (int k = threadIdx.x; k < T; k += C) t += sh[k];
         part[(long long)blockIdx.x * C + threadIdx.x] = t;
     }
 }
@@ -1150,8 +1168,15 @@ int mph_nn_status(int* timeout, int reset) {
 
 // Split-K workspace, grown on demand (the weight gradients have a small
 // output and K = the pixel count).
+static void splitk_reduce(int S, int M, int N, float* C, long long ldc, int accumulate, cudaStream_t s);
 static float* g_ws = nullptr;
 static size_t g_ws_bytes = 0;
+
+static void splitk_reduce(int S, int M, int N, float* C, long long ldc, int accumulate, cudaStream_t s) {
+    const long long total = (long long)M * N;
+    if (S > 4) k_splitk_reduce4<<<(unsigned)((total + 63) / 64), 256, 0, s>>>(g_ws, S, M, N, C, ldc, accumulate);
+    else k_splitk_reduce<<<grid_for(total), 256, 0, s>>>(g_ws, S, M, N, C, ldc, accumulate);
+}
 
 int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const void* B, long long ldb, int tb,
                 float* C, long long ldc, int accumulate, void* stream) {
@@ -1207,7 +1232,7 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
                       : tma_bn == 64 ? launch_tma<64>(g, M, N, tA, tB, out, ldo, acc, K, kchunk, s)
                                      : launch_tma<128>(g, M, N, tA, tB, out, ldo, acc, K, kchunk, s);
         if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string("mph_nn_gemm (TMA): ") + cudaGetErrorString(e));
-        if (S > 1) k_splitk_reduce<<<(unsigned)(((long long)M * N + 63) / 64), 256, 0, s>>>(g_ws, S, M, N, C, ldc, accumulate);
+        if (S > 1) splitk_reduce(S, M, N, C, ldc, accumulate, s);
         return ck("gemm (tcgen05, TMA)");
     }
 #define MPH_GEMM_LAUNCH(KERN)                                                                                  \
@@ -1223,7 +1248,7 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
         MPH_GEMM_LAUNCH(k_gemm_bf16)
     }
 #undef MPH_GEMM_LAUNCH
-    if (S > 1) k_splitk_reduce<<<(unsigned)(((long long)M * N + 63) / 64), 256, 0, s>>>(g_ws, S, M, N, C, ldc, accumulate);
+    if (S > 1) splitk_reduce(S, M, N, C, ldc, accumulate, s);
     return ck(tc ? "gemm (tcgen05)" : "gemm (mma.sync)");
 }
 
@@ -1269,7 +1294,7 @@ static constexpr int kColsumBlocks = 608;
 
 int mph_nn_colsum(const float* X, long long P, int C, float* out, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (C > 0 && C <= 256 && 256 % C == 0 && P >= 256) {
+    if (C > 0 && C <= 256 && P >= 256) {
         if (!g_colsum_ws) {
             const cudaError_t e = cudaMalloc(&g_colsum_ws, sizeof(float) * kColsumBlocks * 256);
             if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string("mph_nn_colsum: ") + cudaGetErrorString(e));

@@ -130,7 +130,7 @@ def test_im2col_16_byte_path(Cc, S):
     assert np.array_equal(got, NO.Net.im2col(x))
 
 
-@pytest.mark.parametrize("P,Cc", [(131072, 32), (2048, 256), (300, 64), (4096, 3), (100, 8)])
+@pytest.mark.parametrize("P,Cc", [(131072, 32), (2048, 256), (300, 64), (4096, 3), (100, 8), (5000, 96), (131072, 3)])
 def test_colsum(P, Cc, S):
     rng = np.random.default_rng(P + Cc)
     x = rng.standard_normal((P, Cc)).astype(np.float32)
