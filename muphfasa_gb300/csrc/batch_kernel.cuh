@@ -87,14 +87,17 @@ __global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __rest
                 if (oka[j]) {
                     int x, y, z;
                     chunk_cell(p, ch, l, x, y, z);
-                    const Nbr oa = neighbours<L::D>(p, x, y, z), ob = neighbours<L::D>(p, x + 1, y, z);
+                    const Nbr oa = neighbours<L::D>(p, x, y, z);
+                    // cell x + 1 pulls through a's offsets except for the x
+                    // wrap (as in k_step_pair)
+                    const int dxm = x == 0 ? -p.nx : 0, dxp = x + 2 == p.nx ? -p.nx : 0;
 #pragma unroll
                     for (int n = 0; n < Q; ++n) {
                         const unsigned ea = (unsigned)n * N + (unsigned)(ca[j] + upstream<Q>(oa, n));
                         if (L::cx(n) == 0) {
                             g[j][n] = St::ldr2(fin, ea);
                         } else {
-                            const unsigned eb = (unsigned)n * N + (unsigned)(ca[j] + 1 + upstream<Q>(ob, n));
+                            const unsigned eb = ea + 1u + (unsigned)(L::cx(n) == 1 ? dxm : dxp);
                             g[j][n] = make_float2(St::ldr1(fin, ea), St::ldr1(fin, eb));
                         }
                     }

@@ -841,16 +841,23 @@ __global__ void __launch_bounds__(256, 3) k_step_pair(const typename St::T* __re
         step_cell<Q, St, kFast, FORCED>(p, pg, fin, fout, x + 1, y, z);
         return;
     }
-    const Nbr oa = neighbours<L::D>(p, x, y, z), ob = neighbours<L::D>(p, x + 1, y, z);
+    const Nbr oa = neighbours<L::D>(p, x, y, z);
+    // Cell b = x + 1 shares y, z with cell a, so its upstream offsets equal
+    // a's except for the x wrap: c_x = +1 pulls from x, which for a at x = 0
+    // wrapped by nx; c_x = -1 wraps by -nx for b at nx - 1.  When a is not
+    // next to a face, b is next to one only if it is the last cell of a row
+    // with non-periodic x faces.
+    const bool b_xface = !p.periodic[0] && x + 2 == p.nx;
+    const int dxm = x == 0 ? -p.nx : 0, dxp = x + 2 == p.nx ? -p.nx : 0;
     float2 g[Q];
-    if (!oa.wall && !ob.wall) {
+    if (!oa.wall && !b_xface) {
 #pragma unroll
         for (int n = 0; n < Q; ++n) {
             const unsigned ea = (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(oa, n));
             if (L::cx(n) == 0) {
                 g[n] = St::ldr2(fin, ea);
             } else {
-                const unsigned eb = (unsigned)n * N + (unsigned)((int)ci + 1 + upstream<Q>(ob, n));
+                const unsigned eb = ea + 1u + (unsigned)(L::cx(n) == 1 ? dxm : dxp);
                 g[n] = make_float2(St::ldr1(fin, ea), St::ldr1(fin, eb));
             }
         }
