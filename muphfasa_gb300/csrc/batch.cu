@@ -37,25 +37,24 @@ using namespace mph;
 
 namespace {
 
-// dpx, kbb and flag are used by the fixed-point precision only; pf selects
-// the prefetching kernel of the 16-bit storages (K = 2, persistent).
+// dpx, kbb and flag are used by the fixed-point precision only.
 cudaError_t launch_batch(int prec, int q, bool forced, int K, bool P, const void* fin, void* fout, const Chunk* chunks,
                          int nchunks, const int2* walls, int nwalls, const KParams* dp, const long long* offs,
-                         const KParamsX* dpx, const long long* kbb, int* flag, cudaStream_t s, bool pf = false) {
+                         const KParamsX* dpx, const long long* kbb, int* flag, cudaStream_t s) {
     switch (prec) {
         case MPH_PREC_F64X:
             return launch_batch_f64x(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, dpx, offs, kbb,
                                      flag, s);
         case MPH_PREC_F64:
-            return launch_batch_exact(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s, false);
+            return launch_batch_exact(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
         case MPH_PREC_F64_FAST:
-            return launch_batch_fast_f64(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s, false);
-        case MPH_PREC_F32: return launch_batch_f32(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s, false);
-        case MPH_PREC_F16S: return launch_batch_f16s(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s, pf);
+            return launch_batch_fast_f64(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
+        case MPH_PREC_F32: return launch_batch_f32(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
+        case MPH_PREC_F16S: return launch_batch_f16s(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
         case MPH_PREC_BF16S:
-            return launch_batch_bf16s(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s, pf);
+            return launch_batch_bf16s(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
         case MPH_PREC_F16C:
-            return launch_batch_f16c(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s, pf);
+            return launch_batch_f16c(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -83,15 +82,14 @@ size_t elem_of(int prec) {
 // slower than the direct kernels (the 16-bit step is bound by instruction
 // issue, and staging adds instructions), so the autotuner does not time it.
 constexpr int kCells[3] = {1, 2, 4};
-constexpr int kCands = 8;
+constexpr int kCands = 7;
 constexpr int kBulkCand = 6;
-constexpr int kPfCand = 7;  // 16-bit storages: K = 2, persistent, prefetching the next chunk
 constexpr int kBulkCells = 512;  // cells per row chunk of the staged kernel
 constexpr int kBulkStages = 3;
 
 bool shifted(int prec) { return prec == MPH_PREC_F16S || prec == MPH_PREC_BF16S || prec == MPH_PREC_F16C; }
 bool candidate_ok(int prec, int cand) {
-    if (cand == kBulkCand || cand == kPfCand) return shifted(prec);
+    if (cand == kBulkCand) return shifted(prec);
     if (shifted(prec)) return cand % 3 != 0;
     if (prec == MPH_PREC_F64X) return cand % 3 != 2;
     return true;
@@ -320,10 +318,9 @@ int step_once(mph_batch* b, int cand) {
         std::swap(b->fa, b->fb);
         return MPH_OK;
     }
-    const int ki = cand == kPfCand ? 1 : cand % 3;
+    const int ki = cand % 3;
     MPH_CK(launch_batch(b->prec, b->q, b->forced, kCells[ki], cand >= 3, b->fa, b->fb, b->d_chunks[ki], b->nchunks[ki],
-                        b->d_walls, b->nwalls, b->d_params, b->d_offs, b->d_px, b->d_kbb, b->d_flag, b->stream,
-                        cand == kPfCand),
+                        b->d_walls, b->nwalls, b->d_params, b->d_offs, b->d_px, b->d_kbb, b->d_flag, b->stream),
            "batch step launch");
     std::swap(b->fa, b->fb);
     return MPH_OK;
@@ -339,7 +336,7 @@ int autotune(mph_batch* b) {
     if (const char* env = std::getenv("MPH_BATCH_CANDIDATE")) {
         const int c = std::atoi(env);
         if (c < 0 || c >= kCands || !candidate_ok(b->prec, c) || (c == kBulkCand && !b->bulk_ok))
-            return fail(MPH_ERR_ARG, "MPH_BATCH_CANDIDATE must be 0..7 (1, 2, 4, 5, 6, 7 for 16-bit storage; "
+            return fail(MPH_ERR_ARG, "MPH_BATCH_CANDIDATE must be 0..6 (1, 2, 4, 5 and 6 for 16-bit storage; "
                                      "0, 1, 3, 4 for fixed point; 0..5 otherwise)");
         b->k_idx = c;
         return ensure_chunks(b, c % 3);

@@ -173,126 +173,6 @@ __global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __rest
     }
 }
 
-// Prefetching persistent kernel for the shifted 16-bit policies (chunks of
-// 512 cells, the K = 2 list): a thread owns the cell pair (2t, 2t + 1) of each
-// chunk it visits and keeps a two-deep pipeline, so the HBM latency of a
-// chunk's loads overlaps the collide of the previous one without more cells
-// per thread:
-//   iteration i: issue the 16-bit loads of chunk i + 1 (its geometry was read
-//   one iteration earlier), read the geometry of chunk i + 2, collide and store
-//   chunk i from the values loaded during iteration i - 1.
-// Values are loaded as raw 16-bit words (the two cells of a pair may lie in
-// different rows when nx is odd) and decoded with the policy's own
-// conversion, so every cell gets the bits of k_batch_step.
-struct ChunkGeom {
-    int c0, x0, yz, nx, ny, nz, per;  // per: periodic flags, bit a for axis a
-    unsigned N;
-    float inx, iny;
-    long long off;
-};
-
-__device__ __forceinline__ ChunkGeom chunk_geom(const Chunk* __restrict__ chunks, const KParams* __restrict__ dp,
-                                                const long long* __restrict__ offs, int ci) {
-    const Chunk ch = chunks[ci];
-    const KParams& p = dp[ch.dom];
-    ChunkGeom g;
-    g.c0 = ch.c0;
-    g.x0 = ch.x0;
-    g.yz = ch.yz;
-    g.nx = p.nx;
-    g.ny = p.ny;
-    g.nz = p.nz;
-    g.per = (p.periodic[0] ? 1 : 0) | (p.periodic[1] ? 2 : 0) | (p.periodic[2] ? 4 : 0);
-    g.N = (unsigned)p.ncell;
-    g.inx = p.inv_nx_f;
-    g.iny = p.inv_ny_f;
-    g.off = offs[ch.dom];
-    return g;
-}
-
-// Raw 16-bit values of the cell pair of this thread in the chunk of `g`:
-// v[n] = value of cell 2t (low half) | value of cell 2t + 1 (high half).
-template <int Q, class St>
-__device__ __forceinline__ void pair_load(const typename St::T* __restrict__ fin_base, const ChunkGeom& g,
-                                          unsigned* v) {
-    using L = Lat<Q>;
-    KParams q;  // the fields chunk_cell and neighbours read
-    q.nx = g.nx;
-    q.ny = g.ny;
-    q.nz = g.nz;
-    q.periodic[0] = g.per & 1;
-    q.periodic[1] = (g.per >> 1) & 1;
-    q.periodic[2] = (g.per >> 2) & 1;
-    q.inv_nx_f = g.inx;
-    q.inv_ny_f = g.iny;
-    const Chunk ch{0, g.c0, g.x0, g.yz};
-    const unsigned short* fin = reinterpret_cast<const unsigned short*>(fin_base + g.off);
-    const int l = 2 * threadIdx.x;
-    const int ca = g.c0 + l;
-    const bool oka = ca < (int)g.N, okb = ca + 1 < (int)g.N;
-    int xa = 0, ya = 0, za = 0, xb = 0, yb = 0, zb = 0;
-    if (oka) chunk_cell(q, ch, l, xa, ya, za);
-    if (okb) chunk_cell(q, ch, l + 1, xb, yb, zb);
-    const Nbr oa = neighbours<L::D>(q, xa, ya, za), ob = neighbours<L::D>(q, xb, yb, zb);
-#pragma unroll
-    for (int n = 0; n < Q; ++n) {
-        unsigned va = 0u, vb = 0u;
-        if (oka) va = __ldg(fin + ((unsigned)n * g.N + (unsigned)(ca + upstream<Q>(oa, n))));
-        if (okb) vb = __ldg(fin + ((unsigned)n * g.N + (unsigned)(ca + 1 + upstream<Q>(ob, n))));
-        v[n] = va | (vb << 16);
-    }
-}
-
-template <int Q, class St, bool FORCED>
-__global__ void __launch_bounds__(256, 3) k_batch_pair_pf(const typename St::T* __restrict__ fin_base,
-                                                          typename St::T* __restrict__ fout_base,
-                                                          const Chunk* __restrict__ chunks, int nchunks,
-                                                          const KParams* __restrict__ dp,
-                                                          const long long* __restrict__ offs) {
-    const int G = gridDim.x;
-    int ci = blockIdx.x;
-    if (ci >= nchunks) return;
-    unsigned cur[Q], nxt[Q];
-    ChunkGeom gc = chunk_geom(chunks, dp, offs, ci);
-    pair_load<Q, St>(fin_base, gc, cur);
-    ChunkGeom gn = gc;
-    if (ci + G < nchunks) gn = chunk_geom(chunks, dp, offs, ci + G);
-    for (; ci < nchunks; ci += G) {
-        const bool more = ci + G < nchunks;
-        if (more) pair_load<Q, St>(fin_base, gn, nxt);
-        ChunkGeom gnn = gn;
-        if (ci + 2 * G < nchunks) gnn = chunk_geom(chunks, dp, offs, ci + 2 * G);
-        // collide and store chunk ci
-        const int dom = chunks[ci].dom;
-        const KParams& p = dp[dom];
-        typename St::T* fout = fout_base + gc.off;
-        const int ca = gc.c0 + 2 * (int)threadIdx.x;
-        const bool oka = ca < (int)gc.N, okb = ca + 1 < (int)gc.N;
-        if (oka) {
-            float2 g[Q];
-#pragma unroll
-            for (int n = 0; n < Q; ++n) g[n] = make_float2(St::dec1(cur[n] & 0xFFFFu), St::dec1(okb ? cur[n] >> 16 : cur[n] & 0xFFFFu));
-            collide_shift<Q, A2, FORCED>(p, g);
-#pragma unroll
-            for (int n = 0; n < Q; ++n) {
-                const unsigned e = (unsigned)n * gc.N + (unsigned)ca;
-                if (okb && (e & 1u) == 0) {
-                    St::str2(fout, e, g[n]);
-                } else {
-                    St::str1(fout, e, g[n].x);
-                    if (okb) St::str1(fout, e + 1, g[n].y);
-                }
-            }
-        }
-        if (more) {
-#pragma unroll
-            for (int n = 0; n < Q; ++n) cur[n] = nxt[n];
-        }
-        gc = gn;
-        gn = gnn;
-    }
-}
-
 // Cells next to a non-periodic face: {domain, linear cell index}, one per
 // thread, with the boundary rules (runs after k_batch_step on the same
 // stream and overwrites those cells).
@@ -335,11 +215,10 @@ int persistent_grid(Kern k) {
 // Cells per thread offered to the autotuner: K in {1, 2, 4} (pairs only for
 // the shifted policies), one chunk per block or a persistent grid.  Launches
 // the chunk kernel, then the wall cells.
-// prefetch (16-bit storages, K = 2, persistent): the prefetching kernel k_batch_pair_pf.
 template <class St, int ARITH>
 cudaError_t launch_batch_t(int q, bool forced, int K, bool persistent, const void* fin, void* fout,
                            const Chunk* chunks, int nchunks, const int2* walls, int nwalls, const KParams* dp,
-                           const long long* offs, cudaStream_t s, bool prefetch = false) {
+                           const long long* offs, cudaStream_t s) {
     return batch_with_q(q, [&](auto qc) {
         constexpr int Q = decltype(qc)::value;
         auto in = static_cast<const typename St::T*>(fin);
@@ -356,15 +235,8 @@ cudaError_t launch_batch_t(int q, bool forced, int K, bool persistent, const voi
         kern<<<grid, 256, 0, s>>>(in, out, chunks, nchunks, dp, offs);                                         \
     }
         if (K == 4) { MPH_BK(4) }
-        else if (K == 2 && !(persistent && St::kShift && prefetch)) { MPH_BK(2) }
-        else if (K == 2) {
-            if constexpr (St::kShift) {
-                auto kern = forced ? k_batch_pair_pf<Q, St, true> : k_batch_pair_pf<Q, St, false>;
-                const int g = persistent_grid(kern);
-                if (g <= 0) return cudaErrorInvalidConfiguration;
-                kern<<<g < nchunks ? g : nchunks, 256, 0, s>>>(in, out, chunks, nchunks, dp, offs);
-            }
-        } else {
+        else if (K == 2) { MPH_BK(2) }
+        else {
             if constexpr (St::kShift) return cudaErrorInvalidValue;
             else { MPH_BK(1) }
         }
@@ -386,7 +258,7 @@ cudaError_t launch_batch_t(int q, bool forced, int K, bool persistent, const voi
 #define MPH_DECL_BATCH(NAME)                                                                                  \
     cudaError_t NAME(int q, bool forced, int K, bool persistent, const void* fin, void* fout, const Chunk* chunks, \
                      int nchunks, const int2* walls, int nwalls, const KParams* dp, const long long* offs,        \
-                     cudaStream_t s, bool prefetch);
+                     cudaStream_t s);
 MPH_DECL_BATCH(launch_batch_exact)
 MPH_DECL_BATCH(launch_batch_fast_f64)
 MPH_DECL_BATCH(launch_batch_f32)

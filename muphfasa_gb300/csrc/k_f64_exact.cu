@@ -351,8 +351,8 @@ cudaError_t launch_bc_fill_arr(int dim, int q, const int dlo[3], const int dhi[3
 
 cudaError_t launch_batch_exact(int q, bool forced, int K, bool persistent, const void* fin, void* fout, const Chunk* chunks, int nchunks,
                                const int2* walls, int nwalls, const KParams* dp, const long long* offs,
-                               cudaStream_t s, bool prefetch) {
-    return launch_batch_t<StF64, kExact>(q, forced, K, persistent, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s, prefetch);
+                               cudaStream_t s) {
+    return launch_batch_t<StF64, kExact>(q, forced, K, persistent, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
 }
 
 }  // namespace mph

@@ -15,8 +15,8 @@ cudaError_t launch_step_bulk_bf16s(int mode, int q, bool forced, const void* fin
     return launch_step_bulk_t<StBF16S>(mode, q, forced, fin, fout, p, pg, total_elems, cells, stages, flag, s);
 }
 cudaError_t launch_batch_bf16s(int q, bool forced, int K, bool persistent, const void* fin, void* fout, const Chunk* chunks, int nchunks,
-                       const int2* walls, int nwalls, const KParams* dp, const long long* offs, cudaStream_t s, bool prefetch) {
-    return launch_batch_t<StBF16S, kFast>(q, forced, K, persistent, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s, prefetch);
+                       const int2* walls, int nwalls, const KParams* dp, const long long* offs, cudaStream_t s) {
+    return launch_batch_t<StBF16S, kFast>(q, forced, K, persistent, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
 }
 cudaError_t launch_batch_bulk_bf16s(int mode, int q, bool forced, int stages, int lpad, const void* fin, void* fout,
                                    const RowChunk* chunks, int nchunks, const int2* walls, int nwalls,
