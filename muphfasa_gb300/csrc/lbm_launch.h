@@ -101,15 +101,6 @@ cudaError_t launch_step_f64x_pipe(int q, bool forced, const long long* fin, long
                                   const KParamsX& px, const KParams* pg, const long long* kbb, int* flag,
                                   int ctas, cudaStream_t s);
 
-// ---- k_f64x_bulk.cu (the fixed-point step with bulk-copy staging) -------
-// mode 0 prepares the kernel (once per handle, before any launch or stream
-// capture), mode 1 launches one step over the window of p; stages 2 or 3;
-// flag |= 1 on a range error, |= 2 on a wait timeout.  cudaErrorNotSupported
-// where it does not apply (obstacles): use launch_step_f64x then.
-cudaError_t launch_step_f64x_bulk(int mode, int q, bool forced, const long long* fin, long long* fout, const KParams& p,
-                                  const KParamsX& px, const KParams* pg, const long long* kbb, int* flag, int stages,
-                                  cudaStream_t s);
-
 // ---- monitor.cu (steady-state residual, FP64) ---------------------------
 // out2 = {sum |u - u_prev|^2, sum |u|^2} of the stored-population velocity;
 // u_prev (dim x ncell doubles) is overwritten with u.

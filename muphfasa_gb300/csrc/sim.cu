@@ -24,7 +24,6 @@ struct mph_sim {
     long long* d_kbb = nullptr;  // fixed-point bounce-back constants [27][27]
     int* d_flag = nullptr;       // range flag of the fixed-point step (1), wait timeout of a staged step (2)
     int pipe_ctas = 0;           // resident CTAs of the pipelined fixed-point kernel (0: direct kernel)
-    int xbulk_stages = 0;        // fixed point: stages of the bulk-copy staged step (0: direct kernel)
     int bulk_stages = 0;         // 16-bit storage: shared-memory stages of the bulk-copy step (0: direct kernel)
     int bulk_cells = 512;        // cells per chunk of the bulk-copy step
     size_t elem = 8;          // bytes per stored population value
@@ -353,12 +352,6 @@ cudaError_t launch_step_window(mph_sim* s, const KParams& kp, bool whole) {
             return launch_step_fast_f16c(q, forced, s->fa, s->fb, kp, s->d_kp, s->stream);
         }
         case MPH_PREC_F64X:
-            if (s->xbulk_stages > 0) {
-                const cudaError_t e = launch_step_f64x_bulk(1, q, forced, (const long long*)s->fa, (long long*)s->fb, kp,
-                                                            s->kpx, s->d_kp, s->d_kbb, s->d_flag, s->xbulk_stages,
-                                                            s->stream);
-                if (e != cudaErrorNotSupported) return e;
-            }
             if (whole && s->pipe_ctas > 0)
                 return launch_step_f64x_pipe(q, forced, (const long long*)s->fa, (long long*)s->fb, kp, s->kpx,
                                              s->d_kp, s->d_kbb, s->d_flag, s->pipe_ctas, s->stream);
@@ -767,22 +760,6 @@ int mph_create(const mph_desc* desc, mph_sim** out) {
         // vs 16.5 GLUPS at 512^3 D3Q19), or the persistent cp.async pipeline
         // with MPH_F64X_KERNEL=pipe.
         const char* kv = std::getenv("MPH_F64X_KERNEL");
-        if (e == cudaSuccess && kv && std::strcmp(kv, "bulk") == 0) {
-            // the step with bulk-copy staging of its pull operands
-            s->xbulk_stages = 2;
-            if (const char* v = std::getenv("MPH_BULK_STAGES")) s->xbulk_stages = std::atoi(v);
-            if (s->xbulk_stages < 2 || s->xbulk_stages > 3) {
-                free_all(s);
-                delete s;
-                return fail(MPH_ERR_ARG, "mph_create: MPH_BULK_STAGES must be 2 or 3");
-            }
-            e = launch_step_f64x_bulk(0, d.q, d.forced != 0, nullptr, nullptr, s->kp, s->kpx, nullptr, nullptr,
-                                      nullptr, s->xbulk_stages, nullptr);
-            if (e == cudaErrorNotSupported) {  // does not apply to this domain: the direct kernel
-                s->xbulk_stages = 0;
-                e = cudaSuccess;
-            }
-        }
         if (e == cudaSuccess && kv && std::strcmp(kv, "pipe") == 0) {
             s->pipe_ctas = f64x_pipe_ctas(d.q, d.forced != 0);
             if (s->pipe_ctas <= 0) {

@@ -108,67 +108,3 @@ def test_bulk_step_rejects_bad_settings(mph):
     with pytest.raises(mph.MphError) as e:
         _sim(mph, d, True, stages=4)
     assert e.value.code == 1
-
-
-def _state(mph, s):
-    """The populations in the handle's own storage format (raw bytes)."""
-    import ctypes as C
-    n = C.c_longlong()
-    mph.check(mph.lib().mph_state_bytes(s._h, C.byref(n)))
-    raw = np.empty(n.value, np.uint8)
-    mph.check(mph.lib().mph_get_state(s._h, raw.ctypes.data, n.value))
-    return raw
-
-
-def _simx(mph, desc, bulk, stages=2):
-    keys = ("MPH_F64X_KERNEL", "MPH_BULK_STAGES")
-    old = {k: os.environ.get(k) for k in keys}
-    try:
-        if bulk:
-            os.environ["MPH_F64X_KERNEL"] = "bulk"
-            os.environ["MPH_BULK_STAGES"] = str(stages)
-        else:
-            os.environ.pop("MPH_F64X_KERNEL", None)
-        return mph.Simulation(desc)
-    finally:
-        for k, v in old.items():
-            if v is None:
-                os.environ.pop(k, None)
-            else:
-                os.environ[k] = v
-
-
-@pytest.mark.parametrize("stages", [2, 3])
-@pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}_{'x'.join(map(str, c[1]))}" for c in CASES])
-def test_fixed_point_bulk_step_equals_direct_step(case, stages, mph):
-    """The fixed-point step with bulk-copy staging (MPH_F64X_KERNEL=bulk, row
-    segments of 128 cells) against the direct k_step_x: the same integers after
-    many steps on every lattice and boundary set of the 16-bit cases."""
-    d = _desc(mph, case, "f64x")
-    dim = 2 if case[0] == "D2Q9" else 3
-    a, b = _simx(mph, d, False), _simx(mph, d, True, stages)
-    _init(a, case[1], dim, 5)
-    _init(b, case[1], dim, 5)
-    a.advance(41)
-    b.advance(41)
-    assert np.array_equal(_state(mph, a), _state(mph, b))
-
-
-def test_fixed_point_bulk_step_long_rows_and_host_slabs(mph):
-    """Rows longer than a segment (300 cells: two full segments and a partial
-    one, periodic x wrap inside the first and last), a 3-D channel, and the
-    slab windows of mph_step_host."""
-    case = ("D3Q19", (300, 24, 20), ["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic", "Periodic"],
-            (1e-5, 0, 0), None, None)
-    d = _desc(mph, case, "f64x")
-    a, b = _simx(mph, d, False), _simx(mph, d, True)
-    _init(a, case[1], 3, 9)
-    _init(b, case[1], 3, 9)
-    a.advance(30)
-    b.advance(30)
-    assert np.array_equal(_state(mph, a), _state(mph, b))
-    f = a.f()
-    out_a, out_b = np.empty_like(f), np.empty_like(f)
-    a.step_host(f, out_a, 2)
-    b.step_host(f, out_b, 2)
-    assert np.array_equal(out_a, out_b)
