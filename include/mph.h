@@ -348,8 +348,9 @@ int mph_nn_sync(void* stream);
 /* C (float, ldc) [+]= A . B on the tensor cores, BF16 operands, FP32
  * accumulation: A(m, k) = ta ? A[k lda + m] : A[m lda + k],
  * B(k, n) = tb ? B[k ldb + n] : B[n ldb + k].  GEMMs with few output tiles
- * split K into one process-wide FP32 workspace (a deterministic reduce
- * follows): calls that may split must be ordered on one stream. */
+ * split K into an FP32 workspace of the current device (a deterministic
+ * reduce follows): calls on one device that may split must be ordered on
+ * one stream.  (mph_nn_colsum keeps a per-device workspace the same way.) */
 int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const void* B, long long ldb, int tb,
                 float* C, long long ldc, int accumulate, void* stream);
 /* GEMM kernel choice for later calls: 1 = mma.sync (m16n8k16) tiles, 2 =

@@ -1098,15 +1098,27 @@ static bool tma_map(CUtensorMap* m, const void* ptr, long long rows, long long c
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Per-device state of the surrogate kernels (the workspaces live on the
+// device that was current when they were made).
+constexpr int kMaxDevices = 64;
+
+static int current_device() {
+    int d = 0;
+    if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= kMaxDevices) return -1;
+    return d;
+}
+
 template <int BN>
 static cudaError_t launch_tma(const dim3& g, int M, int N, const CUtensorMap& ta, const CUtensorMap& tb, float* out,
                               long long ldo, int acc, int K, int kchunk, cudaStream_t s) {
-    static bool attr = false;
+    static unsigned long long attr_set = 0;  // bit d: the shared-memory limit is raised on device d
     constexpr size_t smem = tma_smem_bytes<BN>();
-    if (!attr) {
+    const int dev = current_device();
+    if (dev < 0) return cudaErrorInvalidDevice;
+    if (!(attr_set >> dev & 1ull)) {
         const cudaError_t e = cudaFuncSetAttribute(k_gemm_tma<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        attr = true;
+        attr_set |= 1ull << dev;
     }
     k_gemm_tma<BN><<<g, 128, smem, s>>>(M, N, ta, tb, out, ldo, acc, K, kchunk);
     return cudaGetLastError();
@@ -1168,14 +1180,15 @@ int mph_nn_status(int* timeout, int reset) {
 
 // Split-K workspace, grown on demand (the weight gradients have a small
 // output and K = the pixel count).
-static void splitk_reduce(int S, int M, int N, float* C, long long ldc, int accumulate, cudaStream_t s);
-static float* g_ws = nullptr;
-static size_t g_ws_bytes = 0;
+// One per device.
+static float* g_ws_dev[kMaxDevices] = {};
+static size_t g_ws_bytes_dev[kMaxDevices] = {};
 
-static void splitk_reduce(int S, int M, int N, float* C, long long ldc, int accumulate, cudaStream_t s) {
+static void splitk_reduce(const float* ws, int S, int M, int N, float* C, long long ldc, int accumulate,
+                          cudaStream_t s) {
     const long long total = (long long)M * N;
-    if (S > 4) k_splitk_reduce4<<<(unsigned)((total + 63) / 64), 256, 0, s>>>(g_ws, S, M, N, C, ldc, accumulate);
-    else k_splitk_reduce<<<grid_for(total), 256, 0, s>>>(g_ws, S, M, N, C, ldc, accumulate);
+    if (S > 4) k_splitk_reduce4<<<(unsigned)((total + 63) / 64), 256, 0, s>>>(ws, S, M, N, C, ldc, accumulate);
+    else k_splitk_reduce<<<grid_for(total), 256, 0, s>>>(ws, S, M, N, C, ldc, accumulate);
 }
 
 int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const void* B, long long ldb, int tb,
@@ -1209,17 +1222,20 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
     float* out = C;
     long long ldo = ldc;
     int acc = accumulate;
+    float* ws = nullptr;
     if (S > 1) {
+        const int dev = current_device();
+        if (dev < 0) return mph::fail(MPH_ERR_CUDA, "mph_nn_gemm: no current device");
         const size_t need = (size_t)S * M * N * sizeof(float);
-        if (need > g_ws_bytes) {
-            cudaFree(g_ws);
-            g_ws = nullptr;
-            g_ws_bytes = 0;
-            const cudaError_t e = cudaMalloc(&g_ws, need);
+        if (need > g_ws_bytes_dev[dev]) {
+            cudaFree(g_ws_dev[dev]);
+            g_ws_dev[dev] = nullptr;
+            g_ws_bytes_dev[dev] = 0;
+            const cudaError_t e = cudaMalloc(&g_ws_dev[dev], need);
             if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string("mph_nn_gemm workspace: ") + cudaGetErrorString(e));
-            g_ws_bytes = need;
+            g_ws_bytes_dev[dev] = need;
         }
-        out = g_ws;
+        ws = out = g_ws_dev[dev];
         ldo = N;
         acc = 0;
     }
@@ -1232,7 +1248,7 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
                       : tma_bn == 64 ? launch_tma<64>(g, M, N, tA, tB, out, ldo, acc, K, kchunk, s)
                                      : launch_tma<128>(g, M, N, tA, tB, out, ldo, acc, K, kchunk, s);
         if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string("mph_nn_gemm (TMA): ") + cudaGetErrorString(e));
-        if (S > 1) splitk_reduce(S, M, N, C, ldc, accumulate, s);
+        if (S > 1) splitk_reduce(ws, S, M, N, C, ldc, accumulate, s);
         return ck("gemm (tcgen05, TMA)");
     }
 #define MPH_GEMM_LAUNCH(KERN)                                                                                  \
@@ -1248,7 +1264,7 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
         MPH_GEMM_LAUNCH(k_gemm_bf16)
     }
 #undef MPH_GEMM_LAUNCH
-    if (S > 1) splitk_reduce(S, M, N, C, ldc, accumulate, s);
+    if (S > 1) splitk_reduce(ws, S, M, N, C, ldc, accumulate, s);
     return ck(tc ? "gemm (tcgen05)" : "gemm (mma.sync)");
 }
 
@@ -1289,20 +1305,23 @@ int mph_nn_act_bwd(const float* dOut, int ld_dout, int c_off, const void* act_ou
 
 // [blocks][C] partial column sums, shared by every call: calls on different
 // streams must not overlap (the surrogate issues all its kernels on one stream).
-static float* g_colsum_ws = nullptr;
+static float* g_colsum_ws[kMaxDevices] = {};
 static constexpr int kColsumBlocks = 608;
 
 int mph_nn_colsum(const float* X, long long P, int C, float* out, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (C > 0 && C <= 256 && P >= 256) {
-        if (!g_colsum_ws) {
-            const cudaError_t e = cudaMalloc(&g_colsum_ws, sizeof(float) * kColsumBlocks * 256);
+        const int dev = current_device();
+        if (dev < 0) return mph::fail(MPH_ERR_CUDA, "mph_nn_colsum: no current device");
+        if (!g_colsum_ws[dev]) {
+            const cudaError_t e = cudaMalloc(&g_colsum_ws[dev], sizeof(float) * kColsumBlocks * 256);
             if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string("mph_nn_colsum: ") + cudaGetErrorString(e));
         }
+        float* ws = g_colsum_ws[dev];
         const long long rows = (P + kColsumBlocks - 1) / kColsumBlocks;
         const int nb = (int)((P + rows - 1) / rows);
-        k_colsum_part<<<nb, 256, 0, s>>>(X, P, C, rows, g_colsum_ws);
-        k_colsum_final<<<(C + 7) / 8, 256, 0, s>>>(g_colsum_ws, nb, C, out);
+        k_colsum_part<<<nb, 256, 0, s>>>(X, P, C, rows, ws);
+        k_colsum_final<<<(C + 7) / 8, 256, 0, s>>>(ws, nb, C, out);
         return ck("colsum");
     }
     k_colsum<<<C, 256, 0, s>>>(X, P, C, out);
