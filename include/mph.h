@@ -365,6 +365,14 @@ int mph_nn_gemm_mode(int mode);
 /* Reads (and with reset != 0 clears) the flag the tcgen05 GEMM sets when a
  * bounded wait for its tensor-core work runs out. */
 int mph_nn_status(int* timeout, int reset);
+/* Y[p][co] (+)= 3 x 3, pad 1 convolution of the NHWC BF16 activation X
+ * [Bn][H][W][C] with Wt [Cout][9 C] (tap-major, channel-minor): the GEMM of
+ * im2col(X) with Wt^T without the im2col matrix (tcgen05 with TMA tensor
+ * copies of each tap's shifted pixels, zero padding from TMA's out-of-range
+ * fill).  MPH_ERR_UNSUPPORTED when C is not a multiple of 32 or image rows do
+ * not tile into 128-pixel blocks (use mph_nn_im2col3 + mph_nn_gemm then). */
+int mph_nn_conv3(const void* X, int Bn, int H, int W, int C, const void* Wt, int Cout, float* Y, int accumulate,
+                 void* stream);
 int mph_nn_im2col3(const void* X, int Bn, int H, int W, int C, void* Xcol, void* stream);
 int mph_nn_col2im3(const float* dXcol, int Bn, int H, int W, int C, float* dX, void* stream);
 /* out = act(Y + bias) into columns [c_off, c_off + C) of rows of width ld_out

@@ -46,7 +46,7 @@ EXPORTS = [
     "mph_set_state", "mph_host_alloc", "mph_host_free", "mph_nn_alloc", "mph_nn_free", "mph_nn_copy", "mph_nn_sync", "mph_nn_gemm", "mph_nn_im2col3", "mph_nn_col2im3",
     "mph_nn_bias_act", "mph_nn_act_bwd", "mph_nn_colsum", "mph_nn_pool", "mph_nn_pool_bwd", "mph_nn_up",
     "mph_nn_up_bwd", "mph_nn_slice", "mph_nn_mse", "mph_nn_adam", "mph_nn_cast", "mph_nn_fill",
-    "mph_nn_gemm_mode", "mph_nn_status", "mph_nn_sumsq", "mph_nn_transpose", "mph_nn_wflip",
+    "mph_nn_gemm_mode", "mph_nn_status", "mph_nn_sumsq", "mph_nn_transpose", "mph_nn_wflip", "mph_nn_conv3",
 ]
 
 

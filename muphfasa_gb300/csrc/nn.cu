@@ -520,7 +520,22 @@ __global__ void __launch_bounds__(128) k_gemm_tc05p(int M, int N, int K, const b
 //     consecutive columns.
 // Every wait is bounded (mbar_wait); the outcome is combined over the block
 // before the warp-collective TMEM reads, and a timeout sets g_nn_timeout.
-constexpr int TM_BK = 64, TM_STAGES = 4;
+//
+// Template parameters: BKC = K elements per slice, 64 (128-byte rows, 128-byte
+// swizzle) or 32 (64-byte rows, 64-byte swizzle, for 32-channel convolutions);
+// CONV = implicit-GEMM 3 x 3 convolution: A is not a matrix in memory but the
+// NHWC activation X [B][H][W][C] seen through a 4-D tensor map (C, W, H, B);
+// the 128 rows of an M tile are 128 consecutive pixels (whole image rows, or
+// a 128-pixel piece of one), and the A slice of K index k = t C + c0 (tap t =
+// 3 dy + dx) is the box of BKC channels at (c0, x0 + dx - 1, y0 + dy - 1, b):
+// the tap's shifted pixels, with the padding read as zeros by TMA (coordinates
+// outside the image).  So A(p, t C + c) = X[pixel p shifted by tap t][c], the
+// im2col matrix, without writing it.
+constexpr int TM_STAGES = 4;
+
+struct ConvGeom {
+    int C, H, W;  // channels, height, width of the activation (CONV kernels)
+};
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, unsigned long long* bar) {
     asm volatile(
@@ -530,18 +545,30 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
         : "memory");
 }
 
-// K-major shared-memory matrix descriptor, 128-byte swizzle: rows of 128 B,
-// atoms of 8 rows 1024 B apart (stride byte offset), leading byte offset
-// unused (1), descriptor version 1 (bits 46-47), layout type 2 (bits 61-63).
-__device__ __forceinline__ unsigned long long smem_desc_sw128(unsigned addr) {
-    return (unsigned long long)((addr >> 4) & 0x3FFF) | (1ull << 16) | ((unsigned long long)(1024 >> 4) << 32) |
-           (1ull << 46) | (2ull << 61);
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];\n" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
 }
 
-template <int BN>
+// K-major shared-memory matrix descriptor of a swizzled tile: rows of BKC * 2
+// bytes, atoms of 8 rows (stride byte offset 8 rows), leading byte offset
+// unused (1), descriptor version 1 (bits 46-47), layout type at bits 61-63:
+// 2 = 128-byte swizzle (BKC 64), 4 = 64-byte swizzle (BKC 32).
+template <int BKC>
+__device__ __forceinline__ unsigned long long smem_desc_sw(unsigned addr) {
+    constexpr unsigned long long sbo = (8 * BKC * 2) >> 4, layout = BKC == 64 ? 2ull : 4ull;
+    return (unsigned long long)((addr >> 4) & 0x3FFF) | (1ull << 16) | (sbo << 32) | (1ull << 46) | (layout << 61);
+}
+
+template <int BN, int BKC, bool CONV>
 __global__ void __launch_bounds__(128) k_gemm_tma(int M, int N, const __grid_constant__ CUtensorMap tmA,
                                                   const __grid_constant__ CUtensorMap tmB, float* __restrict__ C,
-                                                  long long ldc, int accumulate, int K, int kchunk) {
+                                                  long long ldc, int accumulate, int K, int kchunk, const ConvGeom cg) {
+    constexpr int TM_BK = BKC;
     constexpr int A_BYTES = 128 * TM_BK * 2, B_BYTES = BN * TM_BK * 2;
     extern __shared__ unsigned char tm_dyn[];
     __shared__ __align__(8) unsigned long long full[TM_STAGES], empty[TM_STAGES], done;
@@ -585,8 +612,19 @@ __global__ void __launch_bounds__(128) k_gemm_tma(int M, int N, const __grid_con
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(&full[s])),
                          "r"(A_BYTES + B_BYTES)
                          : "memory");
-            tma_load_2d(sA + s * A_BYTES, &tmA, kb + kt * TM_BK, m0, &full[s]);
-            tma_load_2d(sB + s * B_BYTES, &tmB, kb + kt * TM_BK, n0, &full[s]);
+            const int k = kb + kt * TM_BK;
+            if constexpr (CONV) {
+                // M tile -> first pixel (b, y0, x0); K index -> tap and channel block
+                const int hw = cg.H * cg.W;
+                const int b = m0 / hw, rem = m0 - b * hw;
+                const int y0 = rem / cg.W, x0 = rem - y0 * cg.W;
+                const int t = k / cg.C, c0 = k - t * cg.C;
+                const int dy = t / 3, dx = t - 3 * dy;
+                tma_load_4d(sA + s * A_BYTES, &tmA, c0, x0 + dx - 1, y0 + dy - 1, b, &full[s]);
+            } else {
+                tma_load_2d(sA + s * A_BYTES, &tmA, k, m0, &full[s]);
+            }
+            tma_load_2d(sB + s * B_BYTES, &tmB, k, n0, &full[s]);
         }
     } else if (tid == 32) {  // MMA issuer
         const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(BN >> 3) << 17) | ((unsigned)(128 >> 4) << 24);
@@ -599,8 +637,8 @@ __global__ void __launch_bounds__(128) k_gemm_tma(int M, int N, const __grid_con
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
 #pragma unroll
             for (int kk = 0; kk < TM_BK / 16; ++kk) {
-                const unsigned long long ad = smem_desc_sw128(smem_u32(sA + s * A_BYTES) + kk * 32);
-                const unsigned long long bd = smem_desc_sw128(smem_u32(sB + s * B_BYTES) + kk * 32);
+                const unsigned long long ad = smem_desc_sw<BKC>(smem_u32(sA + s * A_BYTES) + kk * 32);
+                const unsigned long long bd = smem_desc_sw<BKC>(smem_u32(sB + s * B_BYTES) + kk * 32);
                 const unsigned acc = (kt > 0 || kk > 0) ? 1u : 0u;
                 asm volatile(
                     "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
@@ -656,9 +694,11 @@ __global__ void __launch_bounds__(128) k_gemm_tma(int M, int N, const __grid_con
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(BN));
 }
 
-template <int BN>
+// Stage memory, also holding the 128 x (BN + 1) FP32 epilogue tile.
+template <int BN, int BKC>
 constexpr size_t tma_smem_bytes() {
-    return 1024 + (size_t)TM_STAGES * (128 + BN) * TM_BK * 2;
+    constexpr size_t stages = (size_t)TM_STAGES * (128 + BN) * BKC * 2, tile = (size_t)128 * (BN + 1) * 4;
+    return 1024 + (stages > tile ? stages : tile);
 }
 
 // C[m][n] (+)= sum over splits z of W[z][m][n] (W rows of width N), in split order.
@@ -1088,14 +1128,27 @@ static bool tma_available() {
 
 // Map of a row-major BF16 matrix [rows][cols] (row stride ld elements) read
 // in boxes of 64 columns (128 B, the swizzle span) x box_rows rows.
-static bool tma_map(CUtensorMap* m, const void* ptr, long long rows, long long cols, long long ld, int box_rows) {
+static bool tma_map(CUtensorMap* m, const void* ptr, long long rows, long long cols, long long ld, int box_rows,
+                    int box_cols = 64) {
     const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
     const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-    const cuuint32_t box[2] = {64u, (cuuint32_t)box_rows};
+    const cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
     const cuuint32_t es[2] = {1u, 1u};
     return g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, es,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, box_cols == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Map of an NHWC BF16 activation [B][H][W][C] as the 4-D tensor (C, W, H, B),
+// read in boxes of bkc channels x a 128-pixel piece (bw pixels of bh rows).
+static bool tma_map_act(CUtensorMap* m, const void* ptr, int Bn, int H, int W, int C, int bkc, int bw, int bh) {
+    const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)Bn};
+    const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+    const cuuint32_t box[4] = {(cuuint32_t)bkc, (cuuint32_t)bw, (cuuint32_t)bh, 1u};
+    const cuuint32_t es[4] = {1u, 1u, 1u, 1u};
+    return g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(ptr), dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, bkc == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 // Per-device state of the surrogate kernels (the workspaces live on the
@@ -1108,19 +1161,20 @@ static int current_device() {
     return d;
 }
 
-template <int BN>
+template <int BN, int BKC = 64, bool CONV = false>
 static cudaError_t launch_tma(const dim3& g, int M, int N, const CUtensorMap& ta, const CUtensorMap& tb, float* out,
-                              long long ldo, int acc, int K, int kchunk, cudaStream_t s) {
+                              long long ldo, int acc, int K, int kchunk, cudaStream_t s, ConvGeom cg = ConvGeom{}) {
     static unsigned long long attr_set = 0;  // bit d: the shared-memory limit is raised on device d
-    constexpr size_t smem = tma_smem_bytes<BN>();
+    constexpr size_t smem = tma_smem_bytes<BN, BKC>();
     const int dev = current_device();
     if (dev < 0) return cudaErrorInvalidDevice;
     if (!(attr_set >> dev & 1ull)) {
-        const cudaError_t e = cudaFuncSetAttribute(k_gemm_tma<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_gemm_tma<BN, BKC, CONV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         attr_set |= 1ull << dev;
     }
-    k_gemm_tma<BN><<<g, 128, smem, s>>>(M, N, ta, tb, out, ldo, acc, K, kchunk);
+    k_gemm_tma<BN, BKC, CONV><<<g, 128, smem, s>>>(M, N, ta, tb, out, ldo, acc, K, kchunk, cg);
     return cudaGetLastError();
 }
 
@@ -1184,6 +1238,36 @@ int mph_nn_status(int* timeout, int reset) {
 static float* g_ws_dev[kMaxDevices] = {};
 static size_t g_ws_bytes_dev[kMaxDevices] = {};
 
+// Enough blocks for the 152 SMs: split K (in multiples of 64) when the
+// output tiles are few.
+static void split_plan(long long blocks, int K, int& S, int& kchunk) {
+    S = 1;
+    kchunk = K;
+    if (blocks < 2 * 152 && K >= 8 * 64) {
+        S = (int)std::min<long long>((2 * 152 + blocks - 1) / blocks, K / (4 * 64));
+        S = std::max(1, std::min(S, 64));
+        kchunk = (K + S - 1) / S;
+        kchunk = (kchunk + 63) / 64 * 64;
+        S = (K + kchunk - 1) / kchunk;
+    }
+}
+
+// The split-K workspace of the current device, grown to `need` bytes.
+static int split_workspace(size_t need, float** ws, const char* who) {
+    const int dev = current_device();
+    if (dev < 0) return mph::fail(MPH_ERR_CUDA, std::string(who) + ": no current device");
+    if (need > g_ws_bytes_dev[dev]) {
+        cudaFree(g_ws_dev[dev]);
+        g_ws_dev[dev] = nullptr;
+        g_ws_bytes_dev[dev] = 0;
+        const cudaError_t e = cudaMalloc(&g_ws_dev[dev], need);
+        if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string(who) + " workspace: " + cudaGetErrorString(e));
+        g_ws_bytes_dev[dev] = need;
+    }
+    *ws = g_ws_dev[dev];
+    return MPH_OK;
+}
+
 static void splitk_reduce(const float* ws, int S, int M, int N, float* C, long long ldc, int accumulate,
                           cudaStream_t s) {
     const long long total = (long long)M * N;
@@ -1209,33 +1293,16 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
     const int tm = tc ? TC_BM : BM, tn = tma ? tma_bn : (tc ? TC_BN : BN);
     const long long gx = (N + tn - 1) / tn, gy = (M + tm - 1) / tm;
     if (gy > 65535) return mph::fail(MPH_ERR_ARG, "mph_nn_gemm: M too large for one launch");
-    // Enough blocks for the 152 SMs: split K when the output tiles are few.
     int S = 1, kchunk = K;
-    const long long blocks = gx * gy;
-    if (blocks < 2 * 152 && K >= 8 * 64) {
-        S = (int)std::min<long long>((2 * 152 + blocks - 1) / blocks, K / (4 * 64));
-        S = std::max(1, std::min(S, 64));
-        kchunk = (K + S - 1) / S;
-        kchunk = (kchunk + 63) / 64 * 64;
-        S = (K + kchunk - 1) / kchunk;
-    }
+    split_plan(gx * gy, K, S, kchunk);
     float* out = C;
     long long ldo = ldc;
     int acc = accumulate;
     float* ws = nullptr;
     if (S > 1) {
-        const int dev = current_device();
-        if (dev < 0) return mph::fail(MPH_ERR_CUDA, "mph_nn_gemm: no current device");
-        const size_t need = (size_t)S * M * N * sizeof(float);
-        if (need > g_ws_bytes_dev[dev]) {
-            cudaFree(g_ws_dev[dev]);
-            g_ws_dev[dev] = nullptr;
-            g_ws_bytes_dev[dev] = 0;
-            const cudaError_t e = cudaMalloc(&g_ws_dev[dev], need);
-            if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string("mph_nn_gemm workspace: ") + cudaGetErrorString(e));
-            g_ws_bytes_dev[dev] = need;
-        }
-        ws = out = g_ws_dev[dev];
+        const int rc = split_workspace((size_t)S * M * N * sizeof(float), &ws, "mph_nn_gemm");
+        if (rc) return rc;
+        out = ws;
         ldo = N;
         acc = 0;
     }
@@ -1266,6 +1333,59 @@ int mph_nn_gemm(int M, int N, int K, const void* A, long long lda, int ta, const
 #undef MPH_GEMM_LAUNCH
     if (S > 1) splitk_reduce(ws, S, M, N, C, ldc, accumulate, s);
     return ck(tc ? "gemm (tcgen05)" : "gemm (mma.sync)");
+}
+
+// Y[p][co] (+)= sum over taps t and channels c of X[pixel p shifted by t][c]
+// Wt[co][t C + c]: the forward GEMM of a 3 x 3, pad 1 convolution without the
+// im2col matrix (k_gemm_tma<BN, BKC, true>).  MPH_ERR_UNSUPPORTED when the
+// shapes do not fit the implicit kernel (C not a multiple of 32, image rows
+// that do not tile 128-pixel blocks, unaligned buffers, no TMA); the caller
+// then uses im2col + mph_nn_gemm.
+int mph_nn_conv3(const void* X, int Bn, int H, int W, int C, const void* Wt, int Cout, float* Y, int accumulate,
+                 void* stream) {
+    if (!X || !Wt || !Y || Bn <= 0 || H <= 0 || W <= 0 || C <= 0 || Cout <= 0)
+        return mph::fail(MPH_ERR_ARG, "mph_nn_conv3: bad argument");
+    const long long P = (long long)Bn * H * W;
+    const int bw = W < 128 ? W : 128, bh = 128 / bw;
+    const bool tiles = W >= 128 ? W % 128 == 0 : (128 % W == 0 && H % bh == 0);
+    const bool aligned = ((reinterpret_cast<unsigned long long>(X) | reinterpret_cast<unsigned long long>(Wt)) & 15) == 0;
+    if (C % 32 != 0 || !tiles || P % 128 != 0 || P / 128 > 65535 || !aligned || (long long)9 * C > 0x7fffffffLL ||
+        !tma_available())
+        return mph::fail(MPH_ERR_UNSUPPORTED, "mph_nn_conv3: shapes outside the implicit-GEMM kernel");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int bkc = C % 64 == 0 ? 64 : 32;
+    const int M = (int)P, N = Cout, K = 9 * C;
+    const int bn = N <= 32 ? 32 : (N <= 64 ? 64 : 128);
+    const long long gx = (N + bn - 1) / bn, gy = P / 128;
+    int S = 1, kchunk = K;
+    split_plan(gx * gy, K, S, kchunk);
+    float* out = Y;
+    long long ldo = N;
+    int acc = accumulate;
+    float* ws = nullptr;
+    if (S > 1) {
+        const int rc = split_workspace((size_t)S * M * N * sizeof(float), &ws, "mph_nn_conv3");
+        if (rc) return rc;
+        out = ws;
+        acc = 0;
+    }
+    CUtensorMap tA, tB;
+    if (!tma_map_act(&tA, X, Bn, H, W, C, bkc, bw, bh) || !tma_map(&tB, Wt, N, K, K, bn, bkc))
+        return mph::fail(MPH_ERR_CUDA, "mph_nn_conv3: cuTensorMapEncodeTiled failed");
+    const dim3 g((unsigned)gx, (unsigned)gy, (unsigned)S);
+    const ConvGeom cg{C, H, W};
+    cudaError_t e;
+    if (bkc == 64)
+        e = bn == 32 ? launch_tma<32, 64, true>(g, M, N, tA, tB, out, ldo, acc, K, kchunk, s, cg)
+          : bn == 64 ? launch_tma<64, 64, true>(g, M, N, tA, tB, out, ldo, acc, K, kchunk, s, cg)
+                     : launch_tma<128, 64, true>(g, M, N, tA, tB, out, ldo, acc, K, kchunk, s, cg);
+    else
+        e = bn == 32 ? launch_tma<32, 32, true>(g, M, N, tA, tB, out, ldo, acc, K, kchunk, s, cg)
+          : bn == 64 ? launch_tma<64, 32, true>(g, M, N, tA, tB, out, ldo, acc, K, kchunk, s, cg)
+                     : launch_tma<128, 32, true>(g, M, N, tA, tB, out, ldo, acc, K, kchunk, s, cg);
+    if (e != cudaSuccess) return mph::fail(MPH_ERR_CUDA, std::string("mph_nn_conv3: ") + cudaGetErrorString(e));
+    if (S > 1) splitk_reduce(ws, S, M, N, Y, N, accumulate, s);
+    return ck("conv3 (tcgen05, TMA, implicit GEMM)");
 }
 
 int mph_nn_im2col3(const void* X, int Bn, int H, int W, int C, void* Xcol, void* stream) {

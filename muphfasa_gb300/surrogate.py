@@ -99,6 +99,7 @@ def _lib():
         L.mph_nn_fill.argtypes = [fp, LL, F, P]
         L.mph_nn_transpose.argtypes = [P, LL, I, P, P]
         L.mph_nn_wflip.argtypes = [P, I, I, P, P]
+        L.mph_nn_conv3.argtypes = [P, I, I, I, I, P, I, fp, I, P]
         L.mph_nn_sync.argtypes = [P]
         L.mph_nn_gemm_mode.argtypes = [I]
         L.mph_nn_status.argtypes = [C.POINTER(C.c_int), I]
@@ -110,14 +111,16 @@ class Conv:
     """3 x 3 (pad 1) or 1 x 1 convolution with bias and optional leaky ReLU.
 
     Every GEMM reads both operands K-contiguous (the tensor-core kernel's
-    16-byte asynchronous copies):
-      forward          Y [P][Cout]    = Xcol [P][9 Cin] . Wt^T
+    TMA copies):
+      forward          Y [P][Cout]    = Xcol [P][9 Cin] . Wt^T, as an implicit
+                       GEMM (mph_nn_conv3: the tap-shifted pixels of X are the A
+                       tiles, no im2col) where the shapes allow
       weight gradient  gW [Cout][9 Cin] = dY^T [Cout][P] . Xcol^T [9 Cin][P]
                        (both operands transposed once per step)
       data gradient    dX [P][Cin]    = dYcol [P][9 Cout] . W2^T, with dYcol the
                        im2col of dY and W2 the weights with mirrored taps, so the
                        gradient is a 3 x 3 convolution of dY (no 9 x expanded
-                       FP32 column gradient and no col2im)."""
+                       FP32 column gradient and no col2im), implicit as well."""
 
     def __init__(self, cin, cout, rng, k3=True, act=True):
         self.cin, self.cout, self.k3, self.act = cin, cout, k3, act
@@ -138,6 +141,20 @@ class Conv:
             check(L.mph_nn_fill(buf.ptr, n, 0.0, None))
         self.refresh()
         self.P = 0
+        # whether mph_nn_conv3 takes this layer's forward / data-gradient shapes
+        # (found at the first call)
+        self.implicit = self.bwd_implicit = None
+
+    def _conv3(self, x, Bn, H, W, C, wt, cout, y):
+        """mph_nn_conv3 when it applies, else False (the caller uses im2col + GEMM)."""
+        from . import MphError
+        try:
+            check(_lib().mph_nn_conv3(x.ptr, Bn, H, W, C, wt.ptr, cout, y.ptr, 0, None))
+            return True
+        except MphError as ex:
+            if ex.code != 4:  # MPH_ERR_UNSUPPORTED
+                raise
+            return False
 
     def refresh(self):
         check(_lib().mph_nn_cast(0, self.wt.ptr, self.n, self.wt_bf.ptr, None))
@@ -158,12 +175,17 @@ class Conv:
         L, P = _lib(), Bn * H * W
         self.alloc(P)
         self.x, self.shape = x, (Bn, H, W)
-        A = x
-        if self.k3:
-            check(L.mph_nn_im2col3(x.ptr, Bn, H, W, self.cin, self.xcol.ptr, None))
-            A = self.xcol
-        check(L.mph_nn_gemm(P, self.cout, self.K, A.ptr, self.K, 0, self.wt_bf.ptr, self.K, 0, self.y.ptr,
-                            self.cout, 0, None))
+        self.fwd_implicit = False
+        if self.k3 and self.implicit is not False:
+            self.fwd_implicit = self._conv3(x, Bn, H, W, self.cin, self.wt_bf, self.cout, self.y)
+            self.implicit = self.fwd_implicit
+        if not self.fwd_implicit:
+            A = x
+            if self.k3:
+                check(L.mph_nn_im2col3(x.ptr, Bn, H, W, self.cin, self.xcol.ptr, None))
+                A = self.xcol
+            check(L.mph_nn_gemm(P, self.cout, self.K, A.ptr, self.K, 0, self.wt_bf.ptr, self.K, 0, self.y.ptr,
+                                self.cout, 0, None))
         check(L.mph_nn_bias_act(self.y.ptr, self.b.ptr, P, self.cout, int(self.act),
                                 self.out.ptr if out_f32 is None else None,
                                 out_f32.ptr if out_f32 is not None else None, self.cout, 0, None))
@@ -177,6 +199,8 @@ class Conv:
                                self.dpre.ptr, None))
         check(L.mph_nn_colsum(self.dpre.ptr, P, self.cout, self.gb.ptr, None))
         check(L.mph_nn_cast(0, self.dpre.ptr, P * self.cout, self.dpre_bf.ptr, None))
+        if self.k3 and self.fwd_implicit:  # the weight gradient needs the im2col matrix once
+            check(L.mph_nn_im2col3(self.x.ptr, Bn, H, W, self.cin, self.xcol.ptr, None))
         B = self.xcol if self.k3 else self.x
         check(L.mph_nn_transpose(self.dpre_bf.ptr, P, self.cout, self.dpre_t.ptr, None))
         check(L.mph_nn_transpose(B.ptr, P, self.K, self.xcol_t.ptr, None))
@@ -185,10 +209,14 @@ class Conv:
         if not need_dx:
             return None
         if self.k3:
-            check(L.mph_nn_im2col3(self.dpre_bf.ptr, Bn, H, W, self.cout, self.dycol.ptr, None))
             check(L.mph_nn_wflip(self.wt_bf.ptr, self.cout, self.cin, self.w2.ptr, None))
-            check(L.mph_nn_gemm(P, self.cin, 9 * self.cout, self.dycol.ptr, 9 * self.cout, 0, self.w2.ptr,
-                                9 * self.cout, 0, self.dx.ptr, self.cin, 0, None))
+            done = False
+            if self.bwd_implicit is not False:
+                done = self.bwd_implicit = self._conv3(self.dpre_bf, Bn, H, W, self.cout, self.w2, self.cin, self.dx)
+            if not done:
+                check(L.mph_nn_im2col3(self.dpre_bf.ptr, Bn, H, W, self.cout, self.dycol.ptr, None))
+                check(L.mph_nn_gemm(P, self.cin, 9 * self.cout, self.dycol.ptr, 9 * self.cout, 0, self.w2.ptr,
+                                    9 * self.cout, 0, self.dx.ptr, self.cin, 0, None))
         else:
             check(L.mph_nn_gemm(P, self.K, self.cout, self.dpre_bf.ptr, self.cout, 0, self.wt_bf.ptr, self.K, 1,
                                 self.dx.ptr, self.K, 0, None))

@@ -171,6 +171,43 @@ def test_tma_gemm_shapes_of_the_network(shape, S):
     assert np.all(np.abs(got2 - 2 * ref) <= 2e-5 * scale + 2e-6)
 
 
+@pytest.mark.parametrize("Bn,H,W,Cc,cout", [(2, 16, 128, 32, 64), (2, 8, 64, 64, 32), (4, 16, 16, 96, 32),
+                                            (1, 4, 256, 64, 128), (8, 16, 8, 128, 256), (2, 32, 32, 256, 3)])
+def test_implicit_conv3_against_im2col_gemm(Bn, H, W, Cc, cout, S):
+    """mph_nn_conv3 (implicit GEMM: TMA boxes of each tap's shifted pixels,
+    64- or 32-channel slices, tiles of whole rows or of 128-pixel pieces of a
+    row, split K on the small outputs) against the float64 product of the
+    restatement's im2col with the weights, and accumulate mode."""
+    rng = np.random.default_rng(Bn * H * W + Cc + cout)
+    x = NO.to_bf16(rng.standard_normal((Bn, H, W, Cc)).astype(np.float32))
+    wt = NO.to_bf16(rng.standard_normal((cout, 9 * Cc)).astype(np.float32))
+    dx_, dw = _bf16_dev(S, x), _bf16_dev(S, wt)
+    P = Bn * H * W
+    y = S._f32(P * cout)
+    L = S._lib()
+    S.check(L.mph_nn_conv3(dx_.ptr, Bn, H, W, Cc, dw.ptr, cout, y.ptr, 0, None))
+    got = y.download(P * cout).reshape(P, cout)
+    S.check(L.mph_nn_conv3(dx_.ptr, Bn, H, W, Cc, dw.ptr, cout, y.ptr, 1, None))
+    got2 = y.download(P * cout).reshape(P, cout)
+    flag = C.c_int(-1)
+    S.check(L.mph_nn_status(C.byref(flag), 1))
+    assert flag.value == 0
+    A = NO.Net.im2col(x).astype(np.float64)
+    ref, scale = A @ wt.T.astype(np.float64), np.abs(A) @ np.abs(wt.T).astype(np.float64)
+    assert np.all(np.abs(got - ref) <= 1e-5 * scale + 1e-6)
+    assert np.all(np.abs(got2 - 2 * ref) <= 2e-5 * scale + 2e-6)
+
+
+def test_implicit_conv3_rejects_shapes_it_cannot_tile(S, mph):
+    rng = np.random.default_rng(0)
+    x = _bf16_dev(S, rng.standard_normal((1, 6, 10, 8)).astype(np.float32))
+    w = _bf16_dev(S, rng.standard_normal((32, 72)).astype(np.float32))
+    y = S._f32(60 * 32)
+    with pytest.raises(mph.MphError) as e:
+        S.check(S._lib().mph_nn_conv3(x.ptr, 1, 6, 10, 8, w.ptr, 32, y.ptr, 0, None))
+    assert e.value.code == 4
+
+
 def test_im2col_col2im_adjoint(S):
     rng = np.random.default_rng(3)
     Bn, H, W, Cc = 2, 8, 16, 5
