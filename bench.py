@@ -401,6 +401,56 @@ def run_tgv2d(args):
     return 0
 
 
+def warmstart_curves(ws, cases, fields, rest, max_steps, consistent):
+    """Steps to 1e-8 against the relative error e of the initial field
+    (converged fields + smooth noise), with the plain feq + f_neq start and with
+    the consistent start (ws.consistent_start, `consistent` = (steps, rounds))."""
+    amps = [0.3, 0.1, 3e-2, 1e-2, 1e-3, 1e-4, 1e-5, 1e-6, 0.0]
+    rest = np.asarray(rest, float)
+    out, secs = {}, 0.0
+    for name, cons in (("feq_fneq", None), ("consistent", consistent)):
+        rng = np.random.default_rng(0)
+        run, inits, keys = [], [], []
+        for c, (rho, u) in zip(cases, fields):
+            for e in amps:
+                run.append(c)
+                inits.append(ws.perturbed_fields(c, rho, u, e, rng))
+                keys.append(e)
+        t0 = time.perf_counter()
+        st, _, _, _ = ws.solve(run, inits, max_steps=max_steps, consistent=cons)
+        secs += time.perf_counter() - t0
+        rows = []
+        for e in amps:
+            se = np.array([x for x, k in zip(st, keys) if k == e], float)
+            ok = (se > 0) & (rest > 0)
+            rows.append({"rel_error": e, "steps_median": float(np.median(se[se > 0])) if np.any(se > 0) else None,
+                         "gain_median": float(np.median(rest[ok] / se[ok])) if ok.any() else None})
+        out[name] = rows
+    out["consistent_start"] = {"steps": consistent[0], "rounds": consistent[1]}
+    out["rest_steps_median"] = float(np.median(rest[rest > 0])) if np.any(rest > 0) else None
+    out["cases"] = len(cases)
+    return out, secs
+
+
+def run_warmstart_curve(args, m, ws, log):
+    """--ws-train 0: only the steps-vs-error curves, on the converged fields of
+    the first --ws-curve held-out cases (no data generation, no training)."""
+    n = args.ws_n
+    test_cases = ws.draw_cases(args.ws_test, seed=202, sizes=(n,))
+    sp, ref, secs_plain, _ = ws.solve(test_cases, None, max_steps=args.ws_max_steps)
+    conv = [i for i in range(len(test_cases)) if sp[i] > 0][: args.ws_curve]
+    curves, secs = warmstart_curves(ws, [test_cases[i] for i in conv], [ref[i] for i in conv], [sp[i] for i in conv],
+                                    args.ws_max_steps, tuple(int(v) for v in args.ws_consistent.split(",")))
+    line = {"metric": "steps to residual 1e-8 against the initial field's error", "value": None, "unit": "steps",
+            "n_gpus": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "solver int64 fixed point (FP64-accurate)", "data": "synthetic",
+            "config": {"workload": f"warmstart_curve_d2q9_{n}^2", "test_cases": len(test_cases),
+                       "Re": list(ws.RE), "U": list(ws.U)},
+            "error_vs_steps": curves, "seconds": {"solve_from_rest": round(secs_plain, 1), "curves": round(secs, 1)}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_warmstart(args):
     """Learned warm start: the plain solver (FP64-accurate fixed point, batch
     of all cases, converged cases leaving the batch) generates steady fields
@@ -416,6 +466,8 @@ def run_warmstart(args):
     m.set_device(0)
     n = args.ws_n
     log = lambda *a: print(json.dumps({"progress": a}), file=sys.stderr, flush=True)
+    if args.ws_train == 0:
+        return run_warmstart_curve(args, m, ws, log)
     # draw ws_draw cases (at least ws_train) and keep the first ws_train that
     # reach the residual 1e-8: high-Re cases near tau = 1/2 diverge or stall
     train_cases = ws.draw_cases(max(args.ws_draw, args.ws_train), seed=101, sizes=(n,))
@@ -447,16 +499,9 @@ def run_warmstart(args):
     good = both & (err_all < 0.2)
     # steps to 1e-8 against the initial field's relative error (converged held-out fields + smooth noise)
     conv = [i for i in range(len(test_cases)) if sp[i] > 0][: args.ws_curve]
-    amps = [0.3, 0.1, 3e-2, 1e-2, 1e-3, 1e-4, 1e-5, 1e-6, 0.0]
-    curve, curve_secs = ws.perturbation_curve([test_cases[i] for i in conv], [ref[i] for i in conv], amps,
-                                              max_steps=args.ws_max_steps)
-    rest = np.array(curve["rest"], float)
-    curve_rows = []
-    for e in amps:
-        se = np.array(curve[e], float)
-        ok = (se > 0) & (rest > 0)
-        curve_rows.append({"rel_error": e, "steps_median": float(np.median(se[se > 0])) if np.any(se > 0) else None,
-                           "gain_median": float(np.median(rest[ok] / se[ok])) if ok.any() else None})
+    curves, curve_secs = warmstart_curves(ws, [test_cases[i] for i in conv], [ref[i] for i in conv],
+                                          [sp[i] for i in conv], args.ws_max_steps,
+                                          tuple(int(v) for v in args.ws_consistent.split(",")))
     # single-case wall time (one FP64-accurate handle per case): rest vs predict + warm start
     single = []
     for c in [c for c, ok in zip(test_cases, both) if ok][: args.ws_single]:
@@ -502,8 +547,7 @@ def run_warmstart(args):
                                   "p90": float(np.percentile(errs, 90)) if errs.size else None, "by_kind": by_kind},
             "steps_ratio_when_error_below_0.2": {"cases": int(good.sum()),
                                                  "median": float(np.median(sp[good] / sw[good])) if good.any() else None},
-            "error_vs_steps": {"cases": len(conv), "rows": curve_rows,
-                               "rest_steps_median": float(np.median(rest[rest > 0])) if np.any(rest > 0) else None},
+            "error_vs_steps": curves,
             "seconds": {"generate": round(gen_secs, 1), "train": round(train_secs, 1),
                         "predict_all": round(pred_secs, 3), "batch_plain": round(secs_plain, 1),
                         "batch_warm": round(secs_warm, 1), "curve": round(curve_secs, 1)},
@@ -644,6 +688,8 @@ def main():
     ap.add_argument("--ws-max-steps", type=int, default=400000)
     ap.add_argument("--ws-curve", type=int, default=24, help="warmstart: held-out cases of the error-vs-steps curve")
     ap.add_argument("--ws-single", type=int, default=6, help="warmstart: cases timed on single handles")
+    ap.add_argument("--ws-consistent", default="50,4",
+                    help="warmstart: steps,rounds of the consistent start in the error-vs-steps curves")
     ap.add_argument("--tgv-ref", default="f64x", choices=["f64x", "f64", "f64_fast"],
                     help="tgv3d: reference precision (FP64 or the FP64-accurate fixed point)")
     args = ap.parse_args()
