@@ -100,8 +100,10 @@ def test_nonequilibrium_init_matches_the_steady_populations(mph):
 def test_consistent_start_lowers_the_floor(mph):
     """The consistent start (a few short runs, each followed by a reset of
     (rho, u) to the prescribed field that keeps the solver's own
-    non-equilibrium part) leaves the prescribed moments in place to storage
-    resolution, and from the converged field itself it reaches 1e-8 in fewer
+    non-equilibrium part) leaves the prescribed moments in the stored
+    populations to storage resolution (the moments of the streamed
+    populations, which mph_batch_moments reports, equal them only at a steady
+    state), and from the converged field itself it reaches 1e-8 in fewer
     steps than the feq + f_neq start, its own steps included."""
     from muphfasa_gb300 import warmstart as ws
     cases = _cases(ws, 32, 5, 4)
@@ -113,7 +115,7 @@ def test_consistent_start_lowers_the_floor(mph):
     spent = ws.consistent_start(b, cases, list(range(len(cases))), fields, steps=10, rounds=2)
     assert spent == 20
     for j, (rho, u) in enumerate(fields):
-        r2, u2 = b.moments(j)
+        r2, u2 = ws._moments_d2q9(b.f(j), cases[j]["n"])
         assert np.max(np.abs(r2 - rho)) < 1e-12 and np.max(np.abs(u2 - u)) < 1e-12
     b.close()
     plain, _, _, _ = ws.solve(cases, fields, max_steps=100000)
