@@ -39,9 +39,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 LATTICE_Q = {"D2Q9": 9, "D3Q15": 15, "D3Q19": 19, "D3Q27": 27}
-ELEM = {"f64": 8, "f64_fast": 8, "f32": 4, "f16s": 2, "bf16s": 2, "f64x": 8, "f16c": 2}
+ELEM = {"f64": 8, "f64_fast": 8, "f32": 4, "f16s": 2, "bf16s": 2, "f64x": 8, "f16c": 2, "f16w": 2}
 DTYPE = {"f64": "f64", "f64_fast": "f64", "f32": "f32", "f16s": "f16 storage / f32 arithmetic",
          "bf16s": "bf16 storage / f32 arithmetic", "f16c": "custom 1-4-11 16-bit storage / f32 arithmetic",
+         "f16w": "custom 1-3-12 16-bit storage of (f - w) / w / f32 arithmetic",
          "f64x": "int64 fixed point (f/w in units of 2^-56), FP64-accurate"}
 METRIC = "MLUPS"
 
@@ -186,16 +187,16 @@ def tgv3d_fields(n, u0):
 
 def run_tgv3d(args):
     """Precision study: D3Q27 TGV at n^3, tau 0.52, u0 0.05; the shifted FP16,
-    BF16 and custom 1-4-11 (f16c) storage against the FP64-accurate reference
-    path, velocity L2 and kinetic-energy errors and FP64 mass / momentum sums
-    every `every` steps."""
+    BF16, custom 1-4-11 (f16c) and weight-scaled 1-3-12 (f16w) storage
+    against the FP64-accurate reference path, velocity L2 and kinetic-energy
+    errors and FP64 mass / momentum sums every `every` steps."""
     import muphfasa_gb300 as m
     m.set_device(0)
     n, u0, tau = args.n, 0.05, 0.52
     every, total = args.every, args.tgv_steps
     rho, u = tgv3d_fields(n, u0)
     N = n ** 3
-    names = [args.tgv_ref, "f16s", "bf16s", "f16c"]
+    names = [args.tgv_ref, "f16s", "bf16s", "f16c", "f16w"]
     sims = {}
     for p in names:
         s = m.Simulation(m.make_desc("D3Q27", (n, n, n), 1.0 / tau, precision=p))
@@ -227,12 +228,12 @@ def run_tgv3d(args):
         table.append(row)
         print(json.dumps({"progress": row}), file=sys.stderr, flush=True)
     mlups = {p: N * total / (ms[p] / 1e3) / 1e6 for p in names}
-    bytes_cell = {"f64x": 432, "f64": 432, "f64_fast": 432, "f32": 216, "f16s": 108, "bf16s": 108, "f16c": 108}
+    bytes_cell = {"f64x": 432, "f64": 432, "f64_fast": 432, "f32": 216, "f16s": 108, "bf16s": 108, "f16c": 108, "f16w": 108}
     peak, kind = peaks()
     last = table[-1]
     line = {"metric": "velocity L2 error vs FP64-accurate reference (and MLUPS)",
             "value": last["f16s"]["u_l2_rel"], "unit": "relative", "n_gpus": 1, "steps": total, "warmup": 0,
-            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f16 / bf16 / custom 1-4-11 storage, f32 collide",
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f16 / bf16 / custom 1-4-11 / 1-3-12 storage, f32 collide",
             "data": "synthetic",
             "config": {"workload": f"tgv3d_d3q27_{n}^3", "lattice": "D3Q27", "grid": [n] * 3, "tau": tau, "u0": u0,
                        "reference_precision": names[0], "every": every,

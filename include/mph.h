@@ -76,6 +76,16 @@ extern "C" {
  * saturate), FP32 collide arithmetic; same traffic as FP16 storage, half
  * its rounding error. */
 #define MPH_PREC_F16C 6
+/* (f_i - w_i) / p_i, p_i the power of two nearest to w_i, stored
+ * as a custom 16-bit float (sign, 3 exponent bits biased by 8, 12 stored
+ * mantissa bits: normals 2^-7 .. 1 - 2^-13, subnormal steps of 2^-19), FP32
+ * collide arithmetic; same traffic as FP16 storage.  Scaling by about 1/w_i
+ * puts every population's deviation on one scale, so the exponent needs one
+ * bit less than MPH_PREC_F16C and the significand gets it.  Populations must
+ * stay inside (w_i - p_i, w_i + p_i), p_i >= 0.75 w_i (|u| up to about 0.1):
+ * a store that saturates makes the step report MPH_ERR_NONFINITE.
+ * Single domains only (a batch rejects it). */
+#define MPH_PREC_F16W 7
 
 /* ---- lattice-unit description of one domain ---------------------------- */
 typedef struct {

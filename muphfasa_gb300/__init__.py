@@ -29,7 +29,7 @@ MPH_OK = 0
 ERRORS = {1: "MPH_ERR_ARG", 2: "MPH_ERR_CONFIG", 3: "MPH_ERR_CUDA", 4: "MPH_ERR_UNSUPPORTED",
           5: "MPH_ERR_PARSE", 6: "MPH_ERR_NONFINITE", 7: "MPH_ERR_STATE"}
 BC = {"MovingWall": 0, "NoSlip": 1, "Inflow": 2, "Outflow": 3, "PressureOutlet": 4, "Periodic": 5}
-PRECISION = {"f64": 0, "f64_fast": 1, "f32": 2, "f16s": 3, "bf16s": 4, "f64x": 5, "f16c": 6}
+PRECISION = {"f64": 0, "f64_fast": 1, "f32": 2, "f16s": 3, "bf16s": 4, "f64x": 5, "f16c": 6, "f16w": 7}
 LATTICE_DQ = {"D2Q9": (2, 9), "D3Q15": (3, 15), "D3Q19": (3, 19), "D3Q27": (3, 27)}
 
 # Exported entry points (the declarations of include/mph.h).

@@ -28,7 +28,7 @@ NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-X
 # Translation units that must keep the reference's operation order.
 EXACT_TUS = {"k_f64_exact.cu"}
 HOST_TUS = ["host_config.cpp"]
-DEVICE_TUS = ["k_f64_exact.cu", "k_fast_f64.cu", "k_fast_f32.cu", "k_fast_f16.cu", "k_fast_bf16.cu", "k_fast_f16c.cu", "k_f64x.cu",
+DEVICE_TUS = ["k_f64_exact.cu", "k_fast_f64.cu", "k_fast_f32.cu", "k_fast_f16.cu", "k_fast_bf16.cu", "k_fast_f16c.cu", "k_fast_f16w.cu", "k_f64x.cu",
               "k_f64x_batch.cu", "ceiling.cu", "noalloc.cu", "monitor.cu", "nn.cu", "batch.cu", "sim.cu"]
 
 

@@ -45,10 +45,10 @@ inline std::string get(const mph_inputs* in, const char* key, const std::string&
 
 // mph.precision names of the storage precisions.
 inline int precision_code(const std::string& name) {
-    const char* names[] = {"f64", "f64_fast", "f32", "f16s", "bf16s", "f64x", "f16c"};
+    const char* names[] = {"f64", "f64_fast", "f32", "f16s", "bf16s", "f64x", "f16c", "f16w"};
     const int precs[] = {MPH_PREC_F64, MPH_PREC_F64_FAST, MPH_PREC_F32, MPH_PREC_F16S, MPH_PREC_BF16S, MPH_PREC_F64X,
-                         MPH_PREC_F16C};
-    for (int i = 0; i < 7; ++i)
+                         MPH_PREC_F16C, MPH_PREC_F16W};
+    for (int i = 0; i < 8; ++i)
         if (name == names[i]) return precs[i];
     return -1;
 }

@@ -57,6 +57,9 @@ struct KParams {
     // Window of one step launch: rows [y0, y1) of planes [z0, z1).  The full
     // domain is (0, ny, 0, nz); a host-copy pipeline steps slabs of planes.
     int y0, y1, z0, z1;
+    // Status flag of the handle for storages whose stores can saturate
+    // (StF16W sets bit 4); nullptr otherwise.
+    int* flag;
 };
 
 // Parameters in the compute type R of a collide.
@@ -92,6 +95,7 @@ struct KParamsX {
 struct StF64 {
     using T = double;
     static constexpr bool kShift = false;
+    static constexpr bool kPerPop = false, kRange = false;
     using R = double;
     template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int, unsigned e) { return __ldg(f + e); }
     template <int Q> static __device__ __forceinline__ void ste(T* __restrict__ f, int, unsigned e, R v) { f[e] = v; }
@@ -107,6 +111,7 @@ struct StF64 {
 struct StF32 {
     using T = float;
     static constexpr bool kShift = false;
+    static constexpr bool kPerPop = false, kRange = false;
     using R = float;
     template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int, unsigned e) { return __ldg(f + e); }
     template <int Q> static __device__ __forceinline__ void ste(T* __restrict__ f, int, unsigned e, R v) { f[e] = v; }
@@ -127,6 +132,7 @@ struct StF16S {
     // Shifted kernels work on g = f - w directly: one value (ldr1/str1) or an
     // aligned pair of neighbouring cells (ldr2/str2, e even).
     static constexpr bool kShift = true;
+    static constexpr bool kPerPop = false, kRange = false;
     static __device__ __forceinline__ float ldr1(const T* __restrict__ f, unsigned e) { return __half2float(f[e]); }
     static __device__ __forceinline__ float2 ldr2(const T* __restrict__ f, unsigned e) {
         return __half22float2(*reinterpret_cast<const __half2*>(f + e));
@@ -161,6 +167,7 @@ struct StBF16S {
     using T = __nv_bfloat16;
     using R = float;
     static constexpr bool kShift = true;
+    static constexpr bool kPerPop = false, kRange = false;
     // bf16 is the high half of an FP32 word: widening is a shift / mask.
     static __device__ __forceinline__ float ldr1(const T* __restrict__ f, unsigned e) {
         return __uint_as_float((unsigned)__ldg(reinterpret_cast<const unsigned short*>(f) + e) << 16);
@@ -226,6 +233,7 @@ struct StF16C {
     using T = unsigned short;
     using R = float;
     static constexpr bool kShift = true;
+    static constexpr bool kPerPop = false, kRange = false;
     static __device__ __forceinline__ float ldr1(const T* __restrict__ f, unsigned e) { return f16c::decode(__ldg(f + e)); }
     static __device__ __forceinline__ float dec1(unsigned h) { return f16c::decode(h); }
     static __device__ __forceinline__ float2 dec2(unsigned w) {
@@ -257,6 +265,138 @@ struct StF16C {
     }
 };
 
+// Shifted, weight-scaled custom 16-bit float (MPH_PREC_F16W): the deviation
+// x_n = (f_n - w_n) / p_n, p_n the power of two nearest to w_n (0.75 w_n <=
+// p_n <= 1.125 w_n on every lattice), as sign, 3 exponent bits with bias 8
+// and 12 stored mantissa bits.  Divided by
+// (about) its weight, every population's deviation is of the same size
+// (about 3 |c.u| + |rho - 1|), so eight binades of exponent cover the range
+// and the bit saved on the exponent goes to the significand: 13 significant
+// bits against the 12 of StF16C.  Normals span 2^-7 up to 1 - 2^-13,
+// subnormals are multiples of 2^-19 (the resolution of the small deviations
+// of the rest and cross-flow populations, which carry the pressure); from
+// 1 - 2^-14 up a magnitude saturates at the largest value and the step sets
+// bit 2 (value 4) of the handle's flag: every population must stay inside
+// (w_n - p_n, w_n + p_n), which holds for |u| up to about 0.1 in any
+// direction (a lid at 0.1 included) and fails in an unstable run.
+// The scale is a power of two so that decoding inverts encoding exactly: with
+// w_n itself, the FP32-rounded w_n times its exact inverse differs from 1 by
+// up to 2^-24, and that factor on every deviation compounds step after step
+// (measured: a steady kinetic-energy drift of 3e-5 per 1000 steps of a 3-D
+// Taylor-Green vortex).  Conversions are bit arithmetic around one FP32
+// multiply by a power of two (no denormal flushing in these units):
+//   decode: the 15 magnitude bits placed at FP32 bit 11 read as the FP32
+//           number 2^(e-127)(1 + m/2^12) (a subnormal for e = 0); times
+//           p_n 2^(127-8) it is g_n = f_n - w_n;
+//   encode: g_n times 2^(8-127) / p_n, then the FP32 bits rounded to nearest
+//           even at bit 11.
+namespace f16w {
+// log2 p_n by weight class |c_n|^2 (D2Q9 4/9, 1/9, 1/36 -> 1/2, 1/8, 1/32;
+// D3Q15 2/9, 1/9, 1/72 -> 1/4, 1/8, 1/64; D3Q19 1/3, 1/18, 1/36 -> 1/4,
+// 1/16, 1/32; D3Q27 8/27, 2/27, 1/54, 1/216 -> 1/4, 1/16, 1/64, 1/256).  The
+// scales are built from exponent bits, so an unrolled loop over n sees
+// immediate constants.
+template <int Q> __device__ __forceinline__ constexpr int lp(int n) {
+    using L = Lat<Q>;
+    const int k = L::cx(n) * L::cx(n) + L::cy(n) * L::cy(n) + L::cz(n) * L::cz(n);
+    return Q == 9 ? (k == 0 ? -1 : k == 1 ? -3 : -5)
+         : Q == 15 ? (k == 0 ? -2 : k == 1 ? -3 : -6)
+         : Q == 19 ? (k == 0 ? -2 : k == 1 ? -4 : -5)
+                   : (k == 0 ? -2 : k == 1 ? -4 : k == 2 ? -6 : -8);
+}
+// p_n 2^119 and 2^-119 / p_n
+template <int Q> __device__ __forceinline__ float dscale(int n) { return __int_as_float((lp<Q>(n) + 246) << 23); }
+template <int Q> __device__ __forceinline__ float escale(int n) { return __int_as_float((8 - lp<Q>(n)) << 23); }
+template <int Q> __device__ __forceinline__ float decode(int n, unsigned h) {
+    return __fmul_rn(__uint_as_float(((h & 0x8000u) << 16) | ((h & 0x7FFFu) << 11)), dscale<Q>(n));
+}
+// sat collects the unclamped magnitude codes: above 0x7FFF a value saturated.
+template <int Q> __device__ __forceinline__ unsigned encode(int n, float g, unsigned& sat) {
+    const unsigned u = __float_as_uint(__fmul_rn(g, escale<Q>(n)));
+    const unsigned a = u & 0x7FFFFFFFu;
+    const unsigned r = (a + 0x3FFu + ((a >> 11) & 1u)) >> 11;
+    sat |= r;
+    return ((u >> 16) & 0x8000u) | (r > 0x7FFFu ? 0x7FFFu : r);
+}
+}  // namespace f16w
+
+struct StF16W {
+    using T = unsigned short;
+    using R = float;
+    static constexpr bool kShift = true;
+    // the raw codec takes the population index; stores report saturation
+    static constexpr bool kPerPop = true, kRange = true;
+    template <int Q> static __device__ __forceinline__ float dec1(int n, unsigned h) { return f16w::decode<Q>(n, h); }
+    template <int Q> static __device__ __forceinline__ float2 dec2(int n, unsigned w) {
+        return make_float2(f16w::decode<Q>(n, w & 0xFFFFu), f16w::decode<Q>(n, w >> 16));
+    }
+    template <int Q> static __device__ __forceinline__ float ldr1(int n, const T* __restrict__ f, unsigned e) {
+        return f16w::decode<Q>(n, __ldg(f + e));
+    }
+    template <int Q> static __device__ __forceinline__ float2 ldr2(int n, const T* __restrict__ f, unsigned e) {
+        return dec2<Q>(n, __ldg(reinterpret_cast<const unsigned*>(f + e)));
+    }
+    template <int Q>
+    static __device__ __forceinline__ void str1(int n, T* __restrict__ f, unsigned e, float v, unsigned& sat) {
+        f[e] = (unsigned short)f16w::encode<Q>(n, v, sat);
+    }
+    template <int Q>
+    static __device__ __forceinline__ void str2(int n, T* __restrict__ f, unsigned e, float2 v, unsigned& sat) {
+        *reinterpret_cast<unsigned*>(f + e) = f16w::encode<Q>(n, v.x, sat) | (f16w::encode<Q>(n, v.y, sat) << 16);
+    }
+    // FP32 population f_n = w_n + g_n for the auxiliary kernels (moments,
+    // sums, initialisation, host transfers); their stores saturate without
+    // the flag (initial states are checked by the first step's stores).
+    template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int n, unsigned e) {
+        return ldr1<Q>(n, f, e) + (float)Lat<Q>::w(n);
+    }
+    template <int Q> static __device__ __forceinline__ void ste(T* __restrict__ f, int n, unsigned e, R v) {
+        unsigned sat = 0;
+        str1<Q>(n, f, e, v - (float)Lat<Q>::w(n), sat);
+    }
+    template <int Q> static __device__ __forceinline__ R ld(const T* __restrict__ f, int n, long long i, long long N) {
+        return ldr1<Q>(n, f, (unsigned)(n * N + i)) + (float)Lat<Q>::w(n);
+    }
+    template <int Q> static __device__ __forceinline__ void st(T* __restrict__ f, int n, long long i, long long N, R v) {
+        unsigned sat = 0;
+        f[n * N + i] = (unsigned short)f16w::encode<Q>(n, v - (float)Lat<Q>::w(n), sat);
+    }
+    template <int Q> static __device__ __forceinline__ R rt(int n, R v) {
+        unsigned sat = 0;
+        return f16w::decode<Q>(n, f16w::encode<Q>(n, v - (float)Lat<Q>::w(n), sat)) + (float)Lat<Q>::w(n);
+    }
+};
+
+// Raw loads and stores of the shifted value g_n of population n for any
+// shifted policy (the per-population codec of StF16W takes n; the others
+// ignore it), and the saturation report of the stores.
+template <int Q, class St>
+__device__ __forceinline__ float sh_ld1(int n, const typename St::T* __restrict__ f, unsigned e) {
+    if constexpr (St::kPerPop) return St::template ldr1<Q>(n, f, e);
+    else return St::ldr1(f, e);
+}
+template <int Q, class St>
+__device__ __forceinline__ float2 sh_ld2(int n, const typename St::T* __restrict__ f, unsigned e) {
+    if constexpr (St::kPerPop) return St::template ldr2<Q>(n, f, e);
+    else return St::ldr2(f, e);
+}
+template <int Q, class St>
+__device__ __forceinline__ void sh_st1(int n, typename St::T* __restrict__ f, unsigned e, float v, unsigned& sat) {
+    if constexpr (St::kPerPop) St::template str1<Q>(n, f, e, v, sat);
+    else St::str1(f, e, v);
+}
+template <int Q, class St>
+__device__ __forceinline__ void sh_st2(int n, typename St::T* __restrict__ f, unsigned e, float2 v, unsigned& sat) {
+    if constexpr (St::kPerPop) St::template str2<Q>(n, f, e, v, sat);
+    else St::str2(f, e, v);
+}
+template <class St>
+__device__ __forceinline__ void sh_report(const KParams& p, unsigned sat) {
+    if constexpr (St::kRange) {
+        if (sat > 0x7FFFu) atomicOr(p.flag, 4);
+    }
+}
+
 // 64-bit fixed point (MPH_PREC_F64X): the stored integer is h_n = f_n / w_n
 // in units of 2^-56.  Loads and stores convert to/from FP64 for the
 // auxiliary kernels (moments, init, sums, host transfers); the step kernel of
@@ -265,6 +405,7 @@ constexpr int kFxShift = 56;
 struct StF64X {
     using T = long long;
     static constexpr bool kShift = false;
+    static constexpr bool kPerPop = false, kRange = false;
     using R = double;
     template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int n, unsigned e) {
         return ((double)__ldg(f + e) * 0x1p-56) / Lat<Q>::iw(n);
@@ -436,7 +577,7 @@ __device__ __forceinline__ void pull_shift_interior(const KParams& p, const type
     const Nbr o = neighbours<L::D>(p, x, y, z);
     const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
 #pragma unroll
-    for (int n = 0; n < Q; ++n) g[n] = St::ldr1(fin, (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(o, n)));
+    for (int n = 0; n < Q; ++n) g[n] = sh_ld1<Q, St>(n, fin, (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(o, n)));
 }
 
 // Pull of all Q populations into f.  Cells away from non-periodic faces use
@@ -765,7 +906,7 @@ __device__ __forceinline__ void pull_shift(const KParams& p, const KParams* __re
     if (!o.wall && !(p.cls && p.cls[c] != kFluid)) {
         const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
 #pragma unroll
-        for (int n = 0; n < Q; ++n) g[n] = St::ldr1(fin, (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(o, n)));
+        for (int n = 0; n < Q; ++n) g[n] = sh_ld1<Q, St>(n, fin, (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(o, n)));
     } else {
         pull_edge<Q, St>(p, pg, fin, x, y, z, c, g);
 #pragma unroll
@@ -782,9 +923,10 @@ __device__ __forceinline__ void step_cell(const KParams& p, const KParams* __res
     const long long c = ((long long)z * p.ny + y) * p.nx + x;
     const unsigned N = (unsigned)p.ncell, ci = (unsigned)c;
     if (p.cls && p.cls[c] == kSolid) {  // obstacle cell: rest state f = w
+        unsigned sat = 0;
 #pragma unroll
         for (int n = 0; n < Q; ++n) {
-            if constexpr (St::kShift) St::str1(fout, (unsigned)n * N + ci, 0.0f);
+            if constexpr (St::kShift) sh_st1<Q, St>(n, fout, (unsigned)n * N + ci, 0.0f, sat);
             else St::template ste<Q>(fout, n, (unsigned)n * N + ci, (typename St::R)Lat<Q>::w(n));
         }
         return;
@@ -793,8 +935,10 @@ __device__ __forceinline__ void step_cell(const KParams& p, const KParams* __res
         float g[Q];
         pull_shift<Q, St>(p, pg, fin, x, y, z, c, g);
         collide_shift<Q, A1, FORCED>(p, g);
+        unsigned sat = 0;
 #pragma unroll
-        for (int n = 0; n < Q; ++n) St::str1(fout, (unsigned)n * N + ci, g[n]);
+        for (int n = 0; n < Q; ++n) sh_st1<Q, St>(n, fout, (unsigned)n * N + ci, g[n], sat);
+        sh_report<St>(p, sat);
     } else {
         R f[Q];
         pull<Q, St>(p, pg, fin, x, y, z, c, f);
@@ -855,10 +999,10 @@ __global__ void __launch_bounds__(256, 3) k_step_pair(const typename St::T* __re
         for (int n = 0; n < Q; ++n) {
             const unsigned ea = (unsigned)n * N + (unsigned)((int)ci + upstream<Q>(oa, n));
             if (L::cx(n) == 0) {
-                g[n] = St::ldr2(fin, ea);
+                g[n] = sh_ld2<Q, St>(n, fin, ea);
             } else {
                 const unsigned eb = ea + 1u + (unsigned)(L::cx(n) == 1 ? dxm : dxp);
-                g[n] = make_float2(St::ldr1(fin, ea), St::ldr1(fin, eb));
+                g[n] = make_float2(sh_ld1<Q, St>(n, fin, ea), sh_ld1<Q, St>(n, fin, eb));
             }
         }
     } else {
@@ -869,8 +1013,10 @@ __global__ void __launch_bounds__(256, 3) k_step_pair(const typename St::T* __re
         for (int n = 0; n < Q; ++n) g[n] = make_float2(ga[n], gb[n]);
     }
     collide_shift<Q, A2, FORCED>(p, g);
+    unsigned sat = 0;
 #pragma unroll
-    for (int n = 0; n < Q; ++n) St::str2(fout, (unsigned)n * N + ci, g[n]);
+    for (int n = 0; n < Q; ++n) sh_st2<Q, St>(n, fout, (unsigned)n * N + ci, g[n], sat);
+    sh_report<St>(p, sat);
 }
 
 // updateMacroscopic (SimulationSetup.cpp:142-166): moments of the streamed

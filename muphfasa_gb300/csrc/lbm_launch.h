@@ -72,6 +72,8 @@ cudaError_t launch_step_fast_bf16s(int q, bool forced, const void* fin, void* fo
                                    const KParams* pg, cudaStream_t s);
 cudaError_t launch_step_fast_f16c(int q, bool forced, const void* fin, void* fout, const KParams& p,
                                   const KParams* pg, cudaStream_t s);
+cudaError_t launch_step_fast_f16w(int q, bool forced, const void* fin, void* fout, const KParams& p,
+                                  const KParams* pg, cudaStream_t s);
 // The 16-bit pair step with bulk-copy staging (bulk_step.cuh): chunks of
 // about `cells` cells of whole rows, `stages` shared-memory stages (2 or 3),
 // total_elems = elements of the population array, flag |= 2 on a wait

@@ -136,6 +136,7 @@ cudaError_t mon_with_store(int prec, F&& f) {
         case MPH_PREC_F16S: return f(StF16S{});
         case MPH_PREC_BF16S: return f(StBF16S{});
         case MPH_PREC_F16C: return f(StF16C{});
+        case MPH_PREC_F16W: return f(StF16W{});
         case MPH_PREC_F64X: return f(StF64X{});
     }
     return cudaErrorInvalidValue;

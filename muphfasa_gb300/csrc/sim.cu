@@ -22,7 +22,8 @@ struct mph_sim {
     KParamsX kpx;             // fixed-point constants (MPH_PREC_F64X)
     KParams* d_kp = nullptr;  // global copy for the boundary path
     long long* d_kbb = nullptr;  // fixed-point bounce-back constants [27][27]
-    int* d_flag = nullptr;       // range flag of the fixed-point step (1), wait timeout of a staged step (2)
+    int* d_flag = nullptr;       // range flag of the fixed-point step (1), wait timeout of a staged step (2),
+                                 // saturated weight-scaled 16-bit store (4)
     int pipe_ctas = 0;           // resident CTAs of the pipelined fixed-point kernel (0: direct kernel)
     int bulk_stages = 0;         // 16-bit storage: shared-memory stages of the bulk-copy step (0: direct kernel)
     int bulk_cells = 512;        // cells per chunk of the bulk-copy step
@@ -81,7 +82,8 @@ size_t elem_size(int prec) {
         case MPH_PREC_F32: return 4;
         case MPH_PREC_F16S:
         case MPH_PREC_BF16S:
-        case MPH_PREC_F16C: return 2;
+        case MPH_PREC_F16C:
+        case MPH_PREC_F16W: return 2;
     }
     return 0;
 }
@@ -351,6 +353,8 @@ cudaError_t launch_step_window(mph_sim* s, const KParams& kp, bool whole) {
                 return launch_step_fast_bf16s(q, forced, s->fa, s->fb, kp, s->d_kp, s->stream);
             return launch_step_fast_f16c(q, forced, s->fa, s->fb, kp, s->d_kp, s->stream);
         }
+        case MPH_PREC_F16W:
+            return launch_step_fast_f16w(q, forced, s->fa, s->fb, kp, s->d_kp, s->stream);
         case MPH_PREC_F64X:
             if (whole && s->pipe_ctas > 0)
                 return launch_step_f64x_pipe(q, forced, (const long long*)s->fa, (long long*)s->fb, kp, s->kpx,
@@ -363,9 +367,11 @@ cudaError_t launch_step_window(mph_sim* s, const KParams& kp, bool whole) {
 
 cudaError_t launch_one_step(mph_sim* s) { return launch_step_window(s, s->kp, true); }
 
-// Range flag of the fixed-point step: a cell left the representable range.
+// Status flag: a cell of the fixed-point step left the representable range
+// (1), a wait of a staged step timed out (2), a weight-scaled 16-bit store
+// saturated (4).
 int check_flag(mph_sim* s) {
-    if (s->d.precision != MPH_PREC_F64X && s->bulk_stages == 0) return MPH_OK;
+    if (s->d.precision != MPH_PREC_F64X && s->d.precision != MPH_PREC_F16W && s->bulk_stages == 0) return MPH_OK;
     int flag = 0;
     MPH_CK(cudaMemcpyAsync(&flag, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "read flag");
     MPH_CK(cudaStreamSynchronize(s->stream), "read flag");
@@ -374,6 +380,8 @@ int check_flag(mph_sim* s) {
         return fail(MPH_ERR_CUDA, "staged 16-bit step: a wait for bulk-copied operands exceeded its time limit "
                                   "(the step's results are incomplete)");
     }
+    if (flag & 4) return fail(MPH_ERR_NONFINITE, "weight-scaled 16-bit storage: a population deviation "
+                                                   "|f - w| reached 2 w and saturated (or was not finite)");
     if (flag) return fail(MPH_ERR_NONFINITE, "fixed-point step: a cell left the representable range "
                                                "(rho outside (1/16, 64) or |J|, |u| >= 4)");
     return MPH_OK;
@@ -747,6 +755,11 @@ int mph_create(const mph_desc* desc, mph_sim** out) {
     if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
     if (e == cudaSuccess) e = cudaMalloc(&s->fa, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&s->fb, bytes);
+    if (e == cudaSuccess && d.precision == MPH_PREC_F16W) {  // saturation flag of the stores
+        e = cudaMalloc(&s->d_flag, sizeof(int));
+        if (e == cudaSuccess) e = cudaMemset(s->d_flag, 0, sizeof(int));
+        s->kp.flag = s->d_flag;
+    }
     if (e == cudaSuccess) e = cudaMalloc(&s->d_kp, sizeof(KParams));
     if (e == cudaSuccess) e = cudaMemcpy(s->d_kp, &s->kp, sizeof(KParams), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && d.precision == MPH_PREC_F64X) {

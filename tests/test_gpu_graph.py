@@ -18,7 +18,7 @@ def _pair(mph, monkeypatch, desc_fn):
     return plain, graphed
 
 
-@pytest.mark.parametrize("precision", ["f64", "f64x", "f32", "f16s", "f16c"])
+@pytest.mark.parametrize("precision", ["f64", "f64x", "f32", "f16s", "f16c", "f16w"])
 def test_graph_runs_equal_plain_launches(precision, mph, monkeypatch):
     faces = ["NoSlip", "NoSlip", "NoSlip", "MovingWall", "Periodic", "Periodic"]
     U = [[0.0] * 3 for _ in range(6)]

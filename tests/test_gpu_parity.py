@@ -176,11 +176,11 @@ def test_f64x_range_flag_reports_instead_of_wrapping(mph):
 # from a random (non-smooth) field.  Plain FP32 storage rounds f ~ w to 24 bits
 # (measured 3e-6..8e-5); shifted FP16 / BF16 / the custom 1-4-11 format keep
 # 11 / 8 / 12 bits of f - w (measured 1.9e-4..4.2e-4 / 1.4e-3..3.1e-3 /
-# 9.0e-5..1.8e-4).
-TOL_LOWP = {"f32": 3e-4, "f16s": 3e-3, "bf16s": 1.5e-2, "f16c": 1e-3}
+# 9.0e-5..1.8e-4); the weight-scaled 1-3-12 format 13 bits of (f - w) / w.
+TOL_LOWP = {"f32": 3e-4, "f16s": 3e-3, "bf16s": 1.5e-2, "f16c": 1e-3, "f16w": 1e-3}
 
 
-@pytest.mark.parametrize("prec", ["f32", "f16s", "bf16s", "f16c"])
+@pytest.mark.parametrize("prec", ["f32", "f16s", "bf16s", "f16c", "f16w"])
 @pytest.mark.parametrize("case", LONG[:3], ids=[f"{c[0]}_{c[6]}" for c in LONG[:3]])
 def test_reduced_precision_velocity_error(case, prec, mph, oracle_mod):
     lat, n, faces, omega, force, U, steps = case
@@ -309,7 +309,7 @@ def test_plugin_rejects_too_small_array(mph):
     assert L.mph_pull_collide_fused_arr(2, 9, lo, hi, C.byref(a), C.byref(a), 1.0, None, None) == 1
 
 
-@pytest.mark.parametrize("precision", ["f64", "f64x", "f32", "f16s", "f16c"])
+@pytest.mark.parametrize("precision", ["f64", "f64x", "f32", "f16s", "f16c", "f16w"])
 @pytest.mark.parametrize("lat,n", [("D2Q9", (20, 16)), ("D3Q19", (12, 10, 8)), ("D3Q27", (10, 8, 6))])
 def test_zero_force_is_bit_identical_to_unforced(lat, n, precision, mph):
     """The forced kernels with F = 0 reproduce the unforced ones bit for bit

@@ -10,7 +10,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-PREC = ["f64", "f64x", "f32", "f16s", "bf16s", "f16c"]
+PREC = ["f64", "f64x", "f32", "f16s", "bf16s", "f16c", "f16w"]
 CH3 = ["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic", "Periodic"]
 
 
