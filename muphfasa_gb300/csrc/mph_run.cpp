@@ -5,8 +5,8 @@
 //   mph_run <inputs file> [key=value ...]
 //
 // Reads the reference's inputs keys; two extra keys select this build's
-// options: mph.precision (f64 | f64_fast | f32 | f16s | bf16s | f64x, default
-// f64, the reference's arithmetic) and mph.device (default 0).
+// options: mph.precision (f64 | f64_fast | f32 | f16s | bf16s | f64x | f16c |
+// f16w, default f64, the reference's arithmetic) and mph.device (default 0).
 //
 // Output (SimulationSetup.cpp:169-198):
 //   * every amr.plot_int steps a plot directory <amr.plot_file><step:07d>
@@ -48,7 +48,7 @@ int main(int argc, char** argv) {
     ck(mph_inputs_load(argv[1], argc - 2, const_cast<const char* const*>(argv + 2), &in), "inputs");
     const std::string prec_name = get(in, "mph.precision", "f64");
     const int prec = precision_code(prec_name);
-    if (prec < 0) die("mph.precision must be one of f64 f64_fast f32 f16s bf16s f64x");
+    if (prec < 0) die("mph.precision must be one of f64 f64_fast f32 f16s bf16s f64x f16c f16w");
     ck(mph_set_device(std::atoi(get(in, "mph.device", "0").c_str())), "device");
 
     mph_desc d;
