@@ -165,7 +165,11 @@ int mph_get_f(mph_sim* sim, double* f);
  * initialize(); on the forced path rho/u are overwritten with the stored
  * macroscopic fields, as the reference overwrites m_rho/m_vel. */
 int mph_init_fields(mph_sim* sim, double* rho, double* u);
-/* nsteps x SimulationImpl::advance() (SimulationSetup.cpp:120-139). */
+/* nsteps x SimulationImpl::advance() (SimulationSetup.cpp:120-139).  With
+ * MPH_PREC_F64X or MPH_PREC_F16W a state outside the storage's range makes
+ * the call (and every later step call) return MPH_ERR_NONFINITE until the
+ * state is replaced (mph_set_f, mph_init_fields, mph_init_fields_neq,
+ * mph_set_state clear the handle's status). */
 int mph_advance(mph_sim* sim, int nsteps);
 /* updateMacroscopic (SimulationSetup.cpp:142-166): (rho, u) of the streamed,
  * pre-collision populations; u includes F/2 on the forced path. */

@@ -831,9 +831,20 @@ int mph_destroy(mph_sim* s) {
     return MPH_OK;
 }
 
+namespace {
+// A new state clears the status flag (range, saturation, wait timeout) that
+// the steps of the previous state raised.
+int clear_status(mph_sim* s) {
+    if (s->d_flag) MPH_CK(cudaMemsetAsync(s->d_flag, 0, sizeof(int), s->stream), "clear status flag");
+    return MPH_OK;
+}
+}  // namespace
+
 int mph_set_f(mph_sim* s, const double* f) {
     if (!s || !f) return fail(MPH_ERR_ARG, "mph_set_f: NULL argument");
-    int rc = upload(s, f);
+    int rc = clear_status(s);
+    if (rc) return rc;
+    rc = upload(s, f);
     if (rc) return rc;
     s->has_state = true;
     s->has_uprev = false;
@@ -851,6 +862,7 @@ int mph_get_f(mph_sim* s, double* f) {
 int mph_init_fields(mph_sim* s, double* rho, double* u) {
     if (!s || !rho || !u) return fail(MPH_ERR_ARG, "mph_init_fields: NULL argument");
     int rc = ensure_macro(s);
+    if (!rc) rc = clear_status(s);
     if (rc) return rc;
     const long long N = s->kp.ncell;
     MPH_CK(cudaMemcpyAsync(s->d_rho, rho, sizeof(double) * N, cudaMemcpyHostToDevice, s->stream), "init upload rho");
@@ -870,6 +882,7 @@ int mph_init_fields_neq(mph_sim* s, const double* rho, const double* u) {
     if (!s || !rho || !u) return fail(MPH_ERR_ARG, "mph_init_fields_neq: NULL argument");
     if (s->d.forced) return fail(MPH_ERR_UNSUPPORTED, "mph_init_fields_neq: forced domains are not supported");
     int rc = ensure_macro(s);
+    if (!rc) rc = clear_status(s);
     if (rc) return rc;
     const long long N = s->kp.ncell;
     MPH_CK(cudaMemcpyAsync(s->d_rho, rho, sizeof(double) * N, cudaMemcpyHostToDevice, s->stream), "init upload rho");
@@ -991,6 +1004,8 @@ int mph_set_state(mph_sim* s, const void* buf, long long bytes) {
     if (!s || !buf) return fail(MPH_ERR_ARG, "mph_set_state: NULL argument");
     const long long n = (long long)(s->elem * (size_t)s->d.q * (size_t)s->kp.ncell);
     if (bytes != n) return fail(MPH_ERR_ARG, "mph_set_state: size differs from mph_state_bytes");
+    const int rc = clear_status(s);
+    if (rc) return rc;
     MPH_CK(cudaMemcpyAsync(s->fa, buf, (size_t)n, cudaMemcpyHostToDevice, s->stream), "upload state");
     s->has_state = true;
     s->has_uprev = false;

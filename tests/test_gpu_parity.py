@@ -161,7 +161,9 @@ def test_f64x_pipelined_kernel_equals_direct_kernel(case, mph, monkeypatch):
 
 def test_f64x_range_flag_reports_instead_of_wrapping(mph):
     """Fault injection on the host: a near-vacuum state (rho = 1e-3, below the
-    fixed-point range) makes the step report MPH_ERR_NONFINITE."""
+    fixed-point range) makes the step report MPH_ERR_NONFINITE, and keeps
+    reporting it until a new state replaces the bad one; then the same handle
+    steps normally."""
     d = mph.make_desc("D3Q19", (8, 8, 8), 1.2, precision="f64x")
     s = mph.Simulation(d)
     N = 8 * 8 * 8
@@ -169,6 +171,12 @@ def test_f64x_range_flag_reports_instead_of_wrapping(mph):
     with pytest.raises(mph.MphError) as e:
         s.advance(1)
     assert e.value.code == 6
+    with pytest.raises(mph.MphError) as e:
+        s.advance(1)
+    assert e.value.code == 6
+    s.initialize(np.ones(N), np.zeros(3 * N))
+    s.advance(3)
+    assert np.allclose(s.f().reshape(19, N).sum(axis=0), 1.0, atol=1e-14)
 
 
 # Reduced precisions: velocity error relative to the FP64 oracle, L2 over the
