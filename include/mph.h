@@ -83,8 +83,8 @@ extern "C" {
  * puts every population's deviation on one scale, so the exponent needs one
  * bit less than MPH_PREC_F16C and the significand gets it.  Populations must
  * stay inside (w_i - p_i, w_i + p_i), p_i >= 0.75 w_i (|u| up to about 0.1):
- * a store that saturates makes the step report MPH_ERR_NONFINITE.
- * Single domains only (a batch rejects it). */
+ * a store that saturates makes the step report MPH_ERR_NONFINITE.  Single
+ * domains and batches (the bulk-copy staged variants do not take it). */
 #define MPH_PREC_F16W 7
 
 /* ---- lattice-unit description of one domain ---------------------------- */
@@ -265,9 +265,9 @@ int mph_bc_fill_arr(int dim, int q, const int dom_lo[3], const int dom_hi[3],
  * precision (any MPH_PREC_*) and forcing flag; each has its own size,
  * omega, boundary faces and force.  Domain d's results equal those of a
  * single handle created from descs[d], bit for bit.  With MPH_PREC_F64X a
- * cell leaving the fixed-point range makes the advance return
- * MPH_ERR_NONFINITE, as for a single handle, and flags its domain
- * (mph_batch_range_flags). */
+ * cell leaving the fixed-point range (with MPH_PREC_F16W a saturating store)
+ * makes the advance return MPH_ERR_NONFINITE, as for a single handle, and
+ * flags its domain (mph_batch_range_flags). */
 typedef struct mph_batch mph_batch;
 int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out);
 int mph_batch_destroy(mph_batch* b);
@@ -293,9 +293,10 @@ int mph_batch_set_obstacles(mph_batch* b, int domain, const unsigned char* mask)
  * change of domain d's stored-population velocity since the previous call
  * (+inf on the first call after an init), out[2 d + 1] = ||u_d||_2. */
 int mph_batch_residual(mph_batch* b, double* out);
-/* Fixed-point batches (MPH_PREC_F64X): flags[d] = 1 for every domain d
- * whose populations left the representable range in an advance since the
- * domain was last initialised or set (mph_batch_advance then returned
+/* Fixed-point and weight-scaled 16-bit batches (MPH_PREC_F64X,
+ * MPH_PREC_F16W): flags[d] = 1 for every domain d whose populations left
+ * the representable range in an advance since the domain was last
+ * initialised or set (mph_batch_advance then returned
  * MPH_ERR_NONFINITE, and mph_batch_residual reports NaN for it).  The other
  * domains stepped normally: a caller can drop the flagged ones and go on.
  * All zero for other precisions.  No counterpart in the reference (its

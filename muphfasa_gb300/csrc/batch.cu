@@ -55,6 +55,8 @@ cudaError_t launch_batch(int prec, int q, bool forced, int K, bool P, const void
             return launch_batch_bf16s(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
         case MPH_PREC_F16C:
             return launch_batch_f16c(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
+        case MPH_PREC_F16W:
+            return launch_batch_f16w(q, forced, K, P, fin, fout, chunks, nchunks, walls, nwalls, dp, offs, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -67,7 +69,8 @@ size_t elem_of(int prec) {
         case MPH_PREC_F32: return 4;
         case MPH_PREC_F16S:
         case MPH_PREC_BF16S:
-        case MPH_PREC_F16C: return 2;
+        case MPH_PREC_F16C:
+        case MPH_PREC_F16W: return 2;
     }
     return 0;
 }
@@ -87,9 +90,14 @@ constexpr int kBulkCand = 6;
 constexpr int kBulkCells = 512;  // cells per row chunk of the staged kernel
 constexpr int kBulkStages = 3;
 
-bool shifted(int prec) { return prec == MPH_PREC_F16S || prec == MPH_PREC_BF16S || prec == MPH_PREC_F16C; }
+bool shifted(int prec) {
+    return prec == MPH_PREC_F16S || prec == MPH_PREC_BF16S || prec == MPH_PREC_F16C || prec == MPH_PREC_F16W;
+}
+// Per-domain status flags: the fixed-point range flag and the saturation
+// flag of the weight-scaled 16-bit storage.
+bool per_domain_flags(int prec) { return prec == MPH_PREC_F64X || prec == MPH_PREC_F16W; }
 bool candidate_ok(int prec, int cand) {
-    if (cand == kBulkCand) return shifted(prec);
+    if (cand == kBulkCand) return shifted(prec) && prec != MPH_PREC_F16W;
     if (shifted(prec)) return cand % 3 != 0;
     if (prec == MPH_PREC_F64X) return cand % 3 != 2;
     return true;
@@ -376,7 +384,7 @@ int autotune(mph_batch* b) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->fa, save, bytes, cudaMemcpyDeviceToDevice, b->stream);
     // only the steps of the caller's advances report the range flag
     if (e == cudaSuccess && b->d_flag)
-        e = cudaMemsetAsync(b->d_flag, 0, sizeof(int) * (b->prec == MPH_PREC_F64X ? b->ndom : 1), b->stream);
+        e = cudaMemsetAsync(b->d_flag, 0, sizeof(int) * (per_domain_flags(b->prec) ? b->ndom : 1), b->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     cudaFree(save);
     if (e != cudaSuccess) return cuda_fail(e, "autotune");
@@ -432,11 +440,12 @@ int ensure_graph(mph_batch* b) {
     return MPH_OK;
 }
 
-// Range flags of the fixed-point step, one per domain (read and cleared
-// after an advance, kept in bad_h).
+// Range flags of the fixed-point step and saturation flags of the
+// weight-scaled 16-bit storage, one per domain (read and cleared after an
+// advance, kept in bad_h).
 int check_flag(mph_batch* b) {
     if (!b->d_flag) return MPH_OK;
-    if (b->prec != MPH_PREC_F64X) {  // the staged 16-bit kernel: 2 = a wait timed out
+    if (!per_domain_flags(b->prec)) {  // the staged 16-bit kernel: 2 = a wait timed out
         int f = 0;
         MPH_CK(cudaMemcpyAsync(&f, b->d_flag, sizeof(int), cudaMemcpyDeviceToHost, b->stream), "read flag");
         MPH_CK(cudaStreamSynchronize(b->stream), "read flag");
@@ -458,6 +467,11 @@ int check_flag(mph_batch* b) {
         }
     if (nbad) {
         MPH_CK(cudaMemsetAsync(b->d_flag, 0, sizeof(int) * b->ndom, b->stream), "clear flag");
+        if (b->prec == MPH_PREC_F16W)
+            return fail(MPH_ERR_NONFINITE, "weight-scaled 16-bit batch step: a population of " + std::to_string(nbad) +
+                                               " domain(s) (first: " + std::to_string(first) +
+                                               ") saturated (|f - w| reached the format's range, or was not "
+                                               "finite); mph_batch_range_flags lists them");
         return fail(MPH_ERR_NONFINITE, "fixed-point batch step: a cell of " + std::to_string(nbad) +
                                            " domain(s) (first: " + std::to_string(first) +
                                            ") left the representable range (rho outside (1/16, 64) or |J|, "
@@ -552,6 +566,12 @@ int mph_batch_create(int ndomains, const mph_desc* descs, mph_batch** out) {
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
     if (e == cudaSuccess) e = cudaMalloc(&b->fa, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&b->fb, bytes);
+    if (e == cudaSuccess && b->prec == MPH_PREC_F16W) {  // per-domain saturation flags
+        e = cudaMalloc(&b->d_flag, sizeof(int) * ndomains);
+        if (e == cudaSuccess) e = cudaMemset(b->d_flag, 0, sizeof(int) * ndomains);
+        for (int d = 0; d < ndomains; ++d) b->params_h[d].flag = b->d_flag + d;
+        b->bad_h.assign(ndomains, 0);
+    }
     if (e == cudaSuccess) e = cudaMalloc(&b->d_params, sizeof(KParams) * ndomains);
     if (e == cudaSuccess) e = cudaMemcpy(b->d_params, b->params_h.data(), sizeof(KParams) * ndomains, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_offs, sizeof(long long) * ndomains);
@@ -673,6 +693,7 @@ int mph_batch_advance_looped_timed(mph_batch* b, int nsteps, float* ms) {
                 case MPH_PREC_F16S: e = launch_step_fast_f16s(b->q, b->forced, in, outp, kp, pg, b->stream); break;
                 case MPH_PREC_BF16S: e = launch_step_fast_bf16s(b->q, b->forced, in, outp, kp, pg, b->stream); break;
                 case MPH_PREC_F16C: e = launch_step_fast_f16c(b->q, b->forced, in, outp, kp, pg, b->stream); break;
+                case MPH_PREC_F16W: e = launch_step_fast_f16w(b->q, b->forced, in, outp, kp, pg, b->stream); break;
                 case MPH_PREC_F64X:
                     e = launch_step_f64x(b->q, b->forced, (const long long*)in, (long long*)outp, kp, b->px_h[d], pg,
                                          b->d_kbb + (size_t)d * 27 * 27, b->d_flag + d, b->stream);

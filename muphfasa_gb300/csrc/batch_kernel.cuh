@@ -95,21 +95,23 @@ __global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __rest
                     for (int n = 0; n < Q; ++n) {
                         const unsigned ea = (unsigned)n * N + (unsigned)(ca[j] + upstream<Q>(oa, n));
                         if (L::cx(n) == 0) {
-                            g[j][n] = St::ldr2(fin, ea);
+                            g[j][n] = sh_ld2<Q, St>(n, fin, ea);
                         } else {
                             const unsigned eb = ea + 1u + (unsigned)(L::cx(n) == 1 ? dxm : dxp);
-                            g[j][n] = make_float2(St::ldr1(fin, ea), St::ldr1(fin, eb));
+                            g[j][n] = make_float2(sh_ld1<Q, St>(n, fin, ea), sh_ld1<Q, St>(n, fin, eb));
                         }
                     }
                 }
             }
+            unsigned sat = 0;
 #pragma unroll
             for (int j = 0; j < P; ++j) {
                 if (!oka[j]) continue;
                 collide_shift<Q, A2, FORCED>(p, g[j]);
 #pragma unroll
-                for (int n = 0; n < Q; ++n) St::str2(fout, (unsigned)n * N + (unsigned)ca[j], g[j][n]);
+                for (int n = 0; n < Q; ++n) sh_st2<Q, St>(n, fout, (unsigned)n * N + (unsigned)ca[j], g[j][n], sat);
             }
+            sh_report<St>(p, sat);
             continue;
         }
 #pragma unroll
@@ -131,6 +133,7 @@ __global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __rest
                 for (int n = 0; n < Q; ++n) g[j][n] = make_float2(a[n], okb[j] ? b[n] : a[n]);
             }
         }
+        unsigned sat = 0;
 #pragma unroll
         for (int j = 0; j < P; ++j) {
             if (!oka[j]) continue;
@@ -139,13 +142,14 @@ __global__ void __launch_bounds__(256) k_batch_step(const typename St::T* __rest
             for (int n = 0; n < Q; ++n) {
                 const unsigned e = (unsigned)n * N + (unsigned)ca[j];
                 if (okb[j] && (e & 1u) == 0) {
-                    St::str2(fout, e, g[j][n]);
+                    sh_st2<Q, St>(n, fout, e, g[j][n], sat);
                 } else {
-                    St::str1(fout, e, g[j][n].x);
-                    if (okb[j]) St::str1(fout, e + 1, g[j][n].y);
+                    sh_st1<Q, St>(n, fout, e, g[j][n].x, sat);
+                    if (okb[j]) sh_st1<Q, St>(n, fout, e + 1, g[j][n].y, sat);
                 }
             }
         }
+        sh_report<St>(p, sat);
     } else {
         R f[K][Q];
         int cc[K];
@@ -265,6 +269,7 @@ MPH_DECL_BATCH(launch_batch_f32)
 MPH_DECL_BATCH(launch_batch_f16s)
 MPH_DECL_BATCH(launch_batch_bf16s)
 MPH_DECL_BATCH(launch_batch_f16c)
+MPH_DECL_BATCH(launch_batch_f16w)
 #undef MPH_DECL_BATCH
 // The 16-bit storages' batch step with bulk-copy staging of the pull
 // operands (bulk_step.cuh): `stages` 2 or 3, lpad = elements of one staged

@@ -7,11 +7,11 @@
 //   mph_batch_run <inputs file> [<inputs file> ...] [key=value ...]
 //
 // Every key=value override applies to every domain.  Extra keys:
-//   mph.precision  f64 | f64_fast | f64x | f32 | f16s | bf16s | f16c (default
-//                  f64, the reference's arithmetic; one precision for the
-//                  batch).  With f64x a domain whose populations leave the
-//                  fixed-point range stops there and is reported "diverged";
-//                  the others go on.
+//   mph.precision  f64 | f64_fast | f64x | f32 | f16s | bf16s | f16c | f16w
+//                  (default f64, the reference's arithmetic; one precision
+//                  for the batch).  With f64x (f16w) a domain whose
+//                  populations leave the fixed-point (16-bit) range stops
+//                  there and is reported "diverged"; the others go on.
 //   mph.device     CUDA device (default 0)
 //   mph.tol        > 0: a domain also stops once the steady-state residual
 //                  (relative change of its velocity over mph.check_every
@@ -49,7 +49,7 @@ struct Domain {
     int last = 0;         // last loop step (max_step, or the stop-time bound)
     int done_step = -1;   // loop step at which the domain stopped (-1: running)
     double residual = NAN;
-    bool diverged = false;  // left the fixed-point range (f64x)
+    bool diverged = false;  // left the storage's range (f64x, f16w)
     std::string dir, plot_prefix;
 };
 
@@ -89,7 +89,7 @@ int main(int argc, char** argv) {
         if (i == 0) {
             prec_name = get(in, "mph.precision", "f64");
             prec = precision_code(prec_name);
-            if (prec < 0) die("mph.precision must be one of f64 f64_fast f64x f32 f16s bf16s f16c");
+            if (prec < 0) die("mph.precision must be one of f64 f64_fast f64x f32 f16s bf16s f16c f16w");
             device = std::atoi(get(in, "mph.device", "0").c_str());
             tol = std::atof(get(in, "mph.tol", "0").c_str());
             check_every = std::atoi(get(in, "mph.check_every", "100").c_str());
@@ -144,8 +144,8 @@ int main(int argc, char** argv) {
         }
         if (next == INT_MAX) break;
         const int rc = mph_batch_advance(b, next - step);
-        if (rc == MPH_ERR_NONFINITE && prec == MPH_PREC_F64X) {
-            // domains that left the fixed-point range stop where they are
+        if (rc == MPH_ERR_NONFINITE && (prec == MPH_PREC_F64X || prec == MPH_PREC_F16W)) {
+            // domains that left the storage's range stop where they are
             std::vector<int> flags(dom.size(), 0);
             ck(mph_batch_range_flags(b, flags.data()), "range flags");
             for (size_t i = 0; i < dom.size(); ++i)
@@ -178,7 +178,7 @@ int main(int argc, char** argv) {
     for (size_t i = 0; i < dom.size(); ++i) {
         const Domain& m = dom[i];
         if (m.diverged) {
-            std::cout << "domain " << i << " " << m.inputs << ": diverged (left the fixed-point range) by step "
+            std::cout << "domain " << i << " " << m.inputs << ": diverged (left the storage's range) by step "
                       << m.done_step + 1 << "\n";
             continue;
         }

@@ -18,7 +18,7 @@ def _cavity(mph, n, omega, lid, precision, lattice="D2Q9"):
     return mph.make_desc(lattice, n, omega, faces=faces, face_U=U, precision=precision)
 
 
-@pytest.mark.parametrize("precision", ["f64", "f32", "f16s", "f64x", "f16c"])
+@pytest.mark.parametrize("precision", ["f64", "f32", "f16s", "f64x", "f16c", "f16w"])
 def test_batch_domains_equal_single_handles(precision, mph):
     descs = [_cavity(mph, (17, 17), 1.2, 0.1, precision), _cavity(mph, (64, 48), 1.7, 0.05, precision),
              _cavity(mph, (100, 100), 0.9, 0.1, precision), _cavity(mph, (33, 65), 1.9, 0.08, precision)]
@@ -42,7 +42,7 @@ def test_batch_domains_equal_single_handles(precision, mph):
     assert total == sum(batch.ncells) and kcells in ((1, 2) if precision == "f64x" else (1, 2, 4)) and nchunks > 0
 
 
-@pytest.mark.parametrize("precision", ["f64", "f16s", "bf16s", "f64x", "f16c"])
+@pytest.mark.parametrize("precision", ["f64", "f16s", "bf16s", "f64x", "f16c", "f16w"])
 def test_batch_3d_forced_mixed_boundaries(precision, mph):
     faces_a = ["Periodic", "Periodic", "NoSlip", "NoSlip", "Periodic", "Periodic"]
     faces_b = ["Inflow", "PressureOutlet", "NoSlip", "MovingWall", "Periodic", "Periodic"]
@@ -65,7 +65,7 @@ def test_batch_3d_forced_mixed_boundaries(precision, mph):
         assert np.array_equal(batch.f(i), s.f())
 
 
-@pytest.mark.parametrize("precision", ["f32", "f16s", "bf16s", "f64x", "f16c"])
+@pytest.mark.parametrize("precision", ["f32", "f16s", "bf16s", "f64x", "f16c", "f16w"])
 def test_looped_launches_equal_batched(precision, mph):
     """Per-domain launches (the single-domain kernels, two cells per thread
     for the 16-bit policies on even sides) against the batched kernel; the

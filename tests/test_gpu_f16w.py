@@ -139,8 +139,27 @@ def test_f16w_error_below_f16c_on_a_shear_wave(mph):
     assert err["f16w"] < 0.8 * err["f16c"] and err["f16w"] < 3e-4
 
 
-def test_f16w_batch_is_rejected(mph):
-    """A batch does not take the weight-scaled storage (MPH_ERR_UNSUPPORTED)."""
+def test_f16w_batch_flags_the_saturating_domain(mph):
+    """In a batch, the weight-scaled storage flags the domain whose stores
+    saturate (a forced flow driven past the range) and the advance reports
+    MPH_ERR_NONFINITE; the other domains step on, equal to single handles,
+    and re-initialising the flagged domain clears its flag."""
+    n = (64, 32)
+    N = n[0] * n[1]
+    descs = [mph.make_desc("D2Q9", n, 1.0, faces=["Periodic"] * 6, force=(f, 0.0, 0.0), precision="f16w")
+             for f in (1e-5, 0.05, 2e-5)]
+    b = mph.Batch(descs)
+    u = np.concatenate([np.full(N, 0.2), np.zeros(N)])
+    for d in range(3):
+        b.initialize(d, np.ones(N), u.copy())
     with pytest.raises(mph.MphError) as e:
-        mph.Batch([mph.make_desc("D2Q9", (32, 32), 1.0, precision="f16w")])
-    assert e.value.code == 4
+        b.advance(8)
+    assert e.value.code == 6
+    assert list(b.range_flags()) == [False, True, False]
+    for d in (0, 2):
+        s = mph.Simulation(descs[d])
+        s.initialize(np.ones(N), u.copy())
+        s.advance(8)
+        assert np.array_equal(b.f(d), s.f())
+    b.initialize(1, np.ones(N), np.zeros(2 * N))
+    assert not b.range_flags().any()
