@@ -42,7 +42,7 @@ LATTICE_Q = {"D2Q9": 9, "D3Q15": 15, "D3Q19": 19, "D3Q27": 27}
 ELEM = {"f64": 8, "f64_fast": 8, "f32": 4, "f16s": 2, "bf16s": 2, "f64x": 8, "f16c": 2, "f16w": 2}
 DTYPE = {"f64": "f64", "f64_fast": "f64", "f32": "f32", "f16s": "f16 storage / f32 arithmetic",
          "bf16s": "bf16 storage / f32 arithmetic", "f16c": "custom 1-4-11 16-bit storage / f32 arithmetic",
-         "f16w": "custom 1-3-12 16-bit storage of (f - w) / w / f32 arithmetic",
+         "f16w": "custom 1-3-12 16-bit storage of (f - w) / p, p the power of two nearest to w / f32 arithmetic",
          "f64x": "int64 fixed point (f/w in units of 2^-56), FP64-accurate"}
 METRIC = "MLUPS"
 
