@@ -22,7 +22,7 @@ import time
 
 import numpy as np
 
-from . import Batch, MphError, make_desc, set_device
+from . import Batch, MphError, lattice_tables, make_desc, set_device
 
 RE = (100.0, 2000.0)
 U = (0.02, 0.1)
@@ -131,7 +131,6 @@ def _batch(cases, precision):
 
 def _feq_d2q9(rho, u, n):
     """Equilibrium populations [9][n*n] of (rho, u) (D2Q9, u = [ux..., uy...])."""
-    from . import lattice_tables
     c, w, _ = lattice_tables("D2Q9")
     ux, uy = u[: n * n], u[n * n:]
     usq = ux * ux + uy * uy
@@ -140,7 +139,7 @@ def _feq_d2q9(rho, u, n):
 
 
 def _moments_d2q9(f, n):
-    from . import lattice_tables
+    """(rho, u) of populations f [9][n*n] (D2Q9, u = [ux..., uy...])."""
     c, _, _ = lattice_tables("D2Q9")
     f = f.reshape(9, n * n)
     rho = f.sum(axis=0)
@@ -156,6 +155,7 @@ def consistent_start(b, cases, idx, targets, steps=20, rounds=3):
     u) of each domain while keeping the non-equilibrium part f - feq(rho_f,
     u_f) the solver has built.  Solid cells keep the rest state.  Returns the
     steps spent."""
+    _, w, _ = lattice_tables("D2Q9")
     for _ in range(rounds):
         try:
             b.advance(steps)
@@ -171,8 +171,6 @@ def consistent_start(b, cases, idx, targets, steps=20, rounds=3):
             g = _feq_d2q9(rho_t, u_t, n) + (f - _feq_d2q9(rho_f, u_f, n))
             solid = case_mask(c).reshape(-1).astype(bool)
             if solid.any():
-                from . import lattice_tables
-                _, w, _ = lattice_tables("D2Q9")
                 g[:, solid] = w[:, None]
             b.set_f(j, g.reshape(-1))
     return steps * rounds

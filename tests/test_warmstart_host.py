@@ -88,3 +88,27 @@ def test_targets_and_prediction_round_trip():
     assert np.allclose(u2[: n * n][fluid], u[: n * n][fluid], rtol=1e-6, atol=1e-9)
     assert np.allclose(u2[n * n:][fluid], u[n * n:][fluid], rtol=1e-6, atol=1e-9)
     assert np.all(r2[solid] == 1.0) and np.all(u2[: n * n][solid] == 0) and np.all(u2[n * n:][solid] == 0)
+
+
+def test_consistent_start_moment_helpers():
+    """The host arithmetic of the consistent start: the D2Q9 equilibrium of
+    (rho, u) has exactly those moments (to rounding), and replacing the
+    equilibrium part of a population set keeps its non-equilibrium part while
+    its moments become the prescribed ones (what consistent_start uploads)."""
+    n = 16
+    rng = np.random.default_rng(3)
+    rho = 1 + 0.01 * rng.standard_normal(n * n)
+    u = 0.05 * rng.standard_normal(2 * n * n)
+    feq = ws._feq_d2q9(rho, u, n)
+    r2, u2 = ws._moments_d2q9(feq, n)
+    assert np.max(np.abs(r2 - rho)) < 1e-14 and np.max(np.abs(u2 - u)) < 1e-14
+    # a population set with a non-equilibrium part that carries no mass or momentum
+    c, w, _ = __import__("muphfasa_gb300").lattice_tables("D2Q9")
+    neq = 1e-3 * w[:, None] * (3 * c[:, 0:1] * c[:, 1:2]) * rng.standard_normal(n * n)[None, :]
+    f = feq + neq
+    rho_t, u_t = 1 + 0.02 * rng.standard_normal(n * n), 0.03 * rng.standard_normal(2 * n * n)
+    rf, uf = ws._moments_d2q9(f, n)
+    g = ws._feq_d2q9(rho_t, u_t, n) + (f - ws._feq_d2q9(rf, uf, n))
+    r3, u3 = ws._moments_d2q9(g, n)
+    assert np.max(np.abs(r3 - rho_t)) < 1e-13 and np.max(np.abs(u3 - u_t)) < 1e-13
+    assert np.allclose(g - ws._feq_d2q9(rho_t, u_t, n), neq, atol=1e-15)
