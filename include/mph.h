@@ -83,8 +83,11 @@ extern "C" {
  * puts every population's deviation on one scale, so the exponent needs one
  * bit less than MPH_PREC_F16C and the significand gets it.  Populations must
  * stay inside (w_i - p_i, w_i + p_i), p_i >= 0.75 w_i (|u| up to about 0.1):
- * a store that saturates makes the step report MPH_ERR_NONFINITE.  Single
- * domains and batches (the bulk-copy staged variants do not take it). */
+ * a store that saturates (in a step, mph_set_f, mph_init_fields or
+ * mph_init_fields_neq, and their batch forms) makes that call report
+ * MPH_ERR_NONFINITE; the state is kept, saturated, and the steps go on
+ * reporting it until a state within the range replaces it.  Single domains
+ * and batches (the bulk-copy staged variants do not take it). */
 #define MPH_PREC_F16W 7
 
 /* ---- lattice-unit description of one domain ---------------------------- */

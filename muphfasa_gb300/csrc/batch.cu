@@ -631,7 +631,7 @@ int mph_batch_init_fields(mph_batch* b, int domain, double* rho, double* u) {
     b->time = 0.0;
     b->has_uprev = false;
     if (!b->bad_h.empty()) b->bad_h[domain] = 0;
-    return MPH_OK;
+    return b->prec == MPH_PREC_F16W ? check_flag(b) : MPH_OK;  // saturated stores of the new state
 }
 
 int mph_batch_init_fields_neq(mph_batch* b, int domain, const double* rho, const double* u) {
@@ -650,7 +650,7 @@ int mph_batch_init_fields_neq(mph_batch* b, int domain, const double* rho, const
     b->time = 0.0;
     b->has_uprev = false;
     if (!b->bad_h.empty()) b->bad_h[domain] = 0;
-    return MPH_OK;
+    return b->prec == MPH_PREC_F16W ? check_flag(b) : MPH_OK;  // saturated stores of the new state
 }
 
 int mph_batch_advance(mph_batch* b, int nsteps) {
@@ -743,13 +743,15 @@ int mph_batch_set_f(mph_batch* b, int domain, const double* f) {
         for (int q = 0; q < b->q; ++q) {
             MPH_CK(cudaMemcpyAsync(b->d_stage, f + (size_t)q * N, sizeof(double) * N, cudaMemcpyHostToDevice,
                                    b->stream), "batch set f");
-            MPH_CK(launch_convert(b->prec, b->q, true, base, b->d_stage, q, N, b->stream), "batch convert");
+            MPH_CK(launch_convert(b->prec, b->q, true, base, b->d_stage, q, N, b->stream,
+                                  per_domain_flags(b->prec) ? b->d_flag + domain : nullptr),
+                   "batch convert");
         }
     }
     MPH_CK(cudaStreamSynchronize(b->stream), "batch set f");
     b->has_uprev = false;
     if (!b->bad_h.empty()) b->bad_h[domain] = 0;
-    return MPH_OK;
+    return b->prec == MPH_PREC_F16W ? check_flag(b) : MPH_OK;
 }
 
 int mph_batch_moments(mph_batch* b, int domain, double* rho, double* u) {

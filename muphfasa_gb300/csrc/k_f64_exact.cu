@@ -44,24 +44,36 @@ cudaError_t with_store(int prec, F&& f) {
     return cudaErrorInvalidValue;
 }
 
+// Uploads report saturating stores into flag (weight-scaled 16-bit storage).
 template <int Q, class St>
 __global__ void __launch_bounds__(256) k_convert(typename St::T* __restrict__ store, double* __restrict__ f64, int n,
-                                                 long long N, int to_store) {
+                                                 long long N, int to_store, int* flag) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
-    if (to_store) St::template st<Q>(store, n, i, N, (typename St::R)f64[i]);
-    else f64[i] = (double)St::template ld<Q>(store, n, i, N);
+    if (to_store) {
+        unsigned sat = 0;
+        st_chk<Q, St>(store, n, i, N, (typename St::R)f64[i], sat);
+        report_to<St>(flag, sat);
+    } else {
+        f64[i] = (double)St::template ld<Q>(store, n, i, N);
+    }
 }
 
 template <int Q, class St>
 __global__ void __launch_bounds__(256) k_convert_slab(typename St::T* __restrict__ store, double* __restrict__ stage,
-                                                      long long c0, long long cnt, long long N, int to_store) {
+                                                      long long c0, long long cnt, long long N, int to_store,
+                                                      int* flag) {
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= cnt) return;
     const int n = blockIdx.y;
     double* v = stage + n * cnt + j;
-    if (to_store) St::template st<Q>(store, n, c0 + j, N, (typename St::R)*v);
-    else *v = (double)St::template ld<Q>(store, n, c0 + j, N);
+    if (to_store) {
+        unsigned sat = 0;
+        st_chk<Q, St>(store, n, c0 + j, N, (typename St::R)*v, sat);
+        report_to<St>(flag, sat);
+    } else {
+        *v = (double)St::template ld<Q>(store, n, c0 + j, N);
+    }
 }
 
 __global__ void k_reduce_final(const double* __restrict__ part, int nblocks, double* __restrict__ out) {
@@ -270,21 +282,22 @@ cudaError_t launch_reduce(int prec, int q, const void* f, long long ncell, doubl
 }
 
 cudaError_t launch_convert(int prec, int q, bool to_store, void* store, double* f64, int n, long long ncell,
-                           cudaStream_t s) {
+                           cudaStream_t s, int* flag) {
     dim3 g, b;
     flat_shape(ncell, g, b);
     return with_store(prec, [&](auto st) {
         using St = decltype(st);
         return with_q(q, [&](auto qc) {
             constexpr int Q = decltype(qc)::value;
-            k_convert<Q, St><<<g, b, 0, s>>>(static_cast<typename St::T*>(store), f64, n, ncell, to_store ? 1 : 0);
+            k_convert<Q, St><<<g, b, 0, s>>>(static_cast<typename St::T*>(store), f64, n, ncell, to_store ? 1 : 0,
+                                             flag);
             return cudaGetLastError();
         });
     });
 }
 
 cudaError_t launch_convert_slab(int prec, int q, bool to_store, void* store, double* stage, long long c0,
-                                long long cnt, long long ncell, cudaStream_t s) {
+                                long long cnt, long long ncell, cudaStream_t s, int* flag) {
     if (cnt <= 0) return cudaSuccess;
     const dim3 g((unsigned)((cnt + 255) / 256), (unsigned)q, 1), b(256, 1, 1);
     return with_store(prec, [&](auto st) {
@@ -292,7 +305,7 @@ cudaError_t launch_convert_slab(int prec, int q, bool to_store, void* store, dou
         return with_q(q, [&](auto qc) {
             constexpr int Q = decltype(qc)::value;
             k_convert_slab<Q, St><<<g, b, 0, s>>>(static_cast<typename St::T*>(store), stage, c0, cnt, ncell,
-                                                  to_store ? 1 : 0);
+                                                  to_store ? 1 : 0, flag);
             return cudaGetLastError();
         });
     });

@@ -345,8 +345,8 @@ struct StF16W {
         *reinterpret_cast<unsigned*>(f + e) = f16w::encode<Q>(n, v.x, sat) | (f16w::encode<Q>(n, v.y, sat) << 16);
     }
     // FP32 population f_n = w_n + g_n for the auxiliary kernels (moments,
-    // sums, initialisation, host transfers); their stores saturate without
-    // the flag (initial states are checked by the first step's stores).
+    // sums, initialisation, host transfers); st_sat reports saturation (the
+    // initialisation and upload kernels use it through st_chk).
     template <int Q> static __device__ __forceinline__ R lde(const T* __restrict__ f, int n, unsigned e) {
         return ldr1<Q>(n, f, e) + (float)Lat<Q>::w(n);
     }
@@ -359,6 +359,10 @@ struct StF16W {
     }
     template <int Q> static __device__ __forceinline__ void st(T* __restrict__ f, int n, long long i, long long N, R v) {
         unsigned sat = 0;
+        f[n * N + i] = (unsigned short)f16w::encode<Q>(n, v - (float)Lat<Q>::w(n), sat);
+    }
+    template <int Q>
+    static __device__ __forceinline__ void st_sat(T* __restrict__ f, int n, long long i, long long N, R v, unsigned& sat) {
         f[n * N + i] = (unsigned short)f16w::encode<Q>(n, v - (float)Lat<Q>::w(n), sat);
     }
     template <int Q> static __device__ __forceinline__ R rt(int n, R v) {
@@ -394,6 +398,21 @@ template <class St>
 __device__ __forceinline__ void sh_report(const KParams& p, unsigned sat) {
     if constexpr (St::kRange) {
         if (sat > 0x7FFFu) atomicOr(p.flag, 4);
+    }
+}
+// Store of population value v (compute type R) by the auxiliary kernels, with
+// the saturation report of the policies whose stores can saturate; flag may
+// be null (then saturation is not reported).
+template <int Q, class St>
+__device__ __forceinline__ void st_chk(typename St::T* __restrict__ f, int n, long long i, long long N,
+                                       typename St::R v, unsigned& sat) {
+    if constexpr (St::kRange) St::template st_sat<Q>(f, n, i, N, v, sat);
+    else St::template st<Q>(f, n, i, N, v);
+}
+template <class St>
+__device__ __forceinline__ void report_to(int* flag, unsigned sat) {
+    if constexpr (St::kRange) {
+        if (flag && sat > 0x7FFFu) atomicOr(flag, 4);
     }
 }
 
@@ -1060,12 +1079,14 @@ __global__ void __launch_bounds__(256) k_init(typename St::T* __restrict__ fout,
         for (int d = 0; d < L::D; ++d) u[d] = u[d] - 0.5 * p.F[d] / rho;
     const double usq = (L::D == 2) ? u[0] * u[0] + u[1] * u[1] : u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
     double f[Q];
+    unsigned sat = 0;
 #pragma unroll
     for (int n = 0; n < Q; ++n) {
         const double cu = (n == 0) ? 0.0 : cdot<Q, double>(n, u);
         f[n] = L::w(n) * rho * (1 + 3.0 * cu + 4.5 * cu * cu - 1.5 * usq);
-        St::template st<Q>(fout, n, c, p.ncell, (typename St::R)f[n]);
+        st_chk<Q, St>(fout, n, c, p.ncell, (typename St::R)f[n], sat);
     }
+    report_to<St>(p.flag, sat);
     if (FORCED) {
         // moments of the stored values (as a reload would return them; the
         // read-only cache path must not re-read memory this kernel wrote)
@@ -1129,6 +1150,7 @@ __global__ void __launch_bounds__(256) k_init_neq(typename St::T* __restrict__ f
     const double tau = 1.0 / p.omega;
     const double usq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
     const double divu = G[0][0] + G[1][1] + G[2][2];
+    unsigned sat = 0;
 #pragma unroll
     for (int n = 0; n < Q; ++n) {
         const double cu = cdot<Q, double>(n, u);
@@ -1138,8 +1160,9 @@ __global__ void __launch_bounds__(256) k_init_neq(typename St::T* __restrict__ f
         for (int a = 0; a < L::D; ++a)
             for (int b = 0; b < L::D; ++b) cc += cv[a] * cv[b] * G[a][b];
         const double neq = -3.0 * (tau - 1.0) * L::w(n) * rho * (cc - divu / 3.0);
-        St::template st<Q>(fout, n, c, N, (typename St::R)(feq + neq));
+        st_chk<Q, St>(fout, n, c, N, (typename St::R)(feq + neq), sat);
     }
+    report_to<St>(p.flag, sat);
 }
 
 // FP64 sums of the stored populations: block partials (mass, jx, jy, jz)

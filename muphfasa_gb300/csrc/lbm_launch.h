@@ -42,12 +42,14 @@ cudaError_t launch_reduce(int prec, int q, const void* f, long long ncell, doubl
 // (warm start, unforced domains).
 cudaError_t launch_init_neq(int prec, int q, void* f, const double* rho, const double* u, const KParams& p,
                             cudaStream_t s);
+// Uploads (to_store) OR 4 into *flag when a store saturates (weight-scaled
+// 16-bit storage; flag may be null).
 cudaError_t launch_convert(int prec, int q, bool to_store, void* store, double* f64, int n, long long ncell,
-                           cudaStream_t s);
+                           cudaStream_t s, int* flag = nullptr);
 // All Q populations of the cells [c0, c0 + cnt) between the store and an FP64
 // staging block laid out [q][cnt].
 cudaError_t launch_convert_slab(int prec, int q, bool to_store, void* store, double* stage, long long c0,
-                                long long cnt, long long ncell, cudaStream_t s);
+                                long long cnt, long long ncell, cudaStream_t s, int* flag = nullptr);
 
 struct A4 {
     double* p;

@@ -381,7 +381,8 @@ int check_flag(mph_sim* s) {
                                   "(the step's results are incomplete)");
     }
     if (flag & 4) return fail(MPH_ERR_NONFINITE, "weight-scaled 16-bit storage: a population deviation "
-                                                   "|f - w| reached 2 w and saturated (or was not finite)");
+                                                   "|f - w| reached the format's range p (p the power of two "
+                                                   "nearest to w) and saturated, or was not finite");
     if (flag) return fail(MPH_ERR_NONFINITE, "fixed-point step: a cell left the representable range "
                                                "(rho outside (1/16, 64) or |J|, |u| >= 4)");
     return MPH_OK;
@@ -471,7 +472,8 @@ int upload(mph_sim* s, const double* f) {
                "upload f");
         MPH_CK(cudaEventRecord(s->ev_copied[b], s->copy_stream), "upload order");
         MPH_CK(cudaStreamWaitEvent(s->stream, s->ev_copied[b], 0), "upload order");
-        MPH_CK(launch_convert(s->d.precision, s->d.q, true, s->fa, st, q, s->kp.ncell, s->stream), "convert f");
+        MPH_CK(launch_convert(s->d.precision, s->d.q, true, s->fa, st, q, s->kp.ncell, s->stream, s->d_flag),
+               "convert f");
         MPH_CK(cudaEventRecord(s->ev_converted[b], s->stream), "upload order");
     }
     return MPH_OK;
@@ -603,7 +605,8 @@ int slab_up(mph_sim* s, const double* f, int k, int S, int b) {
     if ((rc = copy_rows(s, st, cnt, f + c0, N, cnt, cudaMemcpyHostToDevice, s->copy_stream))) return rc;
     MPH_CK(cudaEventRecord(copied, s->copy_stream), "upload order");
     MPH_CK(cudaStreamWaitEvent(s->stream, copied, 0), "upload order");
-    MPH_CK(launch_convert_slab(s->d.precision, s->d.q, true, s->fa, st, c0, cnt, N, s->stream), "convert slab");
+    MPH_CK(launch_convert_slab(s->d.precision, s->d.q, true, s->fa, st, c0, cnt, N, s->stream, s->d_flag),
+           "convert slab");
     MPH_CK(cudaEventRecord(freed, s->stream), "upload order");
     return MPH_OK;
 }
@@ -848,7 +851,11 @@ int mph_set_f(mph_sim* s, const double* f) {
     if (rc) return rc;
     s->has_state = true;
     s->has_uprev = false;
-    return sync(s, "mph_set_f");
+    rc = sync(s, "mph_set_f");
+    // a weight-scaled 16-bit store that saturated is reported here (and by
+    // the steps, until a new state replaces this one)
+    if (!rc && s->d.precision == MPH_PREC_F16W) rc = check_flag(s);
+    return rc;
 }
 
 int mph_get_f(mph_sim* s, double* f) {
@@ -875,7 +882,9 @@ int mph_init_fields(mph_sim* s, double* rho, double* u) {
     s->has_state = true;
     s->has_uprev = false;
     s->time = 0.0;
-    return sync(s, "mph_init_fields");
+    rc = sync(s, "mph_init_fields");
+    if (!rc && s->d.precision == MPH_PREC_F16W) rc = check_flag(s);
+    return rc;
 }
 
 int mph_init_fields_neq(mph_sim* s, const double* rho, const double* u) {
@@ -891,7 +900,9 @@ int mph_init_fields_neq(mph_sim* s, const double* rho, const double* u) {
     s->has_state = true;
     s->has_uprev = false;
     s->time = 0.0;
-    return sync(s, "mph_init_fields_neq");
+    rc = sync(s, "mph_init_fields_neq");
+    if (!rc && s->d.precision == MPH_PREC_F16W) rc = check_flag(s);
+    return rc;
 }
 
 int mph_advance(mph_sim* s, int nsteps) {

@@ -63,7 +63,9 @@ def test_f16w_storage_bits_and_values(mph):
     x[:64] = 0.0
     x[64:128] = (1.0 + (2 * np.arange(64) + 1) / 8192.0) * np.exp2(rng.integers(-7, 0, 64))
     f = W + P * x
-    s.set_f(f)
+    with pytest.raises(mph.MphError) as e:  # the saturating values are reported, and stored saturated
+        s.set_f(f)
+    assert e.value.code == 6
     nbytes = 2 * 9 * N
     raw = np.empty(nbytes, np.uint8)
     mph.check(mph.lib().mph_get_state(s._h, raw.ctypes.data, nbytes))
@@ -89,6 +91,32 @@ def test_f16w_storage_bits_and_values(mph):
     # half a unit of the 13-bit significand or of the subnormal step
     lim = np.where(normal, np.abs(xr) * 2.0 ** -13, 2.0 ** -20)
     assert np.all(err[fin] <= lim[fin])
+
+
+def test_f16w_saturating_upload_and_init_report_nonfinite(mph):
+    """Populations outside the format's range are reported where they are
+    stored: mph_set_f and mph_init_fields return MPH_ERR_NONFINITE (the state
+    is kept, saturated), the steps keep reporting it, and a state within the
+    range clears it."""
+    n = (32, 16)
+    N = n[0] * n[1]
+    s = _sim(mph, n=n, faces=["Periodic"] * 6)
+    _, w, _ = mph.lattice_tables("D2Q9")
+    f = np.repeat(w, N).copy()
+    f[N + 5] = 2.5 * w[1]          # (f - w) / p = 1.33: beyond the largest value
+    with pytest.raises(mph.MphError) as e:
+        s.set_f(f)
+    assert e.value.code == 6
+    with pytest.raises(mph.MphError) as e:
+        s.advance(1)
+    assert e.value.code == 6
+    s.set_f(np.repeat(w, N))
+    s.advance(2)
+    with pytest.raises(mph.MphError) as e:  # u = 0.5 along x: (f - w) / p of the population along it is 2.0
+        s.initialize(np.ones(N), np.concatenate([np.full(N, 0.5), np.zeros(N)]))
+    assert e.value.code == 6
+    s.initialize(np.ones(N), np.zeros(2 * N))
+    s.advance(2)
 
 
 def test_f16w_saturating_step_reports_nonfinite(mph):
@@ -163,3 +191,11 @@ def test_f16w_batch_flags_the_saturating_domain(mph):
         assert np.array_equal(b.f(d), s.f())
     b.initialize(1, np.ones(N), np.zeros(2 * N))
     assert not b.range_flags().any()
+    # an upload outside the range names its domain too
+    _, w, _ = mph.lattice_tables("D2Q9")
+    f = np.repeat(w, N).copy()
+    f[3] = 3.0 * w[0]
+    with pytest.raises(mph.MphError) as e:
+        b.set_f(2, f)
+    assert e.value.code == 6
+    assert list(b.range_flags()) == [False, False, True]
