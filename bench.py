@@ -784,7 +784,7 @@ def main():
         e2e = {"value": None, "unit": "MLUPS", "error": str(ex)[:200]}
 
     # Secondary record: the 512-cavity batch (FP32, 40 steps), timed in the
-    # same run so its roofline fraction is on the driver's record.
+    # same run so its roofline fraction travels with the headline line.
     secondary = None
     if rank == 0 and args.secondary_steps > 0:
         try:
