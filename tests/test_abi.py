@@ -64,3 +64,34 @@ def test_no_cpu_fallback_without_a_device(mph):
     with pytest.raises(mph.MphError) as e:
         mph.Simulation(mph.make_desc("D2Q9", (8, 8), 1.0))
     assert e.value.code == 3
+
+
+@pytest.mark.parametrize("name", ["f64", "f64_fast", "f32", "f16s", "bf16s", "f64x", "f16c", "f16w"])
+def test_every_precision_name_is_a_known_storage(name, mph):
+    """Every precision name maps to a storage the library knows: without a
+    device, creating a single handle or a batch in it gets as far as the first
+    CUDA call (MPH_ERR_CUDA), while an unknown precision code is rejected
+    before it (MPH_ERR_ARG / MPH_ERR_UNSUPPORTED)."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    d = mph.make_desc("D2Q9", (8, 8), 1.0, precision=name)
+    assert d.precision == mph.PRECISION[name]
+    with pytest.raises(mph.MphError) as e:
+        mph.Simulation(d)
+    assert e.value.code == 3
+    with pytest.raises(mph.MphError) as e:
+        mph.Batch([d])
+    assert e.value.code == 3
+
+
+def test_unknown_precision_codes_are_rejected_before_the_device(mph):
+    d = mph.make_desc("D2Q9", (8, 8), 1.0)
+    for code in (-1, len(mph.PRECISION), 99):
+        d.precision = code
+        with pytest.raises(mph.MphError) as e:
+            mph.Simulation(d)
+        assert e.value.code == 1
+        with pytest.raises(mph.MphError) as e:
+            mph.Batch([d])
+        assert e.value.code == 4
